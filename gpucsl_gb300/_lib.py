@@ -1,0 +1,143 @@
+"""ctypes binding of libgpucsl_gb300.so (the C ABI declared in include/gpucsl_gb300.h).
+
+There is no fallback: if the shared library is missing or no CUDA device is present,
+every call raises.  Device buffers are torch tensors; their data pointers and the
+current torch stream are handed to the C ABI.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+from functools import lru_cache
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libgpucsl_gb300.so"
+
+GCSL_OK = 0
+GCSL_ERR_INVALID_ARG = 1
+GCSL_ERR_WORKSPACE = 2
+GCSL_ERR_UNSUPPORTED_LEVEL = 3
+GCSL_ERR_TIMEOUT = 4
+GCSL_ERR_DEVICE = 5
+GCSL_ERR_CAPACITY = 6
+GCSL_ERR_UNSUPPORTED = 7
+GCSL_MAX_LEVELS = 64
+GCSL_DTYPE_F64 = 0
+GCSL_DTYPE_F32 = 1
+
+# every symbol the header declares (checked by the CPU test-suite)
+EXPORTED = [
+    "gcsl_version", "gcsl_status_string",
+    "gcsl_corr_workspace_bytes", "gcsl_corr_f64",
+    "gcsl_gauss_workspace_bytes", "gcsl_gauss_skeleton",
+    "gcsl_disc_workspace_bytes", "gcsl_disc_skeleton",
+    "gcsl_compact", "gcsl_unrank", "gcsl_pchisq", "gcsl_disc_table",
+]
+
+
+class GcslStats(ct.Structure):
+    _fields_ = [
+        ("levels_run", ct.c_int32),
+        ("status", ct.c_int32),
+        ("n_records", ct.c_int64),
+        ("edges", ct.c_int64 * GCSL_MAX_LEVELS),
+        ("tests", ct.c_int64 * GCSL_MAX_LEVELS),
+        ("tests_full", ct.c_int64 * GCSL_MAX_LEVELS),
+        ("removed", ct.c_int64 * GCSL_MAX_LEVELS),
+        ("max_degree", ct.c_int32 * GCSL_MAX_LEVELS),
+        ("level_ms", ct.c_float * GCSL_MAX_LEVELS),
+    ]
+
+    def as_dict(self) -> dict:
+        n = max(int(self.levels_run), 0)
+        return {
+            "levels_run": n,
+            "status": int(self.status),
+            "n_records": int(self.n_records),
+            "edges": [int(x) for x in self.edges[:n]],
+            "tests": [int(x) for x in self.tests[:n]],
+            "tests_full": [int(x) for x in self.tests_full[:n]],
+            "removed": [int(x) for x in self.removed[:n]],
+            "max_degree": [int(x) for x in self.max_degree[:n]],
+        }
+
+
+class GcslError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        self.code = code
+        super().__init__(f"{what}: {status_string(code)} (status {code})")
+
+
+_vp = ct.c_void_p
+_i32 = ct.c_int32
+_i64 = ct.c_int64
+_sz = ct.c_size_t
+_dbl = ct.c_double
+
+
+@lru_cache(maxsize=1)
+def lib() -> ct.CDLL:
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            f"{LIB_PATH.name} is not built; run `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(requires nvcc) before using gpucsl_gb300")
+    L = ct.CDLL(str(LIB_PATH))
+    L.gcsl_version.restype = ct.c_int
+    L.gcsl_version.argtypes = []
+    L.gcsl_status_string.restype = ct.c_char_p
+    L.gcsl_status_string.argtypes = [ct.c_int]
+    L.gcsl_corr_workspace_bytes.restype = _sz
+    L.gcsl_corr_workspace_bytes.argtypes = [_i64, _i32]
+    L.gcsl_corr_f64.restype = ct.c_int
+    L.gcsl_corr_f64.argtypes = [_vp, _i32, _i64, _i32, _i64, _vp, _vp, _sz, _vp]
+    L.gcsl_gauss_workspace_bytes.restype = _sz
+    L.gcsl_gauss_workspace_bytes.argtypes = [_i32, _i32]
+    L.gcsl_gauss_skeleton.restype = ct.c_int
+    L.gcsl_gauss_skeleton.argtypes = [_vp, _i32, _i64, ct.POINTER(_dbl), _i32, _i32, _vp, _vp, _vp, _i64, _vp,
+                                      ct.POINTER(GcslStats), _vp, _sz, _vp]
+    L.gcsl_disc_workspace_bytes.restype = _sz
+    L.gcsl_disc_workspace_bytes.argtypes = [_i32, _i64, _i32, _i32]
+    L.gcsl_disc_skeleton.restype = ct.c_int
+    L.gcsl_disc_skeleton.argtypes = [_vp, _i64, _i64, _i32, _vp, _i32, _dbl, _i32, _vp, _vp, _vp, _i64, _vp,
+                                     ct.POINTER(GcslStats), _vp, _sz, _vp]
+    L.gcsl_compact.restype = ct.c_int
+    L.gcsl_compact.argtypes = [_vp, _i32, _vp, _vp]
+    L.gcsl_unrank.restype = ct.c_int
+    L.gcsl_unrank.argtypes = [_i32, _i32, _i64, _vp, _vp]
+    L.gcsl_pchisq.restype = ct.c_int
+    L.gcsl_pchisq.argtypes = [_vp, _vp, _i64, _vp, _vp]
+    L.gcsl_disc_table.restype = ct.c_int
+    L.gcsl_disc_table.argtypes = [_vp, _i64, _i64, _vp, _i32, _i32, ct.POINTER(_i32), _i32, _vp, _vp, _vp]
+    if L.gcsl_version() != 1:
+        raise RuntimeError("libgpucsl_gb300.so ABI version mismatch")
+    return L
+
+
+def status_string(code: int) -> str:
+    try:
+        return lib().gcsl_status_string(int(code)).decode()
+    except Exception:  # library not loadable: plain code
+        return f"status {code}"
+
+
+def check(code: int, what: str) -> None:
+    if code != GCSL_OK:
+        raise GcslError(code, what)
+
+
+def require_cuda():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("gpucsl_gb300 needs a CUDA device (sm_103a); none is available")
+    return torch
+
+
+def stream_ptr(stream=None) -> int:
+    torch = require_cuda()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+def ptr(t) -> int | None:
+    return None if t is None else int(t.data_ptr())

@@ -1,0 +1,307 @@
+// extern "C" entry points of libgpucsl_gb300.so and the host side of the level loops.
+//
+// The level loop of the reference (discover_skeleton_gaussian.py:60-108,
+// discover_skeleton_discrete.py:80-112) synchronises the host once per level to read
+// the maximum degree.  Here every level kernel reads the termination test from the
+// device state itself, so levels are enqueued back to back in growing batches and the
+// host only checks the sticky `done` flag between batches; levels enqueued past the
+// end return at their first instruction.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+namespace gcsl {
+namespace host {
+cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, DevState *st,
+                          cudaStream_t s);
+cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s);
+cudaError_t launch_scan_int(const int *cnt, int p, long long *prefix, DevState *st, cudaStream_t s);
+cudaError_t launch_scan_ll(const long long *cnt, int p, long long *prefix, DevState *st, cudaStream_t s);
+cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, const int *up, const long long *prefix,
+                               double tau, bool tau_valid, uint16_t *G, double *zmin, int *sep_dense, int max_level,
+                               int *rec_pool, long long rec_cap, DevState *st, int num_sms, cudaStream_t s);
+cudaError_t launch_pmax(const double *zmin, int p, long long n_obs, double *pmax, int num_sms, cudaStream_t s);
+size_t corr_workspace_bytes(long long n, int p);
+cudaError_t corr_f64(const void *X, int dtype, long long n, int p, long long ldx, double *C, void *ws,
+                     size_t ws_bytes, int num_sms, cudaStream_t s);
+int disc_table_cap(int device);
+cudaError_t launch_disc_tests(const DiscLevelArgs &A, int num_sms, cudaStream_t s);
+cudaError_t launch_disc_weights(const int *adj, int p, int L, long long *w, DevState *st, cudaStream_t s);
+cudaError_t launch_disc_finalize(const int *adj, int p, int L, uint16_t *G, unsigned long long *win, int *sep,
+                                 int max_level, int *rec, long long rec_cap, DevState *st, int num_sms,
+                                 cudaStream_t s);
+cudaError_t launch_disc_level_stats(const long long *prefix, const int *adj, int p, int L, DevState *st,
+                                    cudaStream_t s);
+cudaError_t launch_pmax_finish(double *pmax, int p, int num_sms, cudaStream_t s);
+cudaError_t launch_disc_table(const uint8_t *data, long long ld, long long n, const uint8_t *dims, int vi, int vj,
+                              const int *S, int L, int table_cap, uint32_t *counts, double *out2, cudaStream_t s);
+cudaError_t launch_pchisq(const double *x, const long long *df, long long count, double *out, cudaStream_t s);
+cudaError_t launch_unrank(int K, int L, long long count, int *out, cudaStream_t s);
+}  // namespace host
+}  // namespace gcsl
+
+using namespace gcsl;
+
+namespace {
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+struct Carver {
+    char *base;
+    size_t off = 0, cap;
+    Carver(void *b, size_t c) : base(static_cast<char *>(b)), cap(c) {}
+    template <typename T>
+    T *take(size_t count) {
+        T *p = reinterpret_cast<T *>(base ? base + off : nullptr);
+        off = align_up(off + count * sizeof(T));
+        return p;
+    }
+};
+
+int device_sms() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
+int map_cuda(cudaError_t e) { return e == cudaSuccess ? GCSL_OK : GCSL_ERR_DEVICE; }
+
+// Copy the device state into the public stats struct.
+int finish_stats(const DevState *d_st, gcsl_stats *stats, cudaStream_t s, bool discrete_edges, long long p) {
+    DevState h;
+    cudaError_t e = cudaMemcpyAsync(&h, d_st, sizeof(DevState), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return GCSL_ERR_DEVICE;
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->levels_run = h.last_level + 1;
+        stats->status = h.status;
+        stats->n_records = (int64_t)h.n_rec_ints;
+        for (int l = 0; l < GCSL_MAX_LEVELS; ++l) {
+            stats->edges[l] = (int64_t)(discrete_edges ? h.edges[l] / 2 : h.edges[l]);
+            stats->tests[l] = (int64_t)h.tests[l];
+            stats->tests_full[l] = (int64_t)h.tests_full[l];
+            stats->removed[l] = (int64_t)h.removed[l];
+            stats->max_degree[l] = h.max_degree[l];
+        }
+        const long long pairs = p * (p - 1) / 2;
+        stats->edges[0] = pairs;
+        stats->tests[0] = pairs;
+        stats->tests_full[0] = pairs;
+    }
+    return h.status;
+}
+
+// Run levels 1..max_level with the given per-level enqueue function, checking the
+// sticky done flag between batches of 1, 2, 4, then 8 levels.
+template <typename EnqueueLevel>
+int run_levels(int max_level, DevState *d_st, cudaStream_t s, EnqueueLevel enqueue) {
+    int level = 1, batch = 1;
+    const int last = std::min(max_level, GCSL_MAX_LEVELS - 1);
+    while (level <= last) {
+        for (int b = 0; b < batch && level <= last; ++b, ++level) {
+            cudaError_t e = enqueue(level);
+            if (e != cudaSuccess) return GCSL_ERR_DEVICE;
+        }
+        if (level > last) break;
+        int32_t done = 0;
+        cudaError_t e = cudaMemcpyAsync(&done, &d_st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return GCSL_ERR_DEVICE;
+        if (done) break;
+        batch = std::min(batch * 2, 8);
+    }
+    if (max_level >= GCSL_MAX_LEVELS) {
+        // levels beyond the state arrays: only an error if the loop had not finished
+        int32_t done = 0;
+        cudaMemcpyAsync(&done, &d_st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        if (!done) return GCSL_ERR_UNSUPPORTED_LEVEL;
+    }
+    return GCSL_OK;
+}
+
+struct GaussWs {
+    DevState *st;
+    int *adj, *up;
+    long long *prefix;
+    double *zmin;
+    size_t bytes;
+};
+
+GaussWs carve_gauss(void *ws, size_t cap, int p) {
+    Carver c(ws, cap);
+    GaussWs w;
+    w.st = c.take<DevState>(1);
+    w.adj = c.take<int>((size_t)p * p);
+    w.up = c.take<int>((size_t)p);
+    w.prefix = c.take<long long>((size_t)p + 1);
+    w.zmin = c.take<double>((size_t)p * p);
+    w.bytes = c.off;
+    return w;
+}
+
+struct DiscWs {
+    DevState *st;
+    int *adj;
+    long long *weights, *prefix;
+    unsigned long long *win;
+    size_t bytes;
+};
+
+DiscWs carve_disc(void *ws, size_t cap, int p) {
+    Carver c(ws, cap);
+    DiscWs w;
+    w.st = c.take<DevState>(1);
+    w.adj = c.take<int>((size_t)p * p);
+    w.weights = c.take<long long>((size_t)p);
+    w.prefix = c.take<long long>((size_t)p + 1);
+    w.win = c.take<unsigned long long>((size_t)p * p);
+    w.bytes = c.off;
+    return w;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gcsl_version(void) { return GCSL_ABI_VERSION; }
+
+const char *gcsl_status_string(int status) {
+    switch (status) {
+    case GCSL_OK: return "ok";
+    case GCSL_ERR_INVALID_ARG: return "invalid argument";
+    case GCSL_ERR_WORKSPACE: return "workspace too small";
+    case GCSL_ERR_UNSUPPORTED_LEVEL: return "level beyond the supported range (no threshold or state slot)";
+    case GCSL_ERR_TIMEOUT: return "device wait timed out";
+    case GCSL_ERR_DEVICE: return "CUDA error";
+    case GCSL_ERR_CAPACITY: return "sepset record pool too small";
+    case GCSL_ERR_UNSUPPORTED: return "unsupported problem size";
+    default: return "unknown status";
+    }
+}
+
+size_t gcsl_corr_workspace_bytes(int64_t n, int32_t p) { return host::corr_workspace_bytes(n, p); }
+
+int gcsl_corr_f64(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ldx, double *C, void *workspace,
+                  size_t workspace_bytes, void *stream) {
+    if (!X || !C || n < 2 || p < 1 || ldx < p || (dtype != GCSL_DTYPE_F64 && dtype != GCSL_DTYPE_F32))
+        return GCSL_ERR_INVALID_ARG;
+    if (!workspace || workspace_bytes < host::corr_workspace_bytes(n, p)) return GCSL_ERR_WORKSPACE;
+    return map_cuda(host::corr_f64(X, dtype, n, p, ldx, C, workspace, workspace_bytes, device_sms(),
+                                   static_cast<cudaStream_t>(stream)));
+}
+
+size_t gcsl_gauss_workspace_bytes(int32_t p, int32_t max_level) {
+    (void)max_level;
+    return carve_gauss(nullptr, 0, p).bytes;
+}
+
+int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double *thresholds, int32_t n_thresholds,
+                        int32_t max_level, uint16_t *G, int32_t *sepsets, int32_t *rec_pool, int64_t rec_cap,
+                        double *pmax, gcsl_stats *stats, void *workspace, size_t workspace_bytes, void *stream) {
+    if (!C || !G || !pmax || p < 1 || n_obs < 4 || !thresholds || n_thresholds < 1 || max_level < 0)
+        return GCSL_ERR_INVALID_ARG;
+    if (rec_pool == nullptr) rec_cap = 0;
+    GaussWs w = carve_gauss(workspace, workspace_bytes, p);
+    if (!workspace || w.bytes > workspace_bytes) return GCSL_ERR_WORKSPACE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int sms = device_sms();
+    if (cudaMemsetAsync(w.st, 0, sizeof(DevState), s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    if (host::launch_level0(C, p, thresholds[0], G, w.zmin, w.st, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    int rc = run_levels(max_level, w.st, s, [&](int level) -> cudaError_t {
+        cudaError_t e = host::launch_compact(G, p, w.adj, w.up, w.st, level, s);
+        if (e == cudaSuccess) e = host::launch_scan_int(w.up, p, w.prefix, w.st, s);
+        const bool tau_valid = level < n_thresholds;
+        const double tau = tau_valid ? thresholds[level] : 0.0;
+        if (e == cudaSuccess)
+            e = host::launch_gauss_level(level, C, p, w.adj, w.up, w.prefix, tau, tau_valid, G, w.zmin, sepsets,
+                                         max_level, rec_pool, rec_cap, w.st, sms, s);
+        return e;
+    });
+    if (rc != GCSL_OK) return rc;
+    if (host::launch_pmax(w.zmin, p, n_obs, pmax, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    return finish_stats(w.st, stats, s, false, p);
+}
+
+size_t gcsl_disc_workspace_bytes(int32_t p, int64_t n, int32_t max_level, int32_t max_dim) {
+    (void)n;
+    (void)max_level;
+    (void)max_dim;
+    return carve_disc(nullptr, 0, p).bytes;
+}
+
+int gcsl_disc_skeleton(const uint8_t *data, int64_t ld, int64_t n, int32_t p, const uint8_t *dims, int32_t max_dim,
+                       double alpha, int32_t max_level, uint16_t *G, int32_t *sepsets, int32_t *rec_pool,
+                       int64_t rec_cap, double *pmax, gcsl_stats *stats, void *workspace, size_t workspace_bytes,
+                       void *stream) {
+    if (!data || !dims || !G || !pmax || p < 1 || n < 1 || ld < n || (ld % 16) != 0 || max_level < 0 ||
+        max_dim < 1 || max_dim > 255 || reinterpret_cast<uintptr_t>(data) % 16 != 0)
+        return GCSL_ERR_INVALID_ARG;
+    if (rec_pool == nullptr) rec_cap = 0;
+    DiscWs w = carve_disc(workspace, workspace_bytes, p);
+    if (!workspace || w.bytes > workspace_bytes) return GCSL_ERR_WORKSPACE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int sms = device_sms();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int cap = host::disc_table_cap(dev);
+    if ((long long)max_dim * max_dim > cap) return GCSL_ERR_UNSUPPORTED;
+    cudaError_t e = cudaMemsetAsync(w.st, 0, sizeof(DevState), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.win, 0xff, sizeof(unsigned long long) * (size_t)p * p, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(pmax, 0, sizeof(double) * (size_t)p * p, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(G, 0, sizeof(uint16_t) * (size_t)p * p, s);
+    if (e != cudaSuccess) return GCSL_ERR_DEVICE;
+    DiscLevelArgs A{data, ld, n, p, dims, alpha, 0, w.adj, w.prefix, G, pmax, w.win, cap, w.st};
+    if (host::launch_disc_tests(A, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    int rc = run_levels(max_level, w.st, s, [&](int level) -> cudaError_t {
+        cudaError_t e2 = host::launch_compact(G, p, w.adj, nullptr, w.st, level, s);
+        if (e2 == cudaSuccess) e2 = host::launch_disc_weights(w.adj, p, level, w.weights, w.st, s);
+        if (e2 == cudaSuccess) e2 = host::launch_scan_ll(w.weights, p, w.prefix, w.st, s);
+        if (e2 == cudaSuccess) e2 = host::launch_disc_level_stats(w.prefix, w.adj, p, level, w.st, s);
+        DiscLevelArgs B = A;
+        B.level = level;
+        if (e2 == cudaSuccess) e2 = host::launch_disc_tests(B, sms, s);
+        if (e2 == cudaSuccess)
+            e2 = host::launch_disc_finalize(w.adj, p, level, G, w.win, sepsets, max_level, rec_pool, rec_cap, w.st,
+                                            sms, s);
+        return e2;
+    });
+    if (rc != GCSL_OK) return rc;
+    if (host::launch_pmax_finish(pmax, p, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    return finish_stats(w.st, stats, s, true, p);
+}
+
+int gcsl_compact(const uint16_t *G, int32_t p, int32_t *adj, void *stream) {
+    if (!G || !adj || p < 1) return GCSL_ERR_INVALID_ARG;
+    return map_cuda(host::launch_compact(G, p, adj, nullptr, nullptr, 0, static_cast<cudaStream_t>(stream)));
+}
+
+int gcsl_unrank(int32_t K, int32_t level, int64_t count, int32_t *out, void *stream) {
+    if (!out || K < 0 || level < 1 || level >= GCSL_MAX_LEVELS || count < 0) return GCSL_ERR_INVALID_ARG;
+    return map_cuda(host::launch_unrank(K, level, count, out, static_cast<cudaStream_t>(stream)));
+}
+
+int gcsl_pchisq(const double *x, const int64_t *df, int64_t count, double *out, void *stream) {
+    if (!x || !df || !out || count < 0) return GCSL_ERR_INVALID_ARG;
+    return map_cuda(host::launch_pchisq(x, reinterpret_cast<const long long *>(df), count, out,
+                                        static_cast<cudaStream_t>(stream)));
+}
+
+int gcsl_disc_table(const uint8_t *data, int64_t ld, int64_t n, const uint8_t *dims, int32_t vi, int32_t vj,
+                    const int32_t *S, int32_t level, uint32_t *counts, double *chi2_pvalue, void *stream) {
+    if (!data || !dims || !counts || !chi2_pvalue || n < 1 || ld < n || (ld % 16) != 0 || level < 0 ||
+        level >= GCSL_MAX_LEVELS || (level > 0 && !S) || reinterpret_cast<uintptr_t>(data) % 16 != 0)
+        return GCSL_ERR_INVALID_ARG;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return map_cuda(host::launch_disc_table(data, ld, n, dims, vi, vj, S, level, host::disc_table_cap(dev), counts,
+                                            chi2_pvalue, static_cast<cudaStream_t>(stream)));
+}
+
+}  // extern "C"

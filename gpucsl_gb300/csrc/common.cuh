@@ -1,0 +1,162 @@
+// Shared device helpers of the skeleton-discovery kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gpucsl_gb300.h"
+
+#define GCSL_WARP 32
+#define GCSL_FULL_MASK 0xffffffffu
+#define GCSL_KEY_NONE 0xffffffffffffffffull
+// Largest conditioning-set size with a register-resident Gaussian test; larger
+// levels run the shared-memory kernel.
+#define GCSL_GAUSS_REG_LEVELS 8
+// Ranks per direction must stay below this bound (keys are rank << 1 | dir).
+#define GCSL_RANK_LIMIT (1ll << 56)
+
+namespace gcsl {
+
+// Device-side state of one skeleton solve.  Per-level slots are written once per
+// level, so no counter has to be reset between levels.
+struct DevState {
+    int32_t status;                          // first error code seen on the device
+    int32_t done;                            // level loop finished (sticky)
+    int32_t last_level;                      // highest level whose tests ran
+    int32_t pad;
+    int32_t max_degree[GCSL_MAX_LEVELS];     // max compacted degree at level start
+    unsigned long long edges[GCSL_MAX_LEVELS];
+    unsigned long long tests[GCSL_MAX_LEVELS];
+    unsigned long long tests_full[GCSL_MAX_LEVELS];
+    unsigned long long removed[GCSL_MAX_LEVELS];
+    unsigned long long n_rec_ints;           // ints used in the record pool
+};
+
+// Arguments of one discrete test-kernel launch.
+struct DiscLevelArgs {
+    const uint8_t *data;      // column-major codes, column stride ld
+    long long ld, n;
+    int p;
+    const uint8_t *dims;
+    double alpha;
+    int level;
+    const int *adj;
+    const long long *prefix;  // per-row weighted prefix of the flattened test list
+    uint16_t *G;
+    double *pmax;
+    unsigned long long *win;  // canonical remover key per (lo, hi)
+    int table_cap;            // max counters of one table copy in shared memory
+    DevState *st;
+};
+
+__device__ __forceinline__ void set_status(DevState *st, int code) { atomicCAS(&st->status, 0, code); }
+
+// C(n, k) for small k by the exact multiplicative recurrence; k is bounded by KMAX
+// so the divisors are compile-time constants after unrolling.
+template <int KMAX>
+__device__ __forceinline__ long long binom_small(long long n, int k) {
+    if (k < 0 || n < k) return 0;
+    unsigned long long r = 1;
+#pragma unroll
+    for (int i = 0; i < KMAX; ++i) {
+        if (i < k) r = r * (unsigned long long)(n - i) / (unsigned long long)(i + 1);
+    }
+    return (long long)r;
+}
+
+// C(n, k), general k (runtime loop).
+__device__ __forceinline__ long long binom_rt(long long n, int k) {
+    if (k < 0 || n < k) return 0;
+    if (k > n - k) k = (int)(n - k);
+    unsigned long long r = 1;
+    for (int i = 0; i < k; ++i) r = r * (unsigned long long)(n - i) / (unsigned long long)(i + 1);
+    return (long long)r;
+}
+
+// Lexicographic unranking of `rank` among the L-subsets of {1..K} into 1-based
+// positions (the order of set_helpers.cu:25-49).  Each position is found by a binary
+// search on the hockey-stick identity sum_{u=1..t} C(N-u, r) = C(N, r+1) - C(N-t, r+1),
+// so the cost is O(L^2 log K) instead of the O(L K) walk.
+template <int L>
+__device__ __forceinline__ void unrank_positions(int K, long long rank, int *pos) {
+    int xprev = 0;
+#pragma unroll
+    for (int c = 0; c < L; ++c) {
+        const int r = L - c - 1;  // elements still to place after this one
+        const int N = K - xprev;  // numbers still available
+        if (r == 0) {
+            pos[c] = xprev + (int)rank + 1;
+        } else {
+            const long long total = binom_small<L>(N, r + 1);
+            const long long target = total - rank;  // want smallest t: C(N-t, r+1) < target
+            int lo = 1, hi = N - r;                  // t in [1, N-r]
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (binom_small<L>(N - mid, r + 1) < target) hi = mid;
+                else lo = mid + 1;
+            }
+            rank -= total - binom_small<L>(N - lo + 1, r + 1);
+            xprev += lo;
+            pos[c] = xprev;
+        }
+    }
+}
+
+// Runtime-level variant for the shared-memory kernels (level up to GCSL_MAX_LEVELS).
+__device__ __forceinline__ void unrank_positions_rt(int L, int K, long long rank, int *pos) {
+    int xprev = 0;
+    for (int c = 0; c < L; ++c) {
+        const int r = L - c - 1;
+        const int N = K - xprev;
+        if (r == 0) {
+            pos[c] = xprev + (int)rank + 1;
+        } else {
+            const long long total = binom_rt(N, r + 1);
+            const long long target = total - rank;
+            int lo = 1, hi = N - r;
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (binom_rt(N - mid, r + 1) < target) hi = mid;
+                else lo = mid + 1;
+            }
+            rank -= total - binom_rt(N - lo + 1, r + 1);
+            xprev += lo;
+            pos[c] = xprev;
+        }
+    }
+}
+
+// Position q (1-based, over the neighbours of v_i without v_j) -> variable id; the
+// ascending neighbour list still contains v_j, which is skipped (set_helpers.cu:51-57).
+__device__ __forceinline__ int resolve_position(const int *__restrict__ nbrs, int vj, int q) {
+    int idx = q - 1;
+    idx += (__ldg(nbrs + idx) >= vj);
+    return __ldg(nbrs + idx);
+}
+
+__device__ __forceinline__ double warp_min(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(GCSL_FULL_MASK, v, o));
+    return v;
+}
+
+// Ordered atomics on non-negative doubles through their bit patterns.
+__device__ __forceinline__ void atomic_max_nonneg(double *addr, double v) {
+    atomicMax(reinterpret_cast<unsigned long long *>(addr), (unsigned long long)__double_as_longlong(v));
+}
+__device__ __forceinline__ void atomic_min_nonneg(double *addr, double v) {
+    atomicMin(reinterpret_cast<unsigned long long *>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
+// Largest i in [0, n) with prefix[i] <= x (prefix non-decreasing, prefix[0] = 0).
+__device__ __forceinline__ int upper_row(const long long *__restrict__ prefix, int n, long long x) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+}  // namespace gcsl

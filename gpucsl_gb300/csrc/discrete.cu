@@ -1,0 +1,514 @@
+// Discrete (chi-squared) PC-stable skeleton kernels for sm_103a (kernel d + write-back e).
+//
+//   tests          disc_test_kernel      (reference: gpucsl/pc/cuda/discrete_ci.cu:37-246,
+//                                         helpers/discrete_helpers.cu:25-186)
+//   p-value        pchisq_dev            (reference: helpers/math_helpers.cu:54-175)
+//   write-back     disc_finalize_kernel  (reference: helpers/graph_helpers.cu:81-101)
+//
+// One CTA evaluates one test at a time (grid-stride over the level's flattened test
+// list): the l+2 uint8 columns are streamed with 16-byte loads and counted into a
+// shared-memory table N[s][a][b] (several copies when the table is small, so that
+// lanes of a warp rarely hit the same counter), the copies are merged, each stratum's
+// marginals and (a, b)-ordered chi^2 partial sum are formed by one thread, and thread 0
+// adds the strata in ascending order and evaluates the p-value.  Counts are exact
+// integers; the chi^2 order is fixed, so results do not depend on scheduling.
+//
+// As in the reference every rank of every direction is tested (discrete_ci.cu:221-244
+// has no effective early exit) and pmax folds all of them.  The removing test with the
+// smallest key (rank, dir) is the canonical remover; its set becomes the sepset.
+#include "common.cuh"
+
+namespace gcsl {
+
+// ---------------------------------------------------------------- p-value
+// Ibbetson (CACM Alg. 209) normal tail as coded by Perlman; the polynomial
+// coefficients are those of the published algorithm.
+__device__ double poz_dev(double z) {
+    double x;
+    if (z == 0.0) {
+        x = 0.0;
+    } else {
+        double y = 0.5 * fabs(z);
+        if (y >= 3.0) {
+            x = 1.0;
+        } else if (y < 1.0) {
+            const double w = y * y;
+            double t = 0.000124818987;
+            t = __dadd_rn(__dmul_rn(t, w), -0.001075204047);
+            t = __dadd_rn(__dmul_rn(t, w), 0.005198775019);
+            t = __dadd_rn(__dmul_rn(t, w), -0.019198292004);
+            t = __dadd_rn(__dmul_rn(t, w), 0.059054035642);
+            t = __dadd_rn(__dmul_rn(t, w), -0.151968751364);
+            t = __dadd_rn(__dmul_rn(t, w), 0.319152932694);
+            t = __dadd_rn(__dmul_rn(t, w), -0.531923007300);
+            t = __dadd_rn(__dmul_rn(t, w), 0.797884560593);
+            x = __dmul_rn(__dmul_rn(t, y), 2.0);
+        } else {
+            y -= 2.0;
+            double t = -0.000045255659;
+            t = __dadd_rn(__dmul_rn(t, y), 0.000152529290);
+            t = __dadd_rn(__dmul_rn(t, y), -0.000019538132);
+            t = __dadd_rn(__dmul_rn(t, y), -0.000676904986);
+            t = __dadd_rn(__dmul_rn(t, y), 0.001390604284);
+            t = __dadd_rn(__dmul_rn(t, y), -0.000794620820);
+            t = __dadd_rn(__dmul_rn(t, y), -0.002034254874);
+            t = __dadd_rn(__dmul_rn(t, y), 0.006549791214);
+            t = __dadd_rn(__dmul_rn(t, y), -0.010557625006);
+            t = __dadd_rn(__dmul_rn(t, y), 0.011630447319);
+            t = __dadd_rn(__dmul_rn(t, y), -0.009279453341);
+            t = __dadd_rn(__dmul_rn(t, y), 0.005353579108);
+            t = __dadd_rn(__dmul_rn(t, y), -0.002141268741);
+            t = __dadd_rn(__dmul_rn(t, y), 0.000535310849);
+            x = __dadd_rn(__dmul_rn(t, y), 0.999936657524);
+        }
+    }
+    return z > 0.0 ? ((x + 1.0) * 0.5) : ((1.0 - x) * 0.5);
+}
+
+__device__ __forceinline__ double ex_dev(double x) { return (x < -20.0) ? 0.0 : exp(x); }
+
+// Upper tail of chi^2 (Hill & Pike, CACM Alg. 299, with the 1985 rounding remark, in
+// Perlman's formulation): the finite series of the even / odd df cases.
+__device__ double pchisq_dev(double x, long long df) {
+    if (x <= 0.0 || df < 1) return 1.0;
+    const double a = 0.5 * x;
+    const bool even = (df & 1) == 0;
+    const double y = (df > 1) ? ex_dev(-a) : 0.0;
+    double s = even ? y : 2.0 * poz_dev(-sqrt(x));
+    if (df <= 2) return s;
+    const double half = 0.5 * ((double)df - 1.0);
+    double z = even ? 1.0 : 0.5;
+    if (a > 20.0) {
+        double e = even ? 0.0 : 0.5723649429247000870717135;
+        const double c = log(a);
+        while (z <= half) {
+            e = __dadd_rn(log(z), e);
+            s = __dadd_rn(s, ex_dev(__dsub_rn(__dsub_rn(__dmul_rn(c, z), a), e)));
+            z += 1.0;
+        }
+        return s;
+    }
+    double e = even ? 1.0 : 0.5641895835477562869480795 / sqrt(a);
+    double c = 0.0;
+    while (z <= half) {
+        e = __dmul_rn(e, a / z);
+        c = __dadd_rn(c, e);
+        z += 1.0;
+    }
+    return __dadd_rn(__dmul_rn(c, y), s);
+}
+
+// ------------------------------------------------------------ test kernel
+
+__device__ __forceinline__ void tri_pair(long long t, int &vi, int &vj) {
+    // t -> (vi > vj), t = vi (vi - 1) / 2 + vj
+    long long i = (long long)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
+    while (i * (i - 1) / 2 > t) --i;
+    while ((i + 1) * i / 2 <= t) ++i;
+    vi = (int)i;
+    vj = (int)(t - i * (i - 1) / 2);
+}
+
+// Count the table N[s][a][b] of one test into shared memory (all threads of the CTA).
+// S / mult live in shared memory; `copies` replicas of T counters are merged into the
+// first one before returning.
+__device__ void count_table(const uint8_t *__restrict__ data, long long ld, long long n, int vi, int vj,
+                            const int *S, const int *mult, int L, int di, int dj, int T, int copies,
+                            uint32_t *sm_tab, int *bad) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int k = tid; k < T * copies; k += nt) sm_tab[k] = 0;
+    __syncthreads();
+    uint32_t *tab = sm_tab + (size_t)(tid % copies) * T;
+    const uint4 *ci = reinterpret_cast<const uint4 *>(data + (size_t)vi * ld);
+    const uint4 *cj = reinterpret_cast<const uint4 *>(data + (size_t)vj * ld);
+    const long long nvec = (n + 15) >> 4;
+    for (long long v = tid; v < nvec; v += nt) {
+        int sidx[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) sidx[q] = 0;
+        for (int k = 0; k < L; ++k) {
+            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(data + (size_t)S[k] * ld) + v);
+            const int mk = mult[k];
+            const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int q = 0; q < 16; ++q) sidx[q] += (int)((ww[q >> 2] >> (8 * (q & 3))) & 0xffu) * mk;
+        }
+        const uint4 xi = __ldg(ci + v), xj = __ldg(cj + v);
+        const uint32_t wi[4] = {xi.x, xi.y, xi.z, xi.w};
+        const uint32_t wj[4] = {xj.x, xj.y, xj.z, xj.w};
+        const long long rem = n - (v << 4);
+        const int nvalid = rem >= 16 ? 16 : (int)rem;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            if (q < nvalid) {
+                const int a = (int)((wi[q >> 2] >> (8 * (q & 3))) & 0xffu);
+                const int b = (int)((wj[q >> 2] >> (8 * (q & 3))) & 0xffu);
+                const int idx = (sidx[q] * di + a) * dj + b;
+                // codes at or above their cardinality are invalid input: never written
+                if ((unsigned)idx < (unsigned)T && a < di && b < dj) atomicAdd(&tab[idx], 1u);
+                else *bad = 1;
+            }
+        }
+    }
+    __syncthreads();
+    if (copies > 1) {
+        for (int k = tid; k < T; k += nt) {
+            uint32_t s = 0;
+            for (int c = 0; c < copies; ++c) s += sm_tab[(size_t)c * T + k];
+            sm_tab[k] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// chi^2 partial sum of one stratum, (a, b) order; E = N_a+ N_+b / N_++, terms with
+// N_++ == 0 or E == 0 skipped (discrete_helpers.cu:164-186).
+__device__ double stratum_chi2(const uint32_t *Ts, int di, int dj) {
+    double part = 0.0;
+    if (di <= 16 && dj <= 16) {
+        uint32_t ma[16], mb[16];
+        uint32_t mt = 0;
+#pragma unroll
+        for (int a = 0; a < 16; ++a) ma[a] = mb[a] = 0;
+        for (int a = 0; a < di; ++a)
+            for (int b = 0; b < dj; ++b) {
+                const uint32_t o = Ts[a * dj + b];
+                ma[a] += o;
+                mb[b] += o;
+                mt += o;
+            }
+        if (mt == 0) return 0.0;
+        for (int a = 0; a < di; ++a)
+            for (int b = 0; b < dj; ++b) {
+                const double e = __ddiv_rn(__dmul_rn((double)ma[a], (double)mb[b]), (double)mt);
+                if (e == 0.0) continue;
+                const double d = __dsub_rn((double)Ts[a * dj + b], e);
+                part = __dadd_rn(part, __ddiv_rn(__dmul_rn(d, d), e));
+            }
+        return part;
+    }
+    // wide tables: the marginals are recomputed from the table (same integers)
+    uint32_t mt = 0;
+    for (int k = 0; k < di * dj; ++k) mt += Ts[k];
+    if (mt == 0) return 0.0;
+    for (int a = 0; a < di; ++a) {
+        uint32_t ma = 0;
+        for (int b = 0; b < dj; ++b) ma += Ts[a * dj + b];
+        for (int b = 0; b < dj; ++b) {
+            uint32_t mb = 0;
+            for (int a2 = 0; a2 < di; ++a2) mb += Ts[a2 * dj + b];
+            const double e = __ddiv_rn(__dmul_rn((double)ma, (double)mb), (double)mt);
+            if (e == 0.0) continue;
+            const double d = __dsub_rn((double)Ts[a * dj + b], e);
+            part = __dadd_rn(part, __ddiv_rn(__dmul_rn(d, d), e));
+        }
+    }
+    return part;
+}
+
+// Statistic of the counted table: strata in parallel, then added in ascending s by
+// thread 0 (the return value is meaningful in thread 0 only).
+__device__ double table_chi2(const uint32_t *sm_tab, int dim_s, int di, int dj, double *s_part) {
+    for (int s = threadIdx.x; s < dim_s; s += blockDim.x) s_part[s] = stratum_chi2(sm_tab + (size_t)s * di * dj, di, dj);
+    __syncthreads();
+    double chi = 0.0;
+    if (threadIdx.x == 0)
+        for (int s = 0; s < dim_s; ++s) chi = __dadd_rn(chi, s_part[s]);
+    return chi;
+}
+
+// Per-test header prepared by thread 0: table geometry and replica count.
+__device__ __forceinline__ bool table_geometry(const uint8_t *dims, const int *S, int *mult, int L, int vi, int vj,
+                                               int table_cap, int &dim_s, int &di, int &dj, int &copies) {
+    long long ds = 1;
+    for (int k = 0; k < L; ++k) {
+        mult[k] = (int)ds;
+        ds *= dims[S[k]];
+        if (ds > table_cap) return false;
+    }
+    di = dims[vi];
+    dj = dims[vj];
+    const long long T = ds * di * dj;
+    if (T > table_cap || ds > 1024) return false;
+    dim_s = (int)ds;
+    copies = 1;
+    if (T <= table_cap / 8) copies = 8;
+    else if (T <= table_cap / 4) copies = 4;
+    else if (T <= table_cap / 2) copies = 2;
+    return true;
+}
+
+__global__ void __launch_bounds__(256) disc_test_kernel(DiscLevelArgs A) {
+    extern __shared__ uint32_t sm_tab[];
+    __shared__ int s_S[GCSL_MAX_LEVELS + 2];
+    __shared__ int s_mult[GCSL_MAX_LEVELS + 2];
+    __shared__ int s_hdr[7];  // vi, vj, di, dj, dim_s, copies, ok
+    __shared__ long long s_rank;
+    __shared__ double s_part[1024];
+    __shared__ int s_bad;
+    DevState *st = A.st;
+    if (threadIdx.x == 0) s_bad = 0;
+    const int L = A.level;
+    if (L > 0) {
+        if (st->done) return;
+        const int md = st->max_degree[L];
+        if (md - 1 < L) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) st->done = 1;
+            return;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->last_level = L;
+    }
+    const long long total = (L == 0) ? (long long)A.p * (A.p - 1) / 2 : A.prefix[A.p];
+    const int tid = threadIdx.x;
+    for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+        if (tid == 0) {
+            int vi, vj;
+            long long rank = 0;
+            if (L == 0) {
+                tri_pair(t, vi, vj);
+            } else {
+                vi = upper_row(A.prefix, A.p, t);
+                const long long off = t - A.prefix[vi];
+                const int deg = A.adj[(size_t)vi * A.p];
+                const long long R = binom_rt(deg - 1, L);
+                const int m = (int)(off / R);
+                rank = off - (long long)m * R;
+                vj = A.adj[(size_t)vi * A.p + 1 + m];
+                unrank_positions_rt(L, deg - 1, rank, s_S);
+                const int *nbrs = A.adj + (size_t)vi * A.p + 1;
+                for (int c = 0; c < L; ++c) s_S[c] = resolve_position(nbrs, vj, s_S[c]);
+            }
+            int dim_s = 0, di = 0, dj = 0, copies = 1;
+            const bool ok = table_geometry(A.dims, s_S, s_mult, L, vi, vj, A.table_cap, dim_s, di, dj, copies);
+            s_hdr[0] = vi;
+            s_hdr[1] = vj;
+            s_hdr[2] = di;
+            s_hdr[3] = dj;
+            s_hdr[4] = dim_s;
+            s_hdr[5] = copies;
+            s_hdr[6] = ok;
+            s_rank = rank;
+            if (!ok) set_status(st, GCSL_ERR_UNSUPPORTED);
+        }
+        __syncthreads();
+        if (!s_hdr[6]) {
+            __syncthreads();
+            continue;
+        }
+        const int vi = s_hdr[0], vj = s_hdr[1], di = s_hdr[2], dj = s_hdr[3], dim_s = s_hdr[4];
+        count_table(A.data, A.ld, A.n, vi, vj, s_S, s_mult, L, di, dj, dim_s * di * dj, s_hdr[5], sm_tab,
+                    &s_bad);
+        const double chi = table_chi2(sm_tab, dim_s, di, dj, s_part);
+        if (tid == 0 && s_bad) set_status(st, GCSL_ERR_INVALID_ARG);
+        if (tid == 0) {
+            const long long df = (long long)(di - 1) * (long long)(dj - 1) * (long long)dim_s;
+            const double pv = pchisq_dev(chi, df);
+            const int lo = vi < vj ? vi : vj, hi = vi < vj ? vj : vi;
+            const size_t ix = (size_t)lo * A.p + hi;
+            if (L == 0) {
+                A.pmax[ix] = pv;
+                const uint16_t keep = (pv >= A.alpha) ? 0 : 1;
+                A.G[(size_t)vi * A.p + vj] = keep;
+                A.G[(size_t)vj * A.p + vi] = keep;
+            } else {
+                atomic_max_nonneg(&A.pmax[ix], pv);
+                if (pv >= A.alpha) {
+                    const unsigned long long key = ((unsigned long long)s_rank << 1) | (vi < vj ? 0ull : 1ull);
+                    atomicMin(&A.win[ix], key);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0 && tid == 0) st->tests[L] = (unsigned long long)total;
+}
+
+// One test for the unit entry point: counts and (chi^2, p-value) to global memory.
+struct UnitSet {
+    int S[GCSL_MAX_LEVELS];
+};
+
+__global__ void __launch_bounds__(256) disc_table_kernel(const uint8_t *data, long long ld, long long n,
+                                                         const uint8_t *dims, int vi, int vj, UnitSet us, int L,
+                                                         int table_cap, uint32_t *counts, double *out2) {
+    extern __shared__ uint32_t sm_tab[];
+    __shared__ int s_S[GCSL_MAX_LEVELS + 2];
+    __shared__ int s_mult[GCSL_MAX_LEVELS + 2];
+    __shared__ int s_hdr[4];
+    __shared__ double s_part[1024];
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < L; ++k) s_S[k] = us.S[k];
+        int dim_s = 0, di = 0, dj = 0, copies = 1;
+        const bool ok = table_geometry(dims, s_S, s_mult, L, vi, vj, table_cap, dim_s, di, dj, copies);
+        s_hdr[0] = ok ? dim_s : -1;
+        s_hdr[1] = di;
+        s_hdr[2] = dj;
+        s_hdr[3] = copies;
+    }
+    __syncthreads();
+    const int dim_s = s_hdr[0], di = s_hdr[1], dj = s_hdr[2];
+    if (dim_s < 0) {
+        if (threadIdx.x == 0) out2[0] = out2[1] = -1.0;
+        return;
+    }
+    const int T = dim_s * di * dj;
+    __shared__ int s_bad;
+    if (threadIdx.x == 0) s_bad = 0;
+    count_table(data, ld, n, vi, vj, s_S, s_mult, L, di, dj, T, s_hdr[3], sm_tab, &s_bad);
+    for (int k = threadIdx.x; k < T; k += blockDim.x) counts[k] = sm_tab[k];
+    const double chi = table_chi2(sm_tab, dim_s, di, dj, s_part);
+    if (threadIdx.x == 0) {
+        if (s_bad) {
+            out2[0] = out2[1] = -1.0;
+            return;
+        }
+        out2[0] = chi;
+        out2[1] = pchisq_dev(chi, (long long)(di - 1) * (long long)(dj - 1) * (long long)dim_s);
+    }
+}
+
+// Per-row weights deg_r * C(deg_r - 1, L) of the level's flattened test list.
+__global__ void disc_weights_kernel(const int *__restrict__ adj, int p, int L, long long *__restrict__ w,
+                                    DevState *st) {
+    if (st->done) return;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= p) return;
+    const int deg = adj[(size_t)r * p];
+    const long long R = (deg - 1 >= L) ? binom_rt(deg - 1, L) : 0;
+    if (R >= GCSL_RANK_LIMIT) set_status(st, GCSL_ERR_UNSUPPORTED);
+    w[r] = (long long)deg * R;
+}
+
+// Write-back of a level: canonical remover -> skeleton, sepsets, records.
+__global__ void disc_finalize_kernel(const int *__restrict__ adj, int p, int L, uint16_t *G,
+                                     unsigned long long *win, int *sep_dense, int max_level, int *rec_pool,
+                                     long long rec_cap, DevState *st) {
+    if (st->done) return;
+    if (st->max_degree[L] - 1 < L) return;
+    const long long total = (long long)p * p;
+    unsigned long long removed = 0;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long key = win[k];
+        if (key == GCSL_KEY_NONE) continue;
+        win[k] = GCSL_KEY_NONE;
+        const int lo = (int)(k / p), hi = (int)(k - (long long)lo * p);
+        const long long rank = (long long)(key >> 1);
+        const int vi = (key & 1) ? hi : lo, vj = (key & 1) ? lo : hi;
+        const int *row = adj + (size_t)vi * p;
+        int S[GCSL_MAX_LEVELS];
+        unrank_positions_rt(L, row[0] - 1, rank, S);
+        for (int c = 0; c < L; ++c) S[c] = resolve_position(row + 1, vj, S[c]);
+        G[(size_t)lo * p + hi] = 0;
+        G[(size_t)hi * p + lo] = 0;
+        if (sep_dense != nullptr && L <= max_level) {
+            for (int c = 0; c < L; ++c) {
+                sep_dense[((size_t)lo * p + hi) * max_level + c] = S[c];
+                sep_dense[((size_t)hi * p + lo) * max_level + c] = S[c];
+            }
+        }
+        if (rec_pool != nullptr) {
+            const unsigned long long off = atomicAdd(&st->n_rec_ints, (unsigned long long)(3 + L));
+            if ((long long)(off + 3 + L) <= rec_cap) {
+                rec_pool[off] = lo;
+                rec_pool[off + 1] = hi;
+                rec_pool[off + 2] = L;
+                for (int c = 0; c < L; ++c) rec_pool[off + 3 + c] = S[c];
+            } else {
+                set_status(st, GCSL_ERR_CAPACITY);
+            }
+        }
+        ++removed;
+    }
+    if (removed) atomicAdd(&st->removed[L], removed);
+}
+
+// Edges alive at level start and the level's full test space (for the stats).
+__global__ void disc_level_stats_kernel(const long long *__restrict__ prefix, const int *__restrict__ adj, int p,
+                                        int L, DevState *st) {
+    if (st->done) return;
+    if (threadIdx.x == 0 && blockIdx.x == 0) st->tests_full[L] = (unsigned long long)prefix[p];
+    unsigned long long e = 0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < p; r += gridDim.x * blockDim.x)
+        e += (unsigned long long)adj[(size_t)r * p];
+    if (e) atomicAdd(&st->edges[L], e);  // directed count; halved on the host
+}
+
+__global__ void pmax_finish_kernel(double *pmax, int p) {
+    const long long total = (long long)p * p;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(k / p), j = (int)(k - (long long)i * p);
+        if (i >= j) pmax[k] = -1.0;
+    }
+}
+
+// Unit entry point kernels -------------------------------------------------
+__global__ void pchisq_kernel(const double *x, const long long *df, long long count, double *out) {
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < count;
+         k += (long long)gridDim.x * blockDim.x)
+        out[k] = pchisq_dev(x[k], df[k]);
+}
+
+namespace host {
+
+int disc_table_cap(int device) {
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    // leave room for the static shared arrays of the kernel
+    const int dyn = optin - 16 * 1024;
+    return dyn / (int)sizeof(uint32_t);
+}
+
+cudaError_t launch_disc_tests(const DiscLevelArgs &A, int num_sms, cudaStream_t s) {
+    const size_t smem = (size_t)A.table_cap * sizeof(uint32_t);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(disc_test_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_set = true;
+    }
+    disc_test_kernel<<<num_sms * 4, 256, smem, s>>>(A);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_disc_weights(const int *adj, int p, int L, long long *w, DevState *st, cudaStream_t s) {
+    disc_weights_kernel<<<(p + 255) / 256, 256, 0, s>>>(adj, p, L, w, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_disc_finalize(const int *adj, int p, int L, uint16_t *G, unsigned long long *win, int *sep,
+                                 int max_level, int *rec, long long rec_cap, DevState *st, int num_sms,
+                                 cudaStream_t s) {
+    disc_finalize_kernel<<<num_sms * 2, 256, 0, s>>>(adj, p, L, G, win, sep, max_level, rec, rec_cap, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_disc_level_stats(const long long *prefix, const int *adj, int p, int L, DevState *st,
+                                    cudaStream_t s) {
+    disc_level_stats_kernel<<<(p + 255) / 256, 256, 0, s>>>(prefix, adj, p, L, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pmax_finish(double *pmax, int p, int num_sms, cudaStream_t s) {
+    pmax_finish_kernel<<<num_sms * 2, 256, 0, s>>>(pmax, p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_disc_table(const uint8_t *data, long long ld, long long n, const uint8_t *dims, int vi, int vj,
+                              const int *S, int L, int table_cap, uint32_t *counts, double *out2, cudaStream_t s) {
+    UnitSet us;
+    for (int k = 0; k < GCSL_MAX_LEVELS; ++k) us.S[k] = k < L ? S[k] : 0;
+    const size_t smem = (size_t)table_cap * sizeof(uint32_t);
+    cudaFuncSetAttribute(disc_table_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    disc_table_kernel<<<1, 256, smem, s>>>(data, ld, n, dims, vi, vj, us, L, table_cap, counts, out2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pchisq(const double *x, const long long *df, long long count, double *out, cudaStream_t s) {
+    const int blocks = (int)((count + 255) / 256);
+    pchisq_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(x, df, count, out);
+    return cudaGetLastError();
+}
+
+}  // namespace host
+}  // namespace gcsl

@@ -1,0 +1,518 @@
+// Gaussian PC-stable skeleton kernels for sm_103a.
+//
+//   level 0        gauss_level0_kernel     (reference: gpucsl/pc/cuda/gaussian_ci.cu:18-51)
+//   compaction     compact_kernel          (reference: gpucsl/pc/cuda/helpers/graph_helpers.cu:35-56)
+//   edge prefix    row_scan_kernel
+//   level l <= 8   gauss_level_reg_kernel  (reference: gaussian_ci.cu:66-120,
+//                                           helpers/gaussian_helpers.cu:240-262)
+//   level l > 8    gauss_level_smem_kernel
+//   zmin -> pmax   pmax_kernel             (reference: gpucsl/pc/helpers.py:62-82)
+//
+// Work decomposition of a level: one warp owns one undirected edge {lo, hi} alive at
+// level start and walks the merged key sequence of both directions, key = (rank, dir)
+// with dir 0 for v_i = lo, 32 keys per step (one test per lane).  The warp stops after
+// the first step that contains a removing test; the lowest removing lane is the
+// canonical remover (its set is the sepset) and z* folds the keys up to it.  Because
+// the warp owns the edge for the whole level, the skeleton, sepset and zmin writes
+// need no atomics, and the result does not depend on scheduling.
+#include "common.cuh"
+
+namespace gcsl {
+
+// ----------------------------------------------------------------- level 0
+// Warp per row i, lanes over j > i: Z = |0.5 log|(1+r)/(1-r)||, r = C[i*p + j];
+// remove iff Z < tau0; z*(i,j) = Z (NaN ignored); zero diagonal.
+__global__ void gauss_level0_kernel(const double *__restrict__ C, int p, double tau0, uint16_t *__restrict__ G,
+                                    double *__restrict__ zmin, DevState *st) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long removed = 0;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p; i += warps) {
+        const double *Ci = C + (size_t)i * p;
+        for (int j = i + 1 + lane; j < p; j += 32) {
+            const double r = __ldg(Ci + j);
+            const double z = fabs(0.5 * log(fabs((1.0 + r) / (1.0 - r))));
+            const bool rem = z < tau0;
+            const uint16_t g = rem ? 0 : 1;
+            G[(size_t)i * p + j] = g;
+            G[(size_t)j * p + i] = g;
+            zmin[(size_t)i * p + j] = isnan(z) ? __longlong_as_double(0x7ff0000000000000ll) : z;
+            removed += rem;
+        }
+        if (lane == 0) G[(size_t)i * p + i] = 0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) removed += __shfl_xor_sync(GCSL_FULL_MASK, removed, o);
+    if (lane == 0 && removed) atomicAdd(&st->removed[0], removed);
+}
+
+// ------------------------------------------------------------- compaction
+// Warp per row r: adj[r*p] = degree, adj[r*p + 1 ..] = ascending neighbour ids
+// (entries past the degree keep stale values, as in the reference); also writes
+// up[r] = #neighbours > r and the level's max degree.  Returns at once when the level
+// loop is already finished.
+__global__ void compact_kernel(const uint16_t *__restrict__ G, int p, int *__restrict__ adj, int *__restrict__ up,
+                               DevState *st, int level) {
+    if (st != nullptr && st->done) return;
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    int maxdeg = 0;
+    for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p; r += warps) {
+        const uint16_t *Gr = G + (size_t)r * p;
+        int *row = adj + (size_t)r * p;
+        int cnt = 0, ups = 0;
+        for (int c0 = 0; c0 < p; c0 += 32) {
+            const int c = c0 + lane;
+            const bool e = (c < p) && (c != r) && (Gr[c] != 0);
+            const unsigned b = __ballot_sync(GCSL_FULL_MASK, e);
+            if (e) row[1 + cnt + __popc(b & ((1u << lane) - 1))] = c;
+            cnt += __popc(b);
+            ups += __popc(__ballot_sync(GCSL_FULL_MASK, e && c > r));
+        }
+        if (lane == 0) {
+            row[0] = cnt;
+            if (up != nullptr) up[r] = ups;
+        }
+        maxdeg = max(maxdeg, cnt);
+    }
+    if (lane == 0 && st != nullptr) atomicMax(&st->max_degree[level], maxdeg);
+}
+
+// Single-block exclusive scan of a per-row count (int or weighted long long) into
+// prefix[0..p]; prefix[p] is the total.
+template <typename T>
+__global__ void row_scan_kernel(const T *__restrict__ cnt, int p, long long *__restrict__ prefix, DevState *st) {
+    if (st->done) return;
+    __shared__ long long warp_tot[32];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int per = (p + nt - 1) / nt;
+    const int b = tid * per, e = min(p, b + per);
+    long long s = 0;
+    for (int i = b; i < e; ++i) s += (long long)cnt[i];
+    // inclusive scan of s across the block
+    long long v = s;
+    const int lane = tid & 31, w = tid >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        long long t = __shfl_up_sync(GCSL_FULL_MASK, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) warp_tot[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        long long t = (lane < (nt >> 5)) ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            long long u = __shfl_up_sync(GCSL_FULL_MASK, t, o);
+            if (lane >= o) t += u;
+        }
+        warp_tot[lane] = t;
+    }
+    __syncthreads();
+    long long base = v - s + (w > 0 ? warp_tot[w - 1] : 0);
+    for (int i = b; i < e; ++i) {
+        prefix[i] = base;
+        base += (long long)cnt[i];
+    }
+    if (tid == nt - 1) prefix[p] = base;
+}
+
+// ---------------------------------------------------------- level l, L <= 8
+// Partial-correlation statistic of one test from the augmented matrix
+// [[C_SS, C_S,vi, C_S,vj], [., 1, C_vi,vj], [., ., 1]]: L elimination steps leave the
+// trailing 2x2 block H = M0 - M1 M2^-1 M1^T of gaussian_helpers.cu:78-89.
+template <int L>
+__device__ __forceinline__ double gauss_test_reg(const double *__restrict__ C, int p, int vi, int vj, const int *S) {
+    double A[L * (L + 1) / 2];  // lower triangle of C_SS, row-packed
+    double a[L], b[L];
+#pragma unroll
+    for (int r = 0; r < L; ++r) {
+        const double *Cr = C + (size_t)S[r] * p;
+#pragma unroll
+        for (int c = 0; c < r; ++c) A[r * (r + 1) / 2 + c] = __ldg(Cr + S[c]);
+        A[r * (r + 1) / 2 + r] = __ldg(Cr + S[r]);
+        a[r] = __ldg(C + (size_t)vi * p + S[r]);
+        b[r] = __ldg(C + (size_t)vj * p + S[r]);
+    }
+    const double rij = __ldg(C + (size_t)vi * p + vj);
+    // Cholesky (left-looking) with the two extra rows solved alongside.
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+        double d = A[j * (j + 1) / 2 + j];
+#pragma unroll
+        for (int k = 0; k < j; ++k) d -= A[j * (j + 1) / 2 + k] * A[j * (j + 1) / 2 + k];
+        d = sqrt(d);
+        const double inv = 1.0 / d;
+        A[j * (j + 1) / 2 + j] = d;
+#pragma unroll
+        for (int i = j + 1; i < L; ++i) {
+            double s = A[i * (i + 1) / 2 + j];
+#pragma unroll
+            for (int k = 0; k < j; ++k) s -= A[i * (i + 1) / 2 + k] * A[j * (j + 1) / 2 + k];
+            A[i * (i + 1) / 2 + j] = s * inv;
+        }
+        double sa = a[j], sb = b[j];
+#pragma unroll
+        for (int k = 0; k < j; ++k) {
+            sa -= a[k] * A[j * (j + 1) / 2 + k];
+            sb -= b[k] * A[j * (j + 1) / 2 + k];
+        }
+        a[j] = sa * inv;
+        b[j] = sb * inv;
+    }
+    double h00 = 1.0, h11 = 1.0, h01 = rij;
+#pragma unroll
+    for (int k = 0; k < L; ++k) {
+        h00 -= a[k] * a[k];
+        h11 -= b[k] * b[k];
+        h01 -= a[k] * b[k];
+    }
+    const double rho = h01 / (sqrt(fabs(h00)) * sqrt(fabs(h11)));
+    return fabs(0.5 * (log(fabs(1.0 + rho)) - log(fabs(1.0 - rho))));
+}
+
+struct EdgeJob {
+    int lo, hi, deg_lo, deg_hi;
+    long long R0, R1, T, Rmin;
+    int longer;
+};
+
+template <int KMAX>
+__device__ __forceinline__ bool load_edge(const int *__restrict__ adj, const int *__restrict__ up,
+                                          const long long *__restrict__ prefix, int p, long long e, int L,
+                                          EdgeJob &J) {
+    const int i = upper_row(prefix, p, e);
+    const long long k = e - prefix[i];
+    const int *row = adj + (size_t)i * p;
+    const int deg = row[0];
+    const int j = row[1 + (deg - up[i]) + (int)k];
+    J.lo = i;
+    J.hi = j;
+    J.deg_lo = deg;
+    J.deg_hi = adj[(size_t)j * p];
+    const int K0 = J.deg_lo - 1, K1 = J.deg_hi - 1;
+    J.R0 = (K0 >= L) ? (KMAX > 0 ? binom_small<KMAX>(K0, L) : binom_rt(K0, L)) : 0;
+    J.R1 = (K1 >= L) ? (KMAX > 0 ? binom_small<KMAX>(K1, L) : binom_rt(K1, L)) : 0;
+    J.T = J.R0 + J.R1;
+    J.Rmin = J.R0 < J.R1 ? J.R0 : J.R1;
+    J.longer = J.R0 > J.R1 ? 0 : 1;
+    return J.R0 < GCSL_RANK_LIMIT && J.R1 < GCSL_RANK_LIMIT;
+}
+
+// merged key index m -> (rank, dir)
+__device__ __forceinline__ void key_of(const EdgeJob &J, long long m, long long &rank, int &dir) {
+    if (m < 2 * J.Rmin) {
+        rank = m >> 1;
+        dir = (int)(m & 1);
+    } else {
+        rank = m - J.Rmin;
+        dir = J.longer;
+    }
+}
+
+__device__ __forceinline__ void write_removal(const EdgeJob &J, int L, const int *S, int p, int max_level,
+                                              uint16_t *G, int *sep_dense, int *rec_pool, long long rec_cap,
+                                              DevState *st) {
+    G[(size_t)J.lo * p + J.hi] = 0;
+    G[(size_t)J.hi * p + J.lo] = 0;
+    if (sep_dense != nullptr && L <= max_level) {
+        for (int k = 0; k < L; ++k) {
+            sep_dense[((size_t)J.lo * p + J.hi) * max_level + k] = S[k];
+            sep_dense[((size_t)J.hi * p + J.lo) * max_level + k] = S[k];
+        }
+    }
+    if (rec_pool != nullptr) {
+        const unsigned long long off = atomicAdd(&st->n_rec_ints, (unsigned long long)(3 + L));
+        if ((long long)(off + 3 + L) <= rec_cap) {
+            rec_pool[off] = J.lo;
+            rec_pool[off + 1] = J.hi;
+            rec_pool[off + 2] = L;
+            for (int k = 0; k < L; ++k) rec_pool[off + 3 + k] = S[k];
+        } else {
+            set_status(st, GCSL_ERR_CAPACITY);
+        }
+    }
+}
+
+// Common level entry: stop when the loop is finished or the level cannot run.
+__device__ __forceinline__ bool level_active(DevState *st, int level, bool tau_valid) {
+    if (st->done) return false;
+    const int md = st->max_degree[level];
+    if (md - 1 < level) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->done = 1;
+        return false;
+    }
+    if (!tau_valid) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            set_status(st, GCSL_ERR_UNSUPPORTED_LEVEL);
+            st->done = 1;
+        }
+        return false;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->last_level = level;
+    return true;
+}
+
+template <int L>
+__global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__restrict__ C, int p,
+                                                             const int *__restrict__ adj, const int *__restrict__ up,
+                                                             const long long *__restrict__ prefix, double tau,
+                                                             bool tau_valid, uint16_t *G, double *zmin,
+                                                             int *sep_dense, int max_level, int *rec_pool,
+                                                             long long rec_cap, DevState *st) {
+    if (!level_active(st, L, tau_valid)) return;
+    const int lane = threadIdx.x & 31;
+    const long long n_edges = prefix[p];
+    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    unsigned long long n_tests = 0, n_full = 0, n_removed = 0;
+    for (long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n_edges; e += warps) {
+        EdgeJob J;
+        if (!load_edge<L>(adj, up, prefix, p, e, L, J)) {
+            if (lane == 0) set_status(st, GCSL_ERR_UNSUPPORTED);
+            continue;
+        }
+        n_full += J.T;
+        double zl = __longlong_as_double(0x7ff0000000000000ll);
+        bool removed = false;
+        for (long long base = 0; base < J.T; base += 32) {
+            const long long m = base + lane;
+            const bool valid = m < J.T;
+            double z = __longlong_as_double(0x7ff8000000000000ll);
+            int S[L];
+            if (valid) {
+                long long rank;
+                int dir;
+                key_of(J, m, rank, dir);
+                const int vi = dir ? J.hi : J.lo, vj = dir ? J.lo : J.hi;
+                const int K = (dir ? J.deg_hi : J.deg_lo) - 1;
+                int pos[L];
+                unrank_positions<L>(K, rank, pos);
+                const int *nbrs = adj + (size_t)vi * p + 1;
+#pragma unroll
+                for (int c = 0; c < L; ++c) S[c] = resolve_position(nbrs, vj, pos[c]);
+                z = gauss_test_reg<L>(C, p, vi, vj, S);
+            }
+            const bool rem = valid && (z < tau);
+            const unsigned bal = __ballot_sync(GCSL_FULL_MASK, rem);
+            const int first = bal ? (__ffs(bal) - 1) : 32;
+            const double zc = (valid && lane <= first && !isnan(z)) ? z : __longlong_as_double(0x7ff0000000000000ll);
+            zl = fmin(zl, warp_min(zc));
+            const long long left = J.T - base;
+            n_tests += (unsigned long long)(bal ? first + 1 : (left < 32 ? left : 32));
+            if (bal) {
+                if (lane == first) write_removal(J, L, S, p, max_level, G, sep_dense, rec_pool, rec_cap, st);
+                removed = true;
+                break;
+            }
+        }
+        if (lane == 0) {
+            double *zp = zmin + (size_t)J.lo * p + J.hi;
+            *zp = fmin(*zp, zl);
+            n_removed += removed;
+        }
+    }
+    if (lane == 0) {
+        atomicAdd(&st->tests[L], n_tests);
+        atomicAdd(&st->tests_full[L], n_full);
+        atomicAdd(&st->removed[L], n_removed);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->edges[L] = (unsigned long long)n_edges;
+}
+
+// ---------------------------------------------------------- level l, any L
+// One warp per edge, one test at a time in key order; the (L+2)-dimensional lower
+// triangle lives in shared memory and the lanes split each elimination step.
+__global__ void __launch_bounds__(128) gauss_level_smem_kernel(const double *__restrict__ C, int p,
+                                                              const int *__restrict__ adj,
+                                                              const int *__restrict__ up,
+                                                              const long long *__restrict__ prefix, int L,
+                                                              double tau, bool tau_valid, uint16_t *G,
+                                                              double *zmin, int *sep_dense, int max_level,
+                                                              int *rec_pool, long long rec_cap, DevState *st) {
+    extern __shared__ double smem[];
+    if (!level_active(st, L, tau_valid)) return;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int D = L + 2;
+    const int tri = D * (D + 1) / 2;
+    double *A = smem + (size_t)wib * (tri + 2);
+    int *S = reinterpret_cast<int *>(smem + (size_t)(blockDim.x >> 5) * (tri + 2)) + wib * (GCSL_MAX_LEVELS + 2);
+    const long long n_edges = prefix[p];
+    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    unsigned long long n_tests = 0, n_full = 0, n_removed = 0;
+    for (long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n_edges; e += warps) {
+        EdgeJob J;
+        if (!load_edge<0>(adj, up, prefix, p, e, L, J)) {
+            if (lane == 0) set_status(st, GCSL_ERR_UNSUPPORTED);
+            continue;
+        }
+        n_full += J.T;
+        double zl = __longlong_as_double(0x7ff0000000000000ll);
+        bool removed = false;
+        for (long long m = 0; m < J.T; ++m) {
+            long long rank;
+            int dir;
+            key_of(J, m, rank, dir);
+            const int vi = dir ? J.hi : J.lo, vj = dir ? J.lo : J.hi;
+            if (lane == 0) {
+                unrank_positions_rt(L, (dir ? J.deg_hi : J.deg_lo) - 1, rank, S);
+                const int *nbrs = adj + (size_t)vi * p + 1;
+                for (int c = 0; c < L; ++c) S[c] = resolve_position(nbrs, vj, S[c]);
+                S[L] = vi;
+                S[L + 1] = vj;
+            }
+            __syncwarp();
+            // lower triangle of the augmented matrix; index r < L is S_r, L is v_i,
+            // L + 1 is v_j; unit diagonal for v_i, v_j and C[v_i, v_j] below it.
+            for (int r = 0; r < D; ++r) {
+                for (int c = lane; c <= r; c += 32) {
+                    double v;
+                    if (r == c && r >= L) v = 1.0;
+                    else if (r == L + 1 && c == L) v = __ldg(C + (size_t)vi * p + vj);
+                    else v = __ldg(C + (size_t)S[r] * p + S[c]);
+                    A[r * (r + 1) / 2 + c] = v;
+                }
+            }
+            __syncwarp();
+            for (int j = 0; j < L; ++j) {
+                const double d = sqrt(A[j * (j + 1) / 2 + j]);
+                const double inv = 1.0 / d;
+                __syncwarp();
+                for (int i = j + 1 + lane; i < D; i += 32) A[i * (i + 1) / 2 + j] *= inv;
+                __syncwarp();
+                // trailing update of rows/cols > j
+                const int nt = D - j - 1;
+                const int cnt = nt * (nt + 1) / 2;
+                (void)cnt;
+                for (int ii = j + 1; ii < D; ++ii) {
+                    const double lij = A[ii * (ii + 1) / 2 + j];
+                    for (int kk = j + 1 + lane; kk <= ii; kk += 32)
+                        A[ii * (ii + 1) / 2 + kk] -= lij * A[kk * (kk + 1) / 2 + j];
+                }
+                __syncwarp();
+            }
+            const double h00 = A[L * (L + 1) / 2 + L];
+            const double h01 = A[(L + 1) * (L + 2) / 2 + L];
+            const double h11 = A[(L + 1) * (L + 2) / 2 + L + 1];
+            const double rho = h01 / (sqrt(fabs(h00)) * sqrt(fabs(h11)));
+            const double z = fabs(0.5 * (log(fabs(1.0 + rho)) - log(fabs(1.0 - rho))));
+            ++n_tests;
+            if (!isnan(z)) zl = fmin(zl, z);
+            if (z < tau) {
+                if (lane == 0) write_removal(J, L, S, p, max_level, G, sep_dense, rec_pool, rec_cap, st);
+                removed = true;
+            }
+            __syncwarp();
+            if (removed) break;
+        }
+        if (lane == 0) {
+            double *zp = zmin + (size_t)J.lo * p + J.hi;
+            *zp = fmin(*zp, zl);
+            n_removed += removed;
+        }
+    }
+    if (lane == 0) {
+        atomicAdd(&st->tests[L < GCSL_MAX_LEVELS ? L : GCSL_MAX_LEVELS - 1], n_tests);
+        atomicAdd(&st->tests_full[L < GCSL_MAX_LEVELS ? L : GCSL_MAX_LEVELS - 1], n_full);
+        atomicAdd(&st->removed[L < GCSL_MAX_LEVELS ? L : GCSL_MAX_LEVELS - 1], n_removed);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->edges[L < GCSL_MAX_LEVELS ? L : GCSL_MAX_LEVELS - 1] = n_edges;
+}
+
+// ------------------------------------------------------------ zmin -> pmax
+// pmax_ij = 2 * sf(sqrt(n - 3) * z*_ij) for i < j (0 when z* = +inf), -1 elsewhere.
+// 2 sf(x) = erfc(x / sqrt 2), written as scipy's ndtr does it (erf below 1/sqrt 2).
+__global__ void pmax_kernel(const double *__restrict__ zmin, int p, double sqrt_nm3, double *__restrict__ pmax) {
+    const long long total = (long long)p * p;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(k / p), j = (int)(k - (long long)i * p);
+        double out = -1.0;
+        if (i < j) {
+            const double x = fabs(sqrt_nm3 * zmin[k]) * 0.70710678118654752440;
+            out = (x < 0.70710678118654752440) ? 1.0 - erf(x) : erfc(x);
+        }
+        pmax[k] = out;
+    }
+}
+
+// Unit kernel: all positions of ranks [0, count) (one thread per rank).
+__global__ void unrank_kernel(int K, int L, long long count, int *out) {
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < count;
+         r += (long long)gridDim.x * blockDim.x)
+        unrank_positions_rt(L, K, r, out + r * L);
+}
+
+// ------------------------------------------------------------- host launchers
+namespace host {
+
+cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, DevState *st,
+                          cudaStream_t s) {
+    const int threads = 256, warps_per_block = threads / 32;
+    int blocks = (p + warps_per_block - 1) / warps_per_block;
+    gauss_level0_kernel<<<blocks, threads, 0, s>>>(C, p, tau0, G, zmin, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s) {
+    const int threads = 256, wpb = threads / 32;
+    int blocks = (p + wpb - 1) / wpb;
+    compact_kernel<<<blocks, threads, 0, s>>>(G, p, adj, up, st, level);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan_int(const int *cnt, int p, long long *prefix, DevState *st, cudaStream_t s) {
+    row_scan_kernel<int><<<1, 1024, 0, s>>>(cnt, p, prefix, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan_ll(const long long *cnt, int p, long long *prefix, DevState *st, cudaStream_t s) {
+    row_scan_kernel<long long><<<1, 1024, 0, s>>>(cnt, p, prefix, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, const int *up, const long long *prefix,
+                               double tau, bool tau_valid, uint16_t *G, double *zmin, int *sep_dense, int max_level,
+                               int *rec_pool, long long rec_cap, DevState *st, int num_sms, cudaStream_t s) {
+    const int threads = 256;
+    const int blocks = num_sms * 8;
+#define GCSL_LVL(K)                                                                                               \
+    case K:                                                                                                       \
+        gauss_level_reg_kernel<K><<<blocks, threads, 0, s>>>(C, p, adj, up, prefix, tau, tau_valid, G, zmin,     \
+                                                             sep_dense, max_level, rec_pool, rec_cap, st);        \
+        break;
+    switch (L) {
+        GCSL_LVL(1)
+        GCSL_LVL(2)
+        GCSL_LVL(3)
+        GCSL_LVL(4)
+        GCSL_LVL(5)
+        GCSL_LVL(6)
+        GCSL_LVL(7)
+        GCSL_LVL(8)
+    default: {
+        const int t = 128, wpb = t / 32;
+        const int D = L + 2;
+        const size_t smem = (size_t)wpb * (D * (D + 1) / 2 + 2) * sizeof(double) +
+                            (size_t)wpb * (GCSL_MAX_LEVELS + 2) * sizeof(int);
+        gauss_level_smem_kernel<<<num_sms * 4, t, smem, s>>>(C, p, adj, up, prefix, L, tau, tau_valid, G, zmin,
+                                                               sep_dense, max_level, rec_pool, rec_cap, st);
+    }
+    }
+#undef GCSL_LVL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unrank(int K, int L, long long count, int *out, cudaStream_t s) {
+    const long long blocks = (count + 127) / 128;
+    unrank_kernel<<<(int)(blocks > 0 ? (blocks < 65535 ? blocks : 65535) : 1), 128, 0, s>>>(K, L, count, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pmax(const double *zmin, int p, long long n_obs, double *pmax, int num_sms, cudaStream_t s) {
+    const double sq = sqrt((double)(n_obs - 3));
+    pmax_kernel<<<num_sms * 4, 256, 0, s>>>(zmin, p, sq, pmax);
+    return cudaGetLastError();
+}
+
+}  // namespace host
+}  // namespace gcsl

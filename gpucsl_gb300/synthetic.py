@@ -1,0 +1,104 @@
+"""Seeded synthetic workloads with the shapes of the skeleton-discovery benchmarks.
+
+The reference's datasets (coolingData, NCI-60, alarm, link, ...) are downloaded by its
+scripts and are not available offline; these generators stand in for them with the
+same kinds of inputs:
+
+* linear-Gaussian DAG data: a random topological order, each forward pair an edge with
+  probability deg / (p - 1), weights +-U[0.1, 1] with a random sign, N(0, 1) noise,
+  X_v = sum_parents w * X_u + eps_v;
+* discrete Bayesian-network data: an Erdos-Renyi DAG with the same edge law, at most
+  `max_in_degree` parents per node (extra parents dropped), per-variable cardinality
+  uniform in [card_lo, card_hi], conditional probability rows drawn from Dirichlet(1),
+  ancestral sampling, uint8 codes.
+
+All draws come from numpy.random.default_rng(seed) (PCG64).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+
+@dataclass
+class GaussianWorkload:
+    data: np.ndarray          # (n, p) float64 or float32, C order
+    dag: np.ndarray           # (p, p) uint8, dag[u, v] = 1 for u -> v
+    weights: np.ndarray       # (p, p) float64
+    seed: int
+
+
+def random_dag(rng: np.random.Generator, p: int, expected_degree: float) -> np.ndarray:
+    """Adjacency of an ER DAG over a random topological order (dag[u, v] = 1 for u -> v)."""
+    order = rng.permutation(p)
+    prob = 0.0 if p < 2 else min(1.0, expected_degree / (p - 1))
+    upper = np.triu(rng.random((p, p)) < prob, 1)
+    dag = np.zeros((p, p), np.uint8)
+    # position a -> position b (a < b) becomes order[a] -> order[b]
+    dag[np.ix_(order, order)] = upper.astype(np.uint8)
+    return dag
+
+
+def gaussian_dag_data(p: int, n: int, expected_degree: float, seed: int,
+                      dtype=np.float64) -> GaussianWorkload:
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(p)
+    prob = 0.0 if p < 2 else min(1.0, expected_degree / (p - 1))
+    upper = np.triu(rng.random((p, p)) < prob, 1)
+    w = rng.uniform(0.1, 1.0, size=(p, p)) * rng.choice([-1.0, 1.0], size=(p, p))
+    W = np.where(upper, w, 0.0)
+    X = rng.standard_normal((n, p))
+    # positions in topological order: column b of the position-space sample depends on a < b
+    Z = np.empty((n, p))
+    for b in range(p):
+        parents = np.nonzero(W[:, b])[0]
+        Z[:, b] = X[:, b] + (Z[:, parents] @ W[parents, b] if parents.size else 0.0)
+    data = np.empty((n, p))
+    data[:, order] = Z
+    dag = np.zeros((p, p), np.uint8)
+    dag[np.ix_(order, order)] = upper.astype(np.uint8)
+    weights = np.zeros((p, p))
+    weights[np.ix_(order, order)] = W
+    return GaussianWorkload(np.ascontiguousarray(data.astype(dtype)), dag, weights, seed)
+
+
+@dataclass
+class DiscreteWorkload:
+    data: np.ndarray          # (n, p) uint8, C order
+    dag: np.ndarray
+    cardinality: np.ndarray   # (p,) nominal cardinalities
+    seed: int
+
+
+def discrete_bn_data(p: int, n: int, expected_degree: float, seed: int, max_in_degree: int = 3,
+                     card_lo: int = 2, card_hi: int = 5) -> DiscreteWorkload:
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(p)
+    prob = 0.0 if p < 2 else min(1.0, expected_degree / (p - 1))
+    upper = np.triu(rng.random((p, p)) < prob, 1)
+    card = rng.integers(card_lo, card_hi + 1, size=p)
+    Z = np.zeros((n, p), np.int64)
+    kept = np.zeros((p, p), bool)
+    card_pos = card[order]
+    for b in range(p):
+        parents = np.nonzero(upper[:, b])[0]
+        if parents.size > max_in_degree:
+            parents = np.sort(rng.choice(parents, size=max_in_degree, replace=False))
+        kept[parents, b] = True
+        k = int(card_pos[b])
+        n_cfg = int(np.prod(card_pos[parents])) if parents.size else 1
+        cpt = rng.dirichlet(np.ones(k), size=n_cfg)            # (n_cfg, k)
+        cfg = np.zeros(n, np.int64)
+        mult = 1
+        for u in parents:
+            cfg += Z[:, u] * mult
+            mult *= int(card_pos[u])
+        cdf = np.cumsum(cpt[cfg], axis=1)
+        u01 = rng.random(n)[:, None]
+        Z[:, b] = np.minimum((u01 > cdf).sum(1), k - 1)
+    data = np.empty((n, p), np.uint8)
+    data[:, order] = Z.astype(np.uint8)
+    dag = np.zeros((p, p), np.uint8)
+    dag[np.ix_(order, order)] = kept.astype(np.uint8)
+    return DiscreteWorkload(np.ascontiguousarray(data), dag, card, seed)

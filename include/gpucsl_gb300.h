@@ -1,0 +1,116 @@
+/*
+ * gpucsl_gb300 — C ABI of the GB300 (sm_103a) skeleton-discovery kernels.
+ *
+ * Plain pointers and sizes only.  Every buffer argument is a DEVICE pointer owned by
+ * the caller (the library allocates nothing on the hot path; scratch space is a
+ * caller-provided workspace whose size is given by the *_workspace_bytes query).
+ * `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ * All calls enqueue work on `stream`; calls that fill a host `gcsl_stats` synchronise
+ * that stream before returning.  Return value: GCSL_OK or a GCSL_ERR_* code; the
+ * library never aborts and never traps on the device.
+ *
+ * Each entry point names the reference (hpi-epic/gpucsl) interface it replaces.
+ */
+#ifndef GPUCSL_GB300_H
+#define GPUCSL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GCSL_ABI_VERSION 1
+
+#define GCSL_OK 0
+#define GCSL_ERR_INVALID_ARG 1
+#define GCSL_ERR_WORKSPACE 2
+#define GCSL_ERR_UNSUPPORTED_LEVEL 3
+#define GCSL_ERR_TIMEOUT 4
+#define GCSL_ERR_DEVICE 5
+#define GCSL_ERR_CAPACITY 6
+#define GCSL_ERR_UNSUPPORTED 7
+
+#define GCSL_MAX_LEVELS 64
+#define GCSL_DTYPE_F64 0
+#define GCSL_DTYPE_F32 1
+
+/* Per-level counters returned to the host. */
+typedef struct gcsl_stats {
+    int32_t levels_run;            /* levels executed, level 0 included */
+    int32_t status;                /* device status word (GCSL_OK when clean) */
+    int64_t n_records;             /* sepset records written to the record pool */
+    int64_t edges[GCSL_MAX_LEVELS];     /* undirected edges alive at level start */
+    int64_t tests[GCSL_MAX_LEVELS];     /* canonical executed tests */
+    int64_t tests_full[GCSL_MAX_LEVELS];/* full test space sum_dir C(d-1, l) */
+    int64_t removed[GCSL_MAX_LEVELS];   /* edges removed at this level */
+    int32_t max_degree[GCSL_MAX_LEVELS];/* max compacted degree at level start */
+    float level_ms[GCSL_MAX_LEVELS];    /* device time per level (0 when not timed) */
+} gcsl_stats;
+
+/* A sepset record in the int32 record pool: [lo, hi, level, S_0 .. S_{level-1}]. */
+
+int gcsl_version(void);
+const char *gcsl_status_string(int status);
+
+/* ------------------------------------------------------------ correlation (a) */
+/* Replaces gpucsl/pc/helpers.py:58-59 (correlation_matrix_of = np.corrcoef(data,
+ * rowvar=False)), called at gpucsl/pc/discover_skeleton_gaussian.py:134-135.
+ * X: n x p samples, row-major with leading dimension ldx (>= p), FP64 or FP32
+ * (dtype GCSL_DTYPE_*); C: p x p FP64 out.  FP64 arithmetic throughout. */
+size_t gcsl_corr_workspace_bytes(int64_t n, int32_t p);
+int gcsl_corr_f64(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ldx, double *C, void *workspace,
+                  size_t workspace_bytes, void *stream);
+
+/* --------------------------------------------------- Gaussian skeleton (b,c,e) */
+/* Replaces the level loop of gpucsl/pc/discover_skeleton_gaussian.py:30-113
+ * (gaussian_ci_worker) with the kernels of gpucsl/pc/cuda/gaussian_ci.cu:18-120,
+ * compaction (gpucsl/pc/cuda/helpers/graph_helpers.cu:35-56) and the zmin->pmax
+ * epilogue (gpucsl/pc/helpers.py:62-82).
+ *   C            p x p FP64 correlation matrix
+ *   thresholds   HOST array of n_thresholds Fisher-z thresholds (helpers.py:42-50)
+ *   G            p x p uint16 skeleton out (symmetric, zero diagonal)
+ *   sepsets      optional p x p x max_level int32 dense sepsets (pre-filled with -1
+ *                by the caller), or NULL
+ *   rec_pool     optional int32 record pool of rec_cap ints, or NULL
+ *   pmax         p x p FP64 out (upper triangle p-values, -1 on/below the diagonal)
+ *   stats        optional host struct; when given the call synchronises `stream`. */
+size_t gcsl_gauss_workspace_bytes(int32_t p, int32_t max_level);
+int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double *thresholds, int32_t n_thresholds,
+                        int32_t max_level, uint16_t *G, int32_t *sepsets, int32_t *rec_pool, int64_t rec_cap,
+                        double *pmax, gcsl_stats *stats, void *workspace, size_t workspace_bytes, void *stream);
+
+/* ----------------------------------------------------- discrete skeleton (d,e) */
+/* Replaces the level loop of gpucsl/pc/discover_skeleton_discrete.py:80-112 with the
+ * kernels of gpucsl/pc/cuda/discrete_ci.cu:37-246 (+ helpers/discrete_helpers.cu).
+ *   data         p columns of ordinal codes, column-major, column stride ld >= n
+ *                (ld a multiple of 16; bytes in [n, ld) are ignored)
+ *   dims         p uint8 observed cardinalities (discover_skeleton_discrete.py:49)
+ *   other arguments as for gcsl_gauss_skeleton; pmax folds every test (the reference
+ *   tests every rank, discrete_ci.cu:221-244). */
+size_t gcsl_disc_workspace_bytes(int32_t p, int64_t n, int32_t max_level, int32_t max_dim);
+int gcsl_disc_skeleton(const uint8_t *data, int64_t ld, int64_t n, int32_t p, const uint8_t *dims,
+                       int32_t max_dim, double alpha, int32_t max_level, uint16_t *G, int32_t *sepsets,
+                       int32_t *rec_pool, int64_t rec_cap, double *pmax, gcsl_stats *stats, void *workspace,
+                       size_t workspace_bytes, void *stream);
+
+/* ------------------------------------------------------------- unit kernels */
+/* Single-kernel entry points used by the parity tests, mirroring the reference's
+ * PYTHON_TEST kernels (tests/test_cuda_graph_helpers.py, test_cuda_set_helpers.py,
+ * test_cuda_discrete_helpers.py). */
+/* graph_helpers.cu:35-56: G (p x p uint16) -> adj (p x p int32 [deg, nbrs...]). */
+int gcsl_compact(const uint16_t *G, int32_t p, int32_t *adj, void *stream);
+/* set_helpers.cu:25-49: out[r * level + c] = 1-based positions of rank r, r < count. */
+int gcsl_unrank(int32_t K, int32_t level, int64_t count, int32_t *out, void *stream);
+/* math_helpers.cu:128-175: out[k] = pchisq(x[k], df[k]). */
+int gcsl_pchisq(const double *x, const int64_t *df, int64_t count, double *out, void *stream);
+/* discrete_helpers.cu:40-85 + 120-186: counts (dim_s*d_i*d_j uint32) and chi^2 of one
+ * test; S is a host array of `level` variable ids. */
+int gcsl_disc_table(const uint8_t *data, int64_t ld, int64_t n, const uint8_t *dims, int32_t vi, int32_t vj,
+                    const int32_t *S, int32_t level, uint32_t *counts, double *chi2_pvalue, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
