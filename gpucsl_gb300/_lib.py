@@ -107,7 +107,7 @@ def lib() -> ct.CDLL:
     L.gcsl_pchisq.restype = ct.c_int
     L.gcsl_pchisq.argtypes = [_vp, _vp, _i64, _vp, _vp]
     L.gcsl_disc_table.restype = ct.c_int
-    L.gcsl_disc_table.argtypes = [_vp, _i64, _i64, _vp, _i32, _i32, ct.POINTER(_i32), _i32, _vp, _vp, _vp]
+    L.gcsl_disc_table.argtypes = [_vp, _i64, _i64, _vp, _i32, _i32, ct.POINTER(_i32), _i32, _vp, _i64, _vp, _vp]
     if L.gcsl_version() != 1:
         raise RuntimeError("libgpucsl_gb300.so ABI version mismatch")
     return L

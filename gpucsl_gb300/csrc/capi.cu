@@ -36,7 +36,8 @@ cudaError_t launch_disc_level_stats(const long long *prefix, const int *adj, int
                                     cudaStream_t s);
 cudaError_t launch_pmax_finish(double *pmax, int p, int num_sms, cudaStream_t s);
 cudaError_t launch_disc_table(const uint8_t *data, long long ld, long long n, const uint8_t *dims, int vi, int vj,
-                              const int *S, int L, int table_cap, uint32_t *counts, double *out2, cudaStream_t s);
+                              const int *S, int L, int table_cap, uint32_t *counts, long long counts_cap, double *out2,
+                              cudaStream_t s);
 cudaError_t launch_pchisq(const double *x, const long long *df, long long count, double *out, cudaStream_t s);
 cudaError_t launch_unrank(int K, int L, long long count, int *out, cudaStream_t s);
 }  // namespace host
@@ -294,14 +295,15 @@ int gcsl_pchisq(const double *x, const int64_t *df, int64_t count, double *out, 
 }
 
 int gcsl_disc_table(const uint8_t *data, int64_t ld, int64_t n, const uint8_t *dims, int32_t vi, int32_t vj,
-                    const int32_t *S, int32_t level, uint32_t *counts, double *chi2_pvalue, void *stream) {
-    if (!data || !dims || !counts || !chi2_pvalue || n < 1 || ld < n || (ld % 16) != 0 || level < 0 ||
+                    const int32_t *S, int32_t level, uint32_t *counts, int64_t counts_cap, double *chi2_pvalue,
+                    void *stream) {
+    if (!data || !dims || !counts || !chi2_pvalue || n < 1 || ld < n || (ld % 16) != 0 || level < 0 || counts_cap < 1 ||
         level >= GCSL_MAX_LEVELS || (level > 0 && !S) || reinterpret_cast<uintptr_t>(data) % 16 != 0)
         return GCSL_ERR_INVALID_ARG;
     int dev = 0;
     cudaGetDevice(&dev);
     return map_cuda(host::launch_disc_table(data, ld, n, dims, vi, vj, S, level, host::disc_table_cap(dev), counts,
-                                            chi2_pvalue, static_cast<cudaStream_t>(stream)));
+                                            counts_cap, chi2_pvalue, static_cast<cudaStream_t>(stream)));
 }
 
 }  // extern "C"

@@ -330,7 +330,8 @@ struct UnitSet {
 
 __global__ void __launch_bounds__(256) disc_table_kernel(const uint8_t *data, long long ld, long long n,
                                                          const uint8_t *dims, int vi, int vj, UnitSet us, int L,
-                                                         int table_cap, uint32_t *counts, double *out2) {
+                                                         int table_cap, uint32_t *counts, long long counts_cap,
+                                                         double *out2) {
     extern __shared__ uint32_t sm_tab[];
     __shared__ int s_S[GCSL_MAX_LEVELS + 2];
     __shared__ int s_mult[GCSL_MAX_LEVELS + 2];
@@ -339,7 +340,8 @@ __global__ void __launch_bounds__(256) disc_table_kernel(const uint8_t *data, lo
     if (threadIdx.x == 0) {
         for (int k = 0; k < L; ++k) s_S[k] = us.S[k];
         int dim_s = 0, di = 0, dj = 0, copies = 1;
-        const bool ok = table_geometry(dims, s_S, s_mult, L, vi, vj, table_cap, dim_s, di, dj, copies);
+        bool ok = table_geometry(dims, s_S, s_mult, L, vi, vj, table_cap, dim_s, di, dj, copies);
+        if (ok && (long long)dim_s * di * dj > counts_cap) ok = false;  // never write past the caller's buffer
         s_hdr[0] = ok ? dim_s : -1;
         s_hdr[1] = di;
         s_hdr[2] = dj;
@@ -495,12 +497,13 @@ cudaError_t launch_pmax_finish(double *pmax, int p, int num_sms, cudaStream_t s)
 }
 
 cudaError_t launch_disc_table(const uint8_t *data, long long ld, long long n, const uint8_t *dims, int vi, int vj,
-                              const int *S, int L, int table_cap, uint32_t *counts, double *out2, cudaStream_t s) {
+                              const int *S, int L, int table_cap, uint32_t *counts, long long counts_cap, double *out2,
+                              cudaStream_t s) {
     UnitSet us;
     for (int k = 0; k < GCSL_MAX_LEVELS; ++k) us.S[k] = k < L ? S[k] : 0;
     const size_t smem = (size_t)table_cap * sizeof(uint32_t);
     cudaFuncSetAttribute(disc_table_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    disc_table_kernel<<<1, 256, smem, s>>>(data, ld, n, dims, vi, vj, us, L, table_cap, counts, out2);
+    disc_table_kernel<<<1, 256, smem, s>>>(data, ld, n, dims, vi, vj, us, L, table_cap, counts, counts_cap, out2);
     return cudaGetLastError();
 }
 

@@ -105,10 +105,13 @@ int gcsl_compact(const uint16_t *G, int32_t p, int32_t *adj, void *stream);
 int gcsl_unrank(int32_t K, int32_t level, int64_t count, int32_t *out, void *stream);
 /* math_helpers.cu:128-175: out[k] = pchisq(x[k], df[k]). */
 int gcsl_pchisq(const double *x, const int64_t *df, int64_t count, double *out, void *stream);
-/* discrete_helpers.cu:40-85 + 120-186: counts (dim_s*d_i*d_j uint32) and chi^2 of one
- * test; S is a host array of `level` variable ids. */
+/* discrete_helpers.cu:40-85 + 120-186: counts (dim_s*d_i*d_j uint32, at most counts_cap
+ * are written) and chi^2 + p-value of one test; S is a host array of `level` variable
+ * ids.  chi2_pvalue receives -1, -1 when the table does not fit counts_cap or the
+ * shared-memory table, or when a code is not below its cardinality. */
 int gcsl_disc_table(const uint8_t *data, int64_t ld, int64_t n, const uint8_t *dims, int32_t vi, int32_t vj,
-                    const int32_t *S, int32_t level, uint32_t *counts, double *chi2_pvalue, void *stream);
+                    const int32_t *S, int32_t level, uint32_t *counts, int64_t counts_cap, double *chi2_pvalue,
+                    void *stream);
 
 #ifdef __cplusplus
 }

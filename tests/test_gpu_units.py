@@ -128,13 +128,16 @@ def _disc_table(torch, data_cols, n, dims, vi, vj, S):
     buf[:, :n] = data_cols
     d = torch.from_numpy(buf).cuda()
     dm = torch.from_numpy(np.asarray(dims, np.uint8)).cuda()
-    dim_s = int(np.prod([dims[s] for s in S])) if len(S) else 1
-    T = dim_s * dims[vi] * dims[vj]
+    dims_i = [int(d) for d in dims]  # Python ints: uint8 products would wrap
+    dim_s = 1
+    for s in S:
+        dim_s *= dims_i[s]
+    T = dim_s * dims_i[vi] * dims_i[vj]
     counts = torch.zeros(T, dtype=torch.int32, device="cuda")
     out2 = torch.zeros(2, dtype=torch.float64, device="cuda")
     Sarr = (ct.c_int32 * max(1, len(S)))(*[int(s) for s in S])
     lib.check(lib.lib().gcsl_disc_table(d.data_ptr(), ld, n, dm.data_ptr(), vi, vj, Sarr, len(S), counts.data_ptr(),
-                                        out2.data_ptr(), lib.stream_ptr()), "disc_table")
+                                        T, out2.data_ptr(), lib.stream_ptr()), "disc_table")
     return counts.cpu().numpy().view(np.uint32), out2.cpu().numpy()
 
 
@@ -163,14 +166,16 @@ def test_contingency_and_chi2_vs_oracle(cuda, n, level):
     cols = np.stack([rng.integers(0, dims[v], n) for v in range(p)]).astype(np.uint8)
     S = sorted(rng.choice(np.arange(2, p), size=level, replace=False).tolist())
     counts, out2 = _disc_table(cuda, cols, n, dims, 0, 1, S)
-    ref_counts = np.zeros_like(counts)
+    ref_counts = np.zeros(counts.size, np.uint32)
     Sa = np.array(S if S else [0], np.int32)
-    cbind.lib().orc_contingency(cbind.ptr(np.ascontiguousarray(cols)), n, n, cbind.ptr(dims), 0, 1,
+    colc = np.ascontiguousarray(cols)
+    dimc = np.ascontiguousarray(dims, dtype=np.uint8)
+    cbind.lib().orc_contingency(cbind.ptr(colc), n, n, cbind.ptr(dimc), 0, 1,
                                 cbind.ptr(Sa) if S else None, level, cbind.ptr(ref_counts))
     assert (counts == ref_counts).all()
     chi = ct.c_double()
     work = np.zeros(counts.size + 4, np.uint32)
-    pv = cbind.lib().orc_discrete_test(cbind.ptr(np.ascontiguousarray(cols)), n, n, cbind.ptr(dims), 0, 1,
+    pv = cbind.lib().orc_discrete_test(cbind.ptr(colc), n, n, cbind.ptr(dimc), 0, 1,
                                        cbind.ptr(Sa) if S else None, level, cbind.ptr(work), ct.byref(chi))
     assert out2[0] == chi.value  # same operations in the same order
     assert abs(out2[1] - pv) <= 1e-12 * max(abs(pv), 1e-300)
