@@ -1,0 +1,431 @@
+#!/usr/bin/env python
+"""Benchmark: conditional-independence tests per second of the Gaussian PC-stable
+skeleton on one GB300 (p = 1000 variables, n = 10000 samples of a seeded
+linear-Gaussian DAG with expected degree 3, alpha = 0.01, levels run until no edge has
+enough neighbours).
+
+One step = one skeleton solve from the FP64 samples resident in HBM: correlation
+matrix (FP64), level 0, every level l until termination, zmin -> pmax.  The metric is
+the canonical executed-test count of a step (identical for every implementation: per
+edge, tests in key order up to and including the first removing test) divided by the
+step time.  `e2e` is the same metric through the C ABI from pinned host samples, with
+the host->device copy of the samples and the device->host read of skeleton, pmax and
+sepset records inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpucsl_gb300|reference]
+
+--impl reference times the CPU restatement of the reference's skeleton loop (the
+reference has no CPU path of its own; its GPU code needs cupy, which is not installed)
+on the host cores, on the same workload and metric.  Under torchrun each rank solves
+its own instance (replicas; the skeleton has no data-path exchange), and the value is
+the tests of all ranks divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+P, N, DEG, SEED, ALPHA = 1000, 10000, 3, 2, 0.01
+METRIC = "CI tests/s"
+UNIT = "tests/s"
+WORKLOAD = "gaussian_skeleton_p1000_n10000_deg3_alpha0.01_to_termination"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpucsl_gb300", choices=["gpucsl_gb300", "reference"])
+    ap.add_argument("--no-extras", action="store_true", help="skip the discrete and CPU-baseline legs")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------- distributed
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        import torch
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# -------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        self.t0 = time.time()
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append(parts)
+            except Exception:
+                pass
+        os.unlink(self.path)
+        if not rows:
+            return None
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return float("nan")
+
+        sm = [num(r[1]) for r in rows]
+        mx = [num(r[2]) for r in rows]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        load = [s for s in sm if s == s]
+        return {"sm_mhz": statistics.median(load) if load else None,
+                "sm_max_mhz": max(m for m in mx if m == m) if any(m == m for m in mx) else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# --------------------------------------------------------------------- helpers
+def fp64_gemm_peak(torch) -> float:
+    """Measured FP64 rate (cuBLAS DGEMM, 4096^3, best of 3) in TFLOP/s: the FP64-pipe
+    denominator of the correlation kernel's roofline."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    del a, b
+    return 2 * 4096 ** 3 / best / 1e12
+
+
+def read_profile_traffic() -> int | None:
+    """DRAM bytes per launch of the correlation tile kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "cov_tile_kernel_p1000_n10000.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return int(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_oracle_solve(data):
+    """One CPU solve with the oracle (numpy FP64): correlation + level loop + pmax."""
+    from oracle import gaussian as og
+
+    C = og.corrcoef(data)
+    return og.skeleton(C, data.shape[0], ALPHA, P - 2)
+
+
+def blas_threads() -> int:
+    try:
+        from threadpoolctl import threadpool_info
+
+        n = [i.get("num_threads", 0) for i in threadpool_info() if i.get("user_api") == "blas"]
+        if n:
+            return int(max(n))
+    except Exception:
+        pass
+    return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    from gpucsl_gb300 import _lib, build as gbuild, engine
+    from gpucsl_gb300.synthetic import discrete_bn_data, gaussian_dag_data
+    from oracle import gaussian as og
+
+    gbuild.build()
+    torch.cuda.set_device(local)
+    L = _lib.lib()
+    w = gaussian_dag_data(P, N, DEG, SEED)
+    thr = og.thresholds(N, ALPHA)
+    X = torch.from_numpy(w.data).cuda()
+    solver = engine.GaussianSolver(P, P - 2)
+    corr_ws = torch.empty(int(L.gcsl_corr_workspace_bytes(N, P)), dtype=torch.uint8, device="cuda")
+    C = torch.empty((P, P), dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def step():
+        engine.correlation(X, out=C, workspace=corr_ws)
+        return solver.run(C, N, thr)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    for _ in range(max(args.warmup, 3)):
+        st = step()
+    torch.cuda.synchronize()
+    E = st.tests
+    levels_run = st.levels_run
+
+    # ---- timed region: K steps, L2 flushed between steps (outside the events)
+    barrier(world)
+    torch.cuda.synchronize()
+    launches0 = int(L.gcsl_kernel_launches())
+    t_step, t_corr = [], []
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        a, b, c = evs[k]
+        a.record()
+        engine.correlation(X, out=C, workspace=corr_ws)
+        b.record()
+        solver.run(C, N, thr)
+        c.record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = int(L.gcsl_kernel_launches()) - launches0
+    barrier(world)
+    for a, b, c in evs:
+        t_corr.append(a.elapsed_time(b) / 1e3)
+        t_step.append(a.elapsed_time(c) / 1e3)
+    total = max_over_ranks(sum(t_step), world)
+    value = world * E * args.steps / total
+
+    # ---- level loop alone (correlation matrix given, the reference benchmark's convention)
+    t_lv = []
+    for _ in range(max(5, args.steps // 3)):
+        flush.zero_()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        solver.run(C, N, thr)
+        s1.record()
+        torch.cuda.synchronize()
+        t_lv.append(s0.elapsed_time(s1) / 1e3)
+
+    # ---- e2e through the C ABI from pinned host samples
+    Xh = torch.from_numpy(w.data).pin_memory()
+    Gh = torch.empty((P, P), dtype=torch.int16).pin_memory()
+    Ph = torch.empty((P, P), dtype=torch.float64).pin_memory()
+    Rh = torch.empty(solver.rec.numel(), dtype=torch.int32).pin_memory()
+    Xd = torch.empty_like(X)
+    t_e2e, d2h_bytes = [], 0
+    for it in range(max(3, args.steps // 2) + 1):
+        flush.zero_()
+        torch.cuda.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        Xd.copy_(Xh, non_blocking=True)
+        engine.correlation(Xd, out=C, workspace=corr_ws)
+        stt = solver.run(C, N, thr)
+        nrec = int(stt.raw["n_records"])
+        Gh.copy_(solver.G, non_blocking=True)
+        Ph.copy_(solver.pmax, non_blocking=True)
+        if nrec:
+            Rh[:nrec].copy_(solver.rec[:nrec], non_blocking=True)
+        s1.record()
+        torch.cuda.synchronize()
+        if it > 0:  # first iteration warms the pinned path
+            t_e2e.append(s0.elapsed_time(s1) / 1e3)
+        d2h_bytes = Gh.numel() * 2 + Ph.numel() * 8 + nrec * 4
+    e2e_total = max_over_ranks(sum(t_e2e), world)
+    e2e_value = world * E * len(t_e2e) / e2e_total
+
+    clocks = sampler.stop()
+
+    # ---- roofline of the dominant kernel (the FP64 correlation GEMM)
+    peak = fp64_gemm_peak(torch)
+    corr_s = statistics.mean(t_corr)
+    corr_flops = N * P * (P + 1)  # symmetric rank-n update X_c^T X_c: n p (p + 1) FLOPs
+    achieved = corr_flops / corr_s / 1e12
+    traffic = read_profile_traffic()
+    roofline = {"bound": "fp64", "kernel": "cov_tile_kernel (correlation build, FP64 DFMA)",
+                "achieved": round(achieved, 4), "peak": round(peak, 4), "unit": "TFLOP/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FP64 is not in MEASURED_PEAKS.json)",
+                "share_of_step": round(corr_s / statistics.mean(t_step), 4),
+                "algorithmic_flops_per_launch": corr_flops}
+
+    out = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "ms_per_step": round(1e3 * total / args.steps, 4),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded linear-Gaussian DAG, numpy PCG64 seed 2)",
+           "config": {"workload": WORKLOAD, "p": P, "n": N, "expected_degree": DEG, "alpha": ALPHA,
+                      "max_level": P - 2, "levels_run": levels_run, "tests_per_step": E,
+                      "step": "FP64 correlation + levels 0..termination + pmax, samples resident in HBM",
+                      "l2": "flushed between steps (256 MB write outside the timed events)",
+                      "parallelism": f"replicas x{world}"},
+           "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": int(Xh.numel() * 8),
+                   "d2h_bytes_per_step": int(d2h_bytes), "ms_per_step": round(1e3 * e2e_total / len(t_e2e), 4)},
+           "level_loop": {"value": round(E / statistics.mean(t_lv), 1), "unit": UNIT,
+                          "ms_per_solve": round(1e3 * statistics.mean(t_lv), 4),
+                          "note": "correlation matrix given (the reference benchmark's timing convention)"},
+           "roofline": roofline, "gpu_launches": launches, "wall_s_timed_region": round(wall, 4),
+           "clocks": clocks}
+
+    # ---- discrete workload (p=200, n=50000, cardinality 2..5, alpha 0.05, max level 3)
+    if not args.no_extras and rank == 0:
+        d = discrete_bn_data(200, 50000, 2, 3)
+        codes, dims = engine.ordinal_encode(d.data)
+        ds = engine.DiscreteSolver(200, 50000, 3, int(dims.max()))
+        ds.load(codes, dims)
+        ds.run(0.05)
+        torch.cuda.synchronize()
+        td = []
+        for _ in range(3):
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record()
+            std = ds.run(0.05)
+            s1.record()
+            torch.cuda.synchronize()
+            td.append(s0.elapsed_time(s1) / 1e3)
+        Ed = int(sum(std.raw["tests"]))
+        nb = sum(int(t) for t in std.raw["tests"])
+        out["discrete"] = {"workload": "discrete_skeleton_p200_n50000_card2-5_alpha0.05_L3",
+                           "value": round(Ed / statistics.mean(td), 1), "unit": UNIT,
+                           "ms_per_solve": round(1e3 * statistics.mean(td), 3), "tests_per_solve": Ed,
+                           "levels_run": std.raw["levels_run"]}
+
+    # ---- CPU baseline: the oracle on the host cores (rank 0, N = 1 only)
+    if not args.no_extras and rank == 0 and world == 1:
+        t0 = time.perf_counter()
+        times = []
+        while True:
+            s = time.perf_counter()
+            r = cpu_oracle_solve(w.data)
+            times.append(time.perf_counter() - s)
+            if time.perf_counter() - t0 > 10.0 or len(times) >= 3:
+                break
+        assert r.tests_canonical == E, (r.tests_canonical, E)
+        out["cpu_baseline"] = {"value": round(E / statistics.mean(times), 1), "unit": UNIT,
+                               "cores": blas_threads(), "kind": "port",
+                               "sample": f"{len(times)} full solves of the same workload "
+                                         f"(numpy corrcoef on {blas_threads()} BLAS threads, level loop "
+                                         f"single-threaded numpy), mean {statistics.mean(times):.2f} s"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------ reference arm
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from gpucsl_gb300.synthetic import gaussian_dag_data
+
+    w = gaussian_dag_data(P, N, DEG, SEED)
+    for _ in range(max(args.warmup, 1)):
+        r = cpu_oracle_solve(w.data)
+    E = r.tests_canonical
+    times = []
+    for _ in range(args.steps):
+        s = time.perf_counter()
+        cpu_oracle_solve(w.data)
+        times.append(time.perf_counter() - s)
+    value = E * len(times) / sum(times)
+    cores = blas_threads()
+    out = {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded linear-Gaussian DAG, numpy PCG64 seed 2)",
+           "config": {"workload": WORKLOAD, "p": P, "n": N, "alpha": ALPHA, "tests_per_step": E,
+                      "levels_run": len(r.levels)},
+           "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"{len(times)} full solves (numpy corrcoef on {cores} BLAS threads, "
+                                      "level loop single-threaded numpy); the reference itself has no CPU path "
+                                      "and its GPU code needs cupy, absent here"},
+           "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -27,7 +27,7 @@ GCSL_DTYPE_F32 = 1
 
 # every symbol the header declares (checked by the CPU test-suite)
 EXPORTED = [
-    "gcsl_version", "gcsl_status_string",
+    "gcsl_version", "gcsl_status_string", "gcsl_kernel_launches",
     "gcsl_corr_workspace_bytes", "gcsl_corr_f64",
     "gcsl_gauss_workspace_bytes", "gcsl_gauss_skeleton",
     "gcsl_disc_workspace_bytes", "gcsl_disc_skeleton",
@@ -84,6 +84,8 @@ def lib() -> ct.CDLL:
     L = ct.CDLL(str(LIB_PATH))
     L.gcsl_version.restype = ct.c_int
     L.gcsl_version.argtypes = []
+    L.gcsl_kernel_launches.restype = ct.c_int64
+    L.gcsl_kernel_launches.argtypes = []
     L.gcsl_status_string.restype = ct.c_char_p
     L.gcsl_status_string.argtypes = [ct.c_int]
     L.gcsl_corr_workspace_bytes.restype = _sz

@@ -45,6 +45,10 @@ cudaError_t launch_unrank(int K, int L, long long count, int *out, cudaStream_t 
 
 using namespace gcsl;
 
+#include <atomic>
+static std::atomic<long long> g_kernel_launches{0};
+void gcsl::host::note_launch(int kernels) { g_kernel_launches.fetch_add(kernels, std::memory_order_relaxed); }
+
 namespace {
 
 constexpr size_t kAlign = 256;
@@ -172,6 +176,8 @@ DiscWs carve_disc(void *ws, size_t cap, int p) {
 extern "C" {
 
 int gcsl_version(void) { return GCSL_ABI_VERSION; }
+
+int64_t gcsl_kernel_launches(void) { return (int64_t)g_kernel_launches.load(std::memory_order_relaxed); }
 
 const char *gcsl_status_string(int status) {
     switch (status) {

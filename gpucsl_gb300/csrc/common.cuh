@@ -16,6 +16,10 @@
 #define GCSL_RANK_LIMIT (1ll << 56)
 
 namespace gcsl {
+namespace host {
+// Count of kernels this library has launched (process-wide, for instrumentation).
+void note_launch(int kernels);
+}  // namespace host
 
 // Device-side state of one skeleton solve.  Per-level slots are written once per
 // level, so no counter has to be reset between levels.

@@ -135,13 +135,18 @@ static cudaError_t corr_impl(const T *X, long long n, int p, long long ldx, doub
     double *sd = mean + p;
     dim3 g1((p + 127) / 128, (unsigned)chunks);
     col_partial_sums_kernel<T><<<g1, 128, 0, s>>>(X, n, p, ldx, partial);
+    note_launch(1);
     col_mean_kernel<<<(p + 127) / 128, 128, 0, s>>>(partial, n, p, (int)chunks, mean);
+    note_launch(1);
     const int nb = (p + CT - 1) / CT;
     const int tiles = nb * (nb + 1) / 2;
     const double scale = 1.0 / (double)(n - 1);
     cov_tile_kernel<T><<<tiles, 256, 0, s>>>(X, n, p, ldx, mean, scale, C);
+    note_launch(1);
     diag_sqrt_kernel<<<(p + 127) / 128, 128, 0, s>>>(C, p, sd);
+    note_launch(1);
     normalize_kernel<<<num_sms * 4, 256, 0, s>>>(C, p, sd);
+    note_launch(1);
     return cudaGetLastError();
 }
 

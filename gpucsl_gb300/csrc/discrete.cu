@@ -470,11 +470,13 @@ cudaError_t launch_disc_tests(const DiscLevelArgs &A, int num_sms, cudaStream_t 
         attr_set = true;
     }
     disc_test_kernel<<<num_sms * 4, 256, smem, s>>>(A);
+    note_launch(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_disc_weights(const int *adj, int p, int L, long long *w, DevState *st, cudaStream_t s) {
     disc_weights_kernel<<<(p + 255) / 256, 256, 0, s>>>(adj, p, L, w, st);
+    note_launch(1);
     return cudaGetLastError();
 }
 
@@ -482,17 +484,20 @@ cudaError_t launch_disc_finalize(const int *adj, int p, int L, uint16_t *G, unsi
                                  int max_level, int *rec, long long rec_cap, DevState *st, int num_sms,
                                  cudaStream_t s) {
     disc_finalize_kernel<<<num_sms * 2, 256, 0, s>>>(adj, p, L, G, win, sep, max_level, rec, rec_cap, st);
+    note_launch(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_disc_level_stats(const long long *prefix, const int *adj, int p, int L, DevState *st,
                                     cudaStream_t s) {
     disc_level_stats_kernel<<<(p + 255) / 256, 256, 0, s>>>(prefix, adj, p, L, st);
+    note_launch(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pmax_finish(double *pmax, int p, int num_sms, cudaStream_t s) {
     pmax_finish_kernel<<<num_sms * 2, 256, 0, s>>>(pmax, p);
+    note_launch(1);
     return cudaGetLastError();
 }
 
@@ -504,12 +509,14 @@ cudaError_t launch_disc_table(const uint8_t *data, long long ld, long long n, co
     const size_t smem = (size_t)table_cap * sizeof(uint32_t);
     cudaFuncSetAttribute(disc_table_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     disc_table_kernel<<<1, 256, smem, s>>>(data, ld, n, dims, vi, vj, us, L, table_cap, counts, counts_cap, out2);
+    note_launch(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pchisq(const double *x, const long long *df, long long count, double *out, cudaStream_t s) {
     const int blocks = (int)((count + 255) / 256);
     pchisq_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(x, df, count, out);
+    note_launch(1);
     return cudaGetLastError();
 }
 

@@ -450,6 +450,7 @@ cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, doub
     const int threads = 256, warps_per_block = threads / 32;
     int blocks = (p + warps_per_block - 1) / warps_per_block;
     gauss_level0_kernel<<<blocks, threads, 0, s>>>(C, p, tau0, G, zmin, st);
+    note_launch(1);
     return cudaGetLastError();
 }
 
@@ -457,16 +458,19 @@ cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState
     const int threads = 256, wpb = threads / 32;
     int blocks = (p + wpb - 1) / wpb;
     compact_kernel<<<blocks, threads, 0, s>>>(G, p, adj, up, st, level);
+    note_launch(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_scan_int(const int *cnt, int p, long long *prefix, DevState *st, cudaStream_t s) {
     row_scan_kernel<int><<<1, 1024, 0, s>>>(cnt, p, prefix, st);
+    note_launch(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_scan_ll(const long long *cnt, int p, long long *prefix, DevState *st, cudaStream_t s) {
     row_scan_kernel<long long><<<1, 1024, 0, s>>>(cnt, p, prefix, st);
+    note_launch(1);
     return cudaGetLastError();
 }
 
@@ -501,18 +505,21 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
     }
     }
 #undef GCSL_LVL
+    note_launch(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_unrank(int K, int L, long long count, int *out, cudaStream_t s) {
     const long long blocks = (count + 127) / 128;
     unrank_kernel<<<(int)(blocks > 0 ? (blocks < 65535 ? blocks : 65535) : 1), 128, 0, s>>>(K, L, count, out);
+    note_launch(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pmax(const double *zmin, int p, long long n_obs, double *pmax, int num_sms, cudaStream_t s) {
     const double sq = sqrt((double)(n_obs - 3));
     pmax_kernel<<<num_sms * 4, 256, 0, s>>>(zmin, p, sq, pmax);
+    note_launch(1);
     return cudaGetLastError();
 }
 

@@ -53,6 +53,9 @@ typedef struct gcsl_stats {
 
 int gcsl_version(void);
 const char *gcsl_status_string(int status);
+/* Number of kernels this library has launched in this process (instrumentation; no
+ * reference counterpart). */
+int64_t gcsl_kernel_launches(void);
 
 /* ------------------------------------------------------------ correlation (a) */
 /* Replaces gpucsl/pc/helpers.py:58-59 (correlation_matrix_of = np.corrcoef(data,
