@@ -29,7 +29,7 @@ GCSL_DTYPE_F32 = 1
 EXPORTED = [
     "gcsl_version", "gcsl_status_string", "gcsl_kernel_launches",
     "gcsl_corr_workspace_bytes", "gcsl_corr_f64",
-    "gcsl_gauss_workspace_bytes", "gcsl_gauss_skeleton",
+    "gcsl_gauss_workspace_bytes", "gcsl_gauss_skeleton", "gcsl_gauss_skeleton_noalloc",
     "gcsl_disc_workspace_bytes", "gcsl_disc_skeleton",
     "gcsl_compact", "gcsl_unrank", "gcsl_pchisq", "gcsl_disc_table",
 ]
@@ -97,6 +97,9 @@ def lib() -> ct.CDLL:
     L.gcsl_gauss_skeleton.restype = ct.c_int
     L.gcsl_gauss_skeleton.argtypes = [_vp, _i32, _i64, ct.POINTER(_dbl), _i32, _i32, _vp, _vp, _vp, _i64, _vp,
                                       ct.POINTER(GcslStats), _vp, _sz, _vp]
+    L.gcsl_gauss_skeleton_noalloc.restype = ct.c_int
+    L.gcsl_gauss_skeleton_noalloc.argtypes = [_vp, _i32, _i64, ct.POINTER(_dbl), _i32, _i32, _vp, _vp, _vp, _i64,
+                                              _vp, ct.POINTER(GcslStats), _vp]
     L.gcsl_disc_workspace_bytes.restype = _sz
     L.gcsl_disc_workspace_bytes.argtypes = [_i32, _i64, _i32, _i32]
     L.gcsl_disc_skeleton.restype = ct.c_int

@@ -84,6 +84,20 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
                         int32_t max_level, uint16_t *G, int32_t *sepsets, int32_t *rec_pool, int64_t rec_cap,
                         double *pmax, gcsl_stats *stats, void *workspace, size_t workspace_bytes, void *stream);
 
+/* Allocation-free variant of gcsl_gauss_skeleton (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc, e.g. a host runtime whose allocator owns
+ * all device memory after start-up.  Same arguments and results as gcsl_gauss_skeleton
+ * minus the workspace: the scratch space is a static device array of
+ * GCSL_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until exit.
+ * p > GCSL_NOALLOC_MAX_P returns GCSL_ERR_UNSUPPORTED.  The first call on a device looks
+ * up the array's address (make it before any stream capture); calls share the array,
+ * so calls whose device work overlaps race and must be serialised. */
+#define GCSL_NOALLOC_MAX_P 512
+#define GCSL_NOALLOC_SCRATCH_BYTES 3211264
+int gcsl_gauss_skeleton_noalloc(const double *C, int32_t p, int64_t n_obs, const double *thresholds,
+                                int32_t n_thresholds, int32_t max_level, uint16_t *G, int32_t *sepsets,
+                                int32_t *rec_pool, int64_t rec_cap, double *pmax, gcsl_stats *stats, void *stream);
+
 /* ----------------------------------------------------- discrete skeleton (d,e) */
 /* Replaces the level loop of gpucsl/pc/discover_skeleton_discrete.py:80-112 with the
  * kernels of gpucsl/pc/cuda/discrete_ci.cu:37-246 (+ helpers/discrete_helpers.cu).
