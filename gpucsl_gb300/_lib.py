@@ -31,7 +31,7 @@ EXPORTED = [
     "gcsl_corr_workspace_bytes", "gcsl_corr_f64",
     "gcsl_gauss_workspace_bytes", "gcsl_gauss_skeleton", "gcsl_gauss_skeleton_noalloc",
     "gcsl_disc_workspace_bytes", "gcsl_disc_skeleton",
-    "gcsl_compact", "gcsl_unrank", "gcsl_pchisq", "gcsl_disc_table",
+    "gcsl_compact", "gcsl_unrank", "gcsl_pchisq", "gcsl_disc_table", "gcsl_tc_gemm_bf16",
 ]
 
 
@@ -113,6 +113,8 @@ def lib() -> ct.CDLL:
     L.gcsl_pchisq.argtypes = [_vp, _vp, _i64, _vp, _vp]
     L.gcsl_disc_table.restype = ct.c_int
     L.gcsl_disc_table.argtypes = [_vp, _i64, _i64, _vp, _i32, _i32, ct.POINTER(_i32), _i32, _vp, _i64, _vp, _vp]
+    L.gcsl_tc_gemm_bf16.restype = ct.c_int
+    L.gcsl_tc_gemm_bf16.argtypes = [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp]
     if L.gcsl_version() != 1:
         raise RuntimeError("libgpucsl_gb300.so ABI version mismatch")
     return L

@@ -40,6 +40,8 @@ cudaError_t launch_disc_table(const uint8_t *data, long long ld, long long n, co
                               cudaStream_t s);
 cudaError_t launch_pchisq(const double *x, const long long *df, long long count, double *out, cudaStream_t s);
 cudaError_t launch_unrank(int K, int L, long long count, int *out, cudaStream_t s);
+cudaError_t launch_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, float *D, int M, int N, int K, int *err,
+                                cudaStream_t s);
 }  // namespace host
 }  // namespace gcsl
 
@@ -310,6 +312,14 @@ int gcsl_disc_table(const uint8_t *data, int64_t ld, int64_t n, const uint8_t *d
     cudaGetDevice(&dev);
     return map_cuda(host::launch_disc_table(data, ld, n, dims, vi, vj, S, level, host::disc_table_cap(dev), counts,
                                             counts_cap, chi2_pvalue, static_cast<cudaStream_t>(stream)));
+}
+
+int gcsl_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, float *D, int32_t M, int32_t N, int32_t K, int32_t *err,
+                      void *stream) {
+    if (!A || !B || !D || !err || M < 128 || N < 128 || K < 64 || M % 128 || N % 128 || K % 64 ||
+        reinterpret_cast<uintptr_t>(A) % 16 || reinterpret_cast<uintptr_t>(B) % 16)
+        return GCSL_ERR_INVALID_ARG;
+    return map_cuda(host::launch_tc_gemm_bf16(A, B, D, M, N, K, err, static_cast<cudaStream_t>(stream)));
 }
 
 }  // extern "C"

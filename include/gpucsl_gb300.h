@@ -130,6 +130,13 @@ int gcsl_disc_table(const uint8_t *data, int64_t ld, int64_t n, const uint8_t *d
                     const int32_t *S, int32_t level, uint32_t *counts, int64_t counts_cap, double *chi2_pvalue,
                     void *stream);
 
+/* Tensor-core building block (no reference counterpart): D = A B^T with A (M x K) and
+ * B (N x K) BF16 row-major, D (M x N) FP32 row-major, through tcgen05 MMAs with TMEM
+ * accumulators.  M, N multiples of 128, K a multiple of 64, 16-byte aligned rows.
+ * *err (device int, caller-zeroed) is set to 1 if a completion wait timed out. */
+int gcsl_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, float *D, int32_t M, int32_t N, int32_t K, int32_t *err,
+                      void *stream);
+
 #ifdef __cplusplus
 }
 #endif
