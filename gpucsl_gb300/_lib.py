@@ -28,7 +28,7 @@ GCSL_DTYPE_F32 = 1
 # every symbol the header declares (checked by the CPU test-suite)
 EXPORTED = [
     "gcsl_version", "gcsl_status_string", "gcsl_kernel_launches",
-    "gcsl_corr_workspace_bytes", "gcsl_corr_f64",
+    "gcsl_corr_workspace_bytes", "gcsl_corr_f64", "gcsl_corr_tc_workspace_bytes", "gcsl_corr_f64_tc",
     "gcsl_gauss_workspace_bytes", "gcsl_gauss_skeleton", "gcsl_gauss_skeleton_noalloc",
     "gcsl_disc_workspace_bytes", "gcsl_disc_skeleton",
     "gcsl_compact", "gcsl_unrank", "gcsl_pchisq", "gcsl_disc_table", "gcsl_tc_gemm_bf16",
@@ -92,6 +92,10 @@ def lib() -> ct.CDLL:
     L.gcsl_corr_workspace_bytes.argtypes = [_i64, _i32]
     L.gcsl_corr_f64.restype = ct.c_int
     L.gcsl_corr_f64.argtypes = [_vp, _i32, _i64, _i32, _i64, _vp, _vp, _sz, _vp]
+    L.gcsl_corr_tc_workspace_bytes.restype = _sz
+    L.gcsl_corr_tc_workspace_bytes.argtypes = [_i64, _i32]
+    L.gcsl_corr_f64_tc.restype = ct.c_int
+    L.gcsl_corr_f64_tc.argtypes = [_vp, _i32, _i64, _i32, _i64, _vp, _vp, _sz, _vp]
     L.gcsl_gauss_workspace_bytes.restype = _sz
     L.gcsl_gauss_workspace_bytes.argtypes = [_i32, _i32]
     L.gcsl_gauss_skeleton.restype = ct.c_int

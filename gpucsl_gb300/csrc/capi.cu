@@ -40,6 +40,9 @@ cudaError_t launch_disc_table(const uint8_t *data, long long ld, long long n, co
                               cudaStream_t s);
 cudaError_t launch_pchisq(const double *x, const long long *df, long long count, double *out, cudaStream_t s);
 cudaError_t launch_unrank(int K, int L, long long count, int *out, cudaStream_t s);
+size_t corr_tc_workspace_bytes(long long n, int p, int num_sms);
+cudaError_t corr_tc(const void *X, int dtype, long long n, int p, long long ldx, double *C, void *ws, size_t ws_bytes,
+                    int num_sms, int *err_out_dev_or_null, cudaStream_t s);
 cudaError_t launch_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, float *D, int M, int N, int K, int *err,
                                 cudaStream_t s);
 }  // namespace host
@@ -204,6 +207,21 @@ int gcsl_corr_f64(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ld
     if (!workspace || workspace_bytes < host::corr_workspace_bytes(n, p)) return GCSL_ERR_WORKSPACE;
     return map_cuda(host::corr_f64(X, dtype, n, p, ldx, C, workspace, workspace_bytes, device_sms(),
                                    static_cast<cudaStream_t>(stream)));
+}
+
+size_t gcsl_corr_tc_workspace_bytes(int64_t n, int32_t p) {
+    if (n < 1 || p < 1) return 0;
+    return host::corr_tc_workspace_bytes(n, p, device_sms());
+}
+
+int gcsl_corr_f64_tc(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ldx, double *C, void *workspace,
+                     size_t workspace_bytes, void *stream) {
+    if (!X || !C || n < 2 || p < 1 || ldx < p || (dtype != GCSL_DTYPE_F64 && dtype != GCSL_DTYPE_F32))
+        return GCSL_ERR_INVALID_ARG;
+    const int sms = device_sms();
+    if (!workspace || workspace_bytes < host::corr_tc_workspace_bytes(n, p, sms)) return GCSL_ERR_WORKSPACE;
+    return map_cuda(host::corr_tc(X, dtype, n, p, ldx, C, workspace, workspace_bytes, sms, nullptr,
+                                  static_cast<cudaStream_t>(stream)));
 }
 
 size_t gcsl_gauss_workspace_bytes(int32_t p, int32_t max_level) {

@@ -150,6 +150,28 @@ static cudaError_t corr_impl(const T *X, long long n, int p, long long ldx, doub
     return cudaGetLastError();
 }
 
+cudaError_t corr_partial_means(const void *X, int dtype, long long n, int p, long long ldx, double *partial,
+                               double *mean, cudaStream_t s) {
+    const long long chunks = (n + CORR_ROWS_PER_CHUNK - 1) / CORR_ROWS_PER_CHUNK;
+    dim3 g1((p + 127) / 128, (unsigned)chunks);
+    if (dtype == GCSL_DTYPE_F64)
+        col_partial_sums_kernel<double><<<g1, 128, 0, s>>>(static_cast<const double *>(X), n, p, ldx, partial);
+    else
+        col_partial_sums_kernel<float><<<g1, 128, 0, s>>>(static_cast<const float *>(X), n, p, ldx, partial);
+    note_launch(1);
+    col_mean_kernel<<<(p + 127) / 128, 128, 0, s>>>(partial, n, p, (int)chunks, mean);
+    note_launch(1);
+    return cudaGetLastError();
+}
+
+cudaError_t corr_normalize(double *C, int p, double *sd, int num_sms, cudaStream_t s) {
+    diag_sqrt_kernel<<<(p + 127) / 128, 128, 0, s>>>(C, p, sd);
+    note_launch(1);
+    normalize_kernel<<<num_sms * 4, 256, 0, s>>>(C, p, sd);
+    note_launch(1);
+    return cudaGetLastError();
+}
+
 cudaError_t corr_f64(const void *X, int dtype, long long n, int p, long long ldx, double *C, void *ws,
                      size_t ws_bytes, int num_sms, cudaStream_t s) {
     if (dtype == GCSL_DTYPE_F64)

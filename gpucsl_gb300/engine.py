@@ -34,8 +34,11 @@ def records_to_dense(rec: np.ndarray, n_ints: int, p: int, max_level: int) -> np
     return out
 
 
-def correlation(X, out=None, workspace=None):
-    """FP64 correlation matrix of device samples X (n x p, float64/float32, row-major)."""
+def correlation(X, out=None, workspace=None, method: str = "dfma"):
+    """FP64 correlation matrix of device samples X (n x p, float64/float32, row-major).
+
+    method "dfma": FP64 GEMM on the CUDA cores; "tc": exact integer-digit products on
+    the tcgen05 tensor cores (same result to about 2^-48 of sum |x_i||x_j|)."""
     torch = _torch()
     if X.dim() != 2:
         raise ValueError("X must be 2-D (samples x variables)")
@@ -46,10 +49,19 @@ def correlation(X, out=None, workspace=None):
     L = _lib.lib()
     if out is None:
         out = torch.empty((p, p), dtype=torch.float64, device=X.device)
+    dt = _lib.GCSL_DTYPE_F64 if X.dtype == torch.float64 else _lib.GCSL_DTYPE_F32
+    if method == "tc":
+        need = int(L.gcsl_corr_tc_workspace_bytes(n, p))
+        if workspace is None or workspace.numel() < need:
+            workspace = torch.empty(need, dtype=torch.uint8, device=X.device)
+        _lib.check(L.gcsl_corr_f64_tc(X.data_ptr(), dt, n, p, p, out.data_ptr(), workspace.data_ptr(),
+                                      workspace.numel(), _lib.stream_ptr()), "gcsl_corr_f64_tc")
+        return out
+    if method != "dfma":
+        raise ValueError(f"unknown correlation method {method!r}")
     need = int(L.gcsl_corr_workspace_bytes(n, p))
     if workspace is None or workspace.numel() < need:
         workspace = torch.empty(need, dtype=torch.uint8, device=X.device)
-    dt = _lib.GCSL_DTYPE_F64 if X.dtype == torch.float64 else _lib.GCSL_DTYPE_F32
     _lib.check(L.gcsl_corr_f64(X.data_ptr(), dt, n, p, p, out.data_ptr(), workspace.data_ptr(), workspace.numel(),
                                _lib.stream_ptr()), "gcsl_corr_f64")
     return out

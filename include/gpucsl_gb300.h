@@ -66,6 +66,15 @@ size_t gcsl_corr_workspace_bytes(int64_t n, int32_t p);
 int gcsl_corr_f64(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ldx, double *C, void *workspace,
                   size_t workspace_bytes, void *stream);
 
+/* Same result as gcsl_corr_f64 computed on the tcgen05 tensor cores: the centred,
+ * power-of-two-scaled samples are split into seven signed 7-bit integer digits (exact in
+ * BF16), digit pairs are accumulated exactly in TMEM and reduced in 64-bit integers, and
+ * each covariance is rounded to FP64 once.  Deviation from an FP64 GEMM: at most about
+ * 2^-48 of sum_t |x_ti||x_tj|.  A completion-wait timeout poisons C with NaN. */
+size_t gcsl_corr_tc_workspace_bytes(int64_t n, int32_t p);
+int gcsl_corr_f64_tc(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ldx, double *C, void *workspace,
+                     size_t workspace_bytes, void *stream);
+
 /* --------------------------------------------------- Gaussian skeleton (b,c,e) */
 /* Replaces the level loop of gpucsl/pc/discover_skeleton_gaussian.py:30-113
  * (gaussian_ci_worker) with the kernels of gpucsl/pc/cuda/gaussian_ci.cu:18-120,

@@ -42,3 +42,41 @@ def test_tc_gemm_random_values(cuda):
     D = _gemm(torch, Ab, Bb)
     ref = Ab @ Bb.T
     assert np.allclose(D, ref, rtol=1e-5, atol=1e-4)
+
+
+@pytest.mark.parametrize("p,n,dt", [(20, 1000, np.float64), (257, 3001, np.float64), (1000, 10000, np.float64),
+                                    (130, 777, np.float32), (64, 100000, np.float64)])
+def test_tc_correlation_matches_numpy(cuda, p, n, dt):
+    torch = cuda
+    from gpucsl_gb300 import engine
+    from gpucsl_gb300.synthetic import gaussian_dag_data
+
+    w = gaussian_dag_data(p, n, 3, p * 7 + n)
+    X = w.data.astype(dt)
+    X[:, 0] += 1000.0  # a large mean: centring happens in FP64 before the split
+    C = engine.correlation(torch.from_numpy(X).cuda(), method="tc").cpu().numpy()
+    ref = np.corrcoef(X, rowvar=False)
+    err = float(np.abs(C - ref).max())
+    assert np.isfinite(C).all()
+    assert err <= 1e-12, err
+
+
+def test_tc_correlation_skeleton_parity(cuda):
+    """p = 1000, n = 10000 skeleton from the tensor-core correlation matches the oracle."""
+    torch = cuda
+    from gpucsl_gb300 import engine
+    from gpucsl_gb300.synthetic import gaussian_dag_data
+    from oracle import gaussian as og
+
+    w = gaussian_dag_data(1000, 10000, 3, 2)
+    Cg = engine.correlation(torch.from_numpy(w.data).cuda(), method="tc")
+    ref = og.skeleton(og.corrcoef(w.data), 10000, 0.01, 998)
+    s = engine.GaussianSolver(1000, 998)
+    st = s.run(Cg, 10000, og.thresholds(10000, 0.01))
+    G, sep, pmax = s.to_host()
+    assert (G == ref.skeleton).all()
+    assert (sep == ref.sepsets).all()
+    iu = np.triu_indices(1000, 1)
+    rel = np.abs(pmax[iu] - ref.pmax[iu]) / np.maximum(np.abs(ref.pmax[iu]), 1e-300)
+    assert ((rel <= 1e-9) | (np.abs(pmax[iu] - ref.pmax[iu]) <= 1e-300)).all(), float(rel.max())
+    assert st.tests == ref.tests_canonical
