@@ -29,6 +29,7 @@ GCSL_DTYPE_F32 = 1
 EXPORTED = [
     "gcsl_version", "gcsl_status_string", "gcsl_kernel_launches",
     "gcsl_corr_workspace_bytes", "gcsl_corr_f64", "gcsl_corr_tc_workspace_bytes", "gcsl_corr_f64_tc",
+    "gcsl_corr_tc_digits", "gcsl_corr_tc_product",
     "gcsl_gauss_workspace_bytes", "gcsl_gauss_skeleton", "gcsl_gauss_skeleton_noalloc",
     "gcsl_disc_workspace_bytes", "gcsl_disc_skeleton",
     "gcsl_compact", "gcsl_unrank", "gcsl_pchisq", "gcsl_disc_table", "gcsl_tc_gemm_bf16",
@@ -96,6 +97,10 @@ def lib() -> ct.CDLL:
     L.gcsl_corr_tc_workspace_bytes.argtypes = [_i64, _i32]
     L.gcsl_corr_f64_tc.restype = ct.c_int
     L.gcsl_corr_f64_tc.argtypes = [_vp, _i32, _i64, _i32, _i64, _vp, _vp, _sz, _vp]
+    L.gcsl_corr_tc_digits.restype = ct.c_int
+    L.gcsl_corr_tc_digits.argtypes = [_vp, _i32, _i64, _i32, _i64, _vp, _sz, _vp]
+    L.gcsl_corr_tc_product.restype = ct.c_int
+    L.gcsl_corr_tc_product.argtypes = [_i64, _i32, _vp, _vp, _sz, _vp]
     L.gcsl_gauss_workspace_bytes.restype = _sz
     L.gcsl_gauss_workspace_bytes.argtypes = [_i32, _i32]
     L.gcsl_gauss_skeleton.restype = ct.c_int

@@ -18,6 +18,7 @@ cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, doub
                           cudaStream_t s);
 cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s);
 cudaError_t launch_scan_int(const int *cnt, int p, long long *prefix, DevState *st, cudaStream_t s);
+cudaError_t launch_recompact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s);
 cudaError_t launch_scan_ll(const long long *cnt, int p, long long *prefix, DevState *st, cudaStream_t s);
 cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, const int *up, const long long *prefix,
                                double tau, bool tau_valid, uint16_t *G, double *zmin, int *sep_dense, int max_level,
@@ -43,6 +44,9 @@ cudaError_t launch_unrank(int K, int L, long long count, int *out, cudaStream_t 
 size_t corr_tc_workspace_bytes(long long n, int p, int num_sms);
 cudaError_t corr_tc(const void *X, int dtype, long long n, int p, long long ldx, double *C, void *ws, size_t ws_bytes,
                     int num_sms, int *err_out_dev_or_null, cudaStream_t s);
+cudaError_t corr_tc_digits(const void *X, int dtype, long long n, int p, long long ldx, void *ws, size_t ws_bytes,
+                           int num_sms, cudaStream_t s);
+cudaError_t corr_tc_product(long long n, int p, double *C, void *ws, size_t ws_bytes, int num_sms, cudaStream_t s);
 cudaError_t launch_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, float *D, int M, int N, int K, int *err,
                                 cudaStream_t s);
 }  // namespace host
@@ -224,6 +228,23 @@ int gcsl_corr_f64_tc(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t
                                   static_cast<cudaStream_t>(stream)));
 }
 
+int gcsl_corr_tc_digits(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ldx, void *workspace,
+                        size_t workspace_bytes, void *stream) {
+    if (!X || n < 2 || p < 1 || ldx < p || (dtype != GCSL_DTYPE_F64 && dtype != GCSL_DTYPE_F32))
+        return GCSL_ERR_INVALID_ARG;
+    const int sms = device_sms();
+    if (!workspace || workspace_bytes < host::corr_tc_workspace_bytes(n, p, sms)) return GCSL_ERR_WORKSPACE;
+    return map_cuda(host::corr_tc_digits(X, dtype, n, p, ldx, workspace, workspace_bytes, sms,
+                                         static_cast<cudaStream_t>(stream)));
+}
+
+int gcsl_corr_tc_product(int64_t n, int32_t p, double *C, void *workspace, size_t workspace_bytes, void *stream) {
+    if (!C || n < 2 || p < 1) return GCSL_ERR_INVALID_ARG;
+    const int sms = device_sms();
+    if (!workspace || workspace_bytes < host::corr_tc_workspace_bytes(n, p, sms)) return GCSL_ERR_WORKSPACE;
+    return map_cuda(host::corr_tc_product(n, p, C, workspace, workspace_bytes, sms, static_cast<cudaStream_t>(stream)));
+}
+
 size_t gcsl_gauss_workspace_bytes(int32_t p, int32_t max_level) {
     (void)max_level;
     return carve_gauss(nullptr, 0, p).bytes;
@@ -242,7 +263,9 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
     if (cudaMemsetAsync(w.st, 0, sizeof(DevState), s) != cudaSuccess) return GCSL_ERR_DEVICE;
     if (host::launch_level0(C, p, thresholds[0], G, w.zmin, w.st, s) != cudaSuccess) return GCSL_ERR_DEVICE;
     int rc = run_levels(max_level, w.st, s, [&](int level) -> cudaError_t {
-        cudaError_t e = host::launch_compact(G, p, w.adj, w.up, w.st, level, s);
+        // level 1 compacts the full matrix; later levels only shrink the previous lists
+        cudaError_t e = (level == 1) ? host::launch_compact(G, p, w.adj, w.up, w.st, level, s)
+                                     : host::launch_recompact(G, p, w.adj, w.up, w.st, level, s);
         if (e == cudaSuccess) e = host::launch_scan_int(w.up, p, w.prefix, w.st, s);
         const bool tau_valid = level < n_thresholds;
         const double tau = tau_valid ? thresholds[level] : 0.0;

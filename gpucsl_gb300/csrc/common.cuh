@@ -11,7 +11,7 @@
 #define GCSL_KEY_NONE 0xffffffffffffffffull
 // Largest conditioning-set size with a register-resident Gaussian test; larger
 // levels run the shared-memory kernel.
-#define GCSL_GAUSS_REG_LEVELS 8
+#define GCSL_GAUSS_REG_LEVELS 12
 // Ranks per direction must stay below this bound (keys are rank << 1 | dir).
 #define GCSL_RANK_LIMIT (1ll << 56)
 

@@ -44,33 +44,78 @@ struct OzDims {
 };
 
 // ------------------------------------------------------------ preparation
-template <typename T>
-__global__ void col_absdev_max_kernel(const T *__restrict__ X, long long n, int p, long long ldx,
-                                      const double *__restrict__ mean, unsigned long long *__restrict__ maxbits) {
-    // block: 32 columns (lanes) x 8 warps over a 256-sample chunk (blockIdx.y)
-    __shared__ double red[8][32];
-    const int j = blockIdx.x * 32 + (threadIdx.x & 31);
-    const int w = threadIdx.x >> 5;
-    const long long t0 = (long long)blockIdx.y * 256, t1 = min(n, t0 + 256);
-    double m = 0.0;
+// Order-preserving signed key of a double (negative values have their magnitude bits
+// flipped), so min / max can be taken with 64-bit integer atomics.
+__device__ __forceinline__ long long ordered_key(double x) {
+    long long k = __double_as_longlong(x);
+    return k < 0 ? (k ^ 0x7fffffffffffffffll) : k;
+}
+__device__ __forceinline__ double key_value(long long k) {
+    return __longlong_as_double(k < 0 ? (k ^ 0x7fffffffffffffffll) : k);
+}
+
+constexpr int OZ_STAT_ROWS = 512;  // samples per column-statistics block
+
+__global__ void colstats_init_kernel(int p, long long *__restrict__ kmin, long long *__restrict__ kmax) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j < p) {
-        const double mu = mean[j];
-        for (long long t = t0 + w; t < t1; t += 8) m = fmax(m, fabs((double)X[t * ldx + j] - mu));
-    }
-    red[w][threadIdx.x & 31] = m;
-    __syncthreads();
-    if (w == 0 && j < p) {
-        for (int q = 1; q < 8; ++q) m = fmax(m, red[q][threadIdx.x & 31]);
-        atomicMax(&maxbits[j], (unsigned long long)__double_as_longlong(m));  // non-negative: bits are ordered
+        kmin[j] = 0x7fffffffffffffffll;
+        kmax[j] = (long long)0x8000000000000000ull;
     }
 }
 
-__global__ void col_exponent_kernel(const unsigned long long *__restrict__ maxbits, int p, int *__restrict__ expo) {
+// One read of X: per (512-sample chunk, column) FP64 partial sum in a fixed order, and
+// column min / max through ordered-key atomics.
+template <typename T>
+__global__ void colstats_kernel(const T *__restrict__ X, long long n, int p, long long ldx,
+                                double *__restrict__ partial, long long *__restrict__ kmin,
+                                long long *__restrict__ kmax) {
+    __shared__ double ssum[8][32];
+    __shared__ long long smin[8][32], smax[8][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int j = blockIdx.x * 32 + lane;
+    const long long t0 = (long long)blockIdx.y * OZ_STAT_ROWS, t1 = min(n, t0 + OZ_STAT_ROWS);
+    double sum = 0.0;
+    long long mn = 0x7fffffffffffffffll, mx = (long long)0x8000000000000000ull;
+    if (j < p) {
+        for (long long t = t0 + w; t < t1; t += 8) {
+            const double x = (double)X[t * ldx + j];
+            sum += x;
+            const long long k = ordered_key(x);
+            mn = k < mn ? k : mn;
+            mx = k > mx ? k : mx;
+        }
+    }
+    ssum[w][lane] = sum;
+    smin[w][lane] = mn;
+    smax[w][lane] = mx;
+    __syncthreads();
+    if (w == 0 && j < p) {
+        for (int q = 1; q < 8; ++q) {
+            sum += ssum[q][lane];
+            mn = smin[q][lane] < mn ? smin[q][lane] : mn;
+            mx = smax[q][lane] > mx ? smax[q][lane] : mx;
+        }
+        partial[(size_t)blockIdx.y * p + j] = sum;
+        atomicMin(&kmin[j], mn);
+        atomicMax(&kmax[j], mx);
+    }
+}
+
+// mean = (chunk sums in order) / n; E = exponent of max |fl(x - mean)| =
+// max(fl(max - mean), fl(mean - min)) (rounding is monotone), so |x - mean| < 2^E.
+__global__ void col_mean_exp_kernel(const double *__restrict__ partial, long long n, int p, int chunks,
+                                    const long long *__restrict__ kmin, const long long *__restrict__ kmax,
+                                    double *__restrict__ mean, int *__restrict__ expo) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= p) return;
-    const double m = __longlong_as_double((long long)maxbits[j]);
+    double s = 0.0;
+    for (int c = 0; c < chunks; ++c) s += partial[(size_t)c * p + j];
+    const double mu = s / (double)n;
+    mean[j] = mu;
+    const double dev = fmax(key_value(kmax[j]) - mu, mu - key_value(kmin[j]));
     int e = 0;
-    if (m > 0.0) frexp(m, &e);  // m = f 2^e with f in [0.5, 1): |x - mean| 2^-e < 1
+    if (dev > 0.0) frexp(dev, &e);
     expo[j] = e;
 }
 
@@ -87,15 +132,22 @@ __global__ void digit_split_kernel(const T *__restrict__ X, long long n, int p, 
     const long long t0 = (long long)blockIdx.x * 32;
     const int j0 = blockIdx.y * 32;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 warps
-    const double magic = 6755399441055744.0;                 // 1.5 * 2^52: fma(., ., magic) rounds to an integer
     for (int r = ty; r < 32; r += 8) {
         const long long t = t0 + r;
         const int j = j0 + tx;
         long long I = 0;
         if (t < n && j < p) {
-            const double y = (double)X[t * ldx + j] - mean[j];  // centred as numpy does (one rounding)
-            const double sc = __longlong_as_double((long long)(1023 + 49 - expo[j]) << 52);  // 2^(49 - E)
-            I = __double_as_longlong(fma(y, sc, magic)) - __double_as_longlong(magic);
+            // y = fl(x - mean) as numpy centres; I = round(|y| 2^(49 - E)) with the sign of y,
+            // from the bits of y: |y| = m 2^(ey - 1075), so I = round(m 2^(ey - 1075 + 49 - E)).
+            const double y = (double)X[t * ldx + j] - mean[j];
+            const long long bits = __double_as_longlong(y);
+            const int ey = (int)((bits >> 52) & 0x7ff);
+            long long m = bits & 0xfffffffffffffll;
+            if (ey != 0) m |= 1ll << 52;
+            const int sh = 1075 - (ey != 0 ? ey : 1) - 49 + expo[j];  // right shift, >= 4 since |y| < 2^E
+            long long mag = 0;
+            if (sh < 63) mag = (m + (1ll << (sh - 1))) >> sh;
+            I = bits < 0 ? -mag : mag;
         }
         long long rem = I;
 #pragma unroll
@@ -346,9 +398,32 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(const uint8_t
     if (warp == 0) tc::tmem_dealloc(tmem, OZ_TMEM_COLS);
 }
 
-// cov_ij for i <= j from the exact split sums; both triangles written.
+__device__ __forceinline__ double pow2(int e) { return __longlong_as_double((long long)(1023 + e) << 52); }
+
+// Covariance of (i, j) from the exact split sums: (2^28 H + L) 2^(E_i + E_j - 56) / (n - 1).
+__device__ __forceinline__ double oz_cov(const long long *__restrict__ part_hi, const long long *__restrict__ part_lo,
+                                         const OzDims &D, const int *__restrict__ expo, double scale, int i, int j) {
+    long long H = 0, Lo = 0;
+    for (int s = 0; s < D.splits; ++s) {
+        const size_t ix = ((size_t)s * D.p_pad + i) * D.p_pad + j;
+        H += part_hi[ix];
+        Lo += part_lo[ix];
+    }
+    const double val = fma((double)H, 268435456.0, (double)Lo);  // exact terms, one rounding
+    return (val * pow2(expo[i] + expo[j] - 56)) * scale;
+}
+
+__global__ void ozaki_diag_kernel(const long long *__restrict__ part_hi, const long long *__restrict__ part_lo,
+                                  OzDims D, const int *__restrict__ expo, double scale, double *__restrict__ inv_sd) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < D.p) inv_sd[i] = 1.0 / sqrt(oz_cov(part_hi, part_lo, D, expo, scale, i, i));
+}
+
+// C_ij = clip(cov_ij / s_i / s_j, -1, 1) for i <= j, written to both triangles (the
+// normalisation of numpy's corrcoef, with reciprocals of the standard deviations).
 __global__ void ozaki_finish_kernel(const long long *__restrict__ part_hi, const long long *__restrict__ part_lo,
-                                    OzDims D, const int *__restrict__ expo, double scale, const int *__restrict__ err,
+                                    OzDims D, const int *__restrict__ expo, double scale,
+                                    const double *__restrict__ inv_sd, const int *__restrict__ err,
                                     double *__restrict__ C) {
     const long long total = (long long)D.p * D.p;
     const bool failed = *err != 0;  // a tensor-core wait timed out: poison the output
@@ -356,15 +431,9 @@ __global__ void ozaki_finish_kernel(const long long *__restrict__ part_hi, const
          k += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(k / D.p), j = (int)(k - (long long)i * D.p);
         if (i > j) continue;
-        long long H = 0, Lo = 0;
-        for (int s = 0; s < D.splits; ++s) {
-            const size_t ix = ((size_t)s * D.p_pad + i) * D.p_pad + j;
-            H += part_hi[ix];
-            Lo += part_lo[ix];
-        }
-        const double val = ldexp((double)H, 28) + (double)Lo;  // exact terms, one rounding
-        const double dot = ldexp(val, expo[i] + expo[j] - 56);  // sum I_i I_j = 2^42 V, I = y 2^(49 - E)
-        const double v = failed ? __longlong_as_double(0x7ff8000000000000ll) : dot * scale;
+        double v = oz_cov(part_hi, part_lo, D, expo, scale, i, j) * inv_sd[i] * inv_sd[j];
+        v = fmin(fmax(v, -1.0), 1.0);
+        if (failed) v = __longlong_as_double(0x7ff8000000000000ll);
         C[(size_t)i * D.p + j] = v;
         C[(size_t)j * D.p + i] = v;
     }
@@ -372,25 +441,21 @@ __global__ void ozaki_finish_kernel(const long long *__restrict__ part_hi, const
 
 namespace host {
 
-cudaError_t corr_partial_means(const void *X, int dtype, long long n, int p, long long ldx, double *partial,
-                               double *mean, cudaStream_t s);
-cudaError_t corr_normalize(double *C, int p, double *sd, int num_sms, cudaStream_t s);
-
 static OzDims oz_dims(long long n, int p, int num_sms) {
     OzDims D;
     D.p = p;
     D.p_pad = (p + OZ_TM - 1) / OZ_TM * OZ_TM;
-    D.n_pad = (n + OZ_KS - 1) / OZ_KS * OZ_KS;
+    D.n_pad = (int)((n + OZ_KS - 1) / OZ_KS * OZ_KS);
     D.n_tiles_j = D.p_pad / OZ_TN;
     const int n_tiles_i = D.p_pad / OZ_TM;
     int tiles = 0;
     for (int i = 0; i < n_tiles_i; ++i) tiles += D.n_tiles_j - 2 * i;
-    const long long slabs = D.n_pad / 16;  // K steps
+    const long long steps = D.n_pad / 16;
     int splits = num_sms / tiles;  // one wave: tiles x splits <= SMs (one CTA per SM holds all TMEM)
     if (splits < 1) splits = 1;
-    if (splits > slabs) splits = (int)slabs;
-    D.slabs_per_split = (int)((slabs + splits - 1) / splits);
-    D.splits = (int)((slabs + D.slabs_per_split - 1) / D.slabs_per_split);
+    if (splits > steps) splits = (int)steps;
+    D.slabs_per_split = (int)((steps + splits - 1) / splits);
+    D.splits = (int)((steps + D.slabs_per_split - 1) / D.slabs_per_split);
     return D;
 }
 
@@ -400,71 +465,82 @@ static int oz_tiles(const OzDims &D) {
     return tiles;
 }
 
-size_t corr_tc_workspace_bytes(long long n, int p, int num_sms) {
-    const OzDims D = oz_dims(n, p, num_sms);
-    const long long chunks = (n + 255) / 256;
-    size_t b = 0;
-    auto take = [&](size_t bytes) { b += (bytes + 255) / 256 * 256; };
-    take((size_t)(chunks * p) * sizeof(double));                  // column partial sums
-    take((size_t)p * sizeof(double));                             // means
-    take((size_t)p * sizeof(double));                             // sd
-    take((size_t)p * sizeof(int));                                // exponents
-    take((size_t)p * sizeof(unsigned long long));                 // column max |x - mean| bits
-    take((size_t)OZ_S * D.p_pad * (size_t)D.n_pad * sizeof(uint16_t));  // digits
-    take((size_t)D.splits * D.p_pad * (size_t)D.p_pad * sizeof(long long) * 2);  // partial words
-    take(sizeof(int));                                            // error flag
-    return b;
-}
+struct OzWs {
+    double *partial, *mean, *inv_sd;
+    long long *kmin, *kmax;
+    int *expo, *err;
+    uint8_t *dig;
+    long long *phi, *plo;
+    size_t bytes;
+};
 
-cudaError_t corr_tc(const void *X, int dtype, long long n, int p, long long ldx, double *C, void *ws, size_t ws_bytes,
-                    int num_sms, int *err_out_dev_or_null, cudaStream_t s) {
-    const OzDims D = oz_dims(n, p, num_sms);
-    if (ws_bytes < corr_tc_workspace_bytes(n, p, num_sms)) return cudaErrorInvalidValue;
-    const long long chunks = (n + 255) / 256;
+static OzWs oz_carve(void *ws, long long n, int p, const OzDims &D) {
+    const long long chunks = (n + OZ_STAT_ROWS - 1) / OZ_STAT_ROWS;
     char *w = static_cast<char *>(ws);
     size_t off = 0;
     auto take = [&](size_t bytes) {
-        char *r = w + off;
+        char *r = w ? w + off : nullptr;
         off += (bytes + 255) / 256 * 256;
         return r;
     };
-    double *partial = reinterpret_cast<double *>(take((size_t)(chunks * p) * sizeof(double)));
-    double *mean = reinterpret_cast<double *>(take((size_t)p * sizeof(double)));
-    double *sd = reinterpret_cast<double *>(take((size_t)p * sizeof(double)));
-    int *expo = reinterpret_cast<int *>(take((size_t)p * sizeof(int)));
-    unsigned long long *maxbits =
-        reinterpret_cast<unsigned long long *>(take((size_t)p * sizeof(unsigned long long)));
-    uint8_t *dig = reinterpret_cast<uint8_t *>(take((size_t)OZ_S * D.p_pad * (size_t)D.n_pad * sizeof(uint16_t)));
-    long long *phi = reinterpret_cast<long long *>(
-        take((size_t)D.splits * D.p_pad * (size_t)D.p_pad * sizeof(long long) * 2));
-    long long *plo = phi + (size_t)D.splits * D.p_pad * (size_t)D.p_pad;
-    int *err = reinterpret_cast<int *>(take(sizeof(int)));
-    if (err_out_dev_or_null) err = err_out_dev_or_null;
+    OzWs o;
+    o.partial = reinterpret_cast<double *>(take((size_t)(chunks * p) * sizeof(double)));
+    o.mean = reinterpret_cast<double *>(take((size_t)p * sizeof(double)));
+    o.inv_sd = reinterpret_cast<double *>(take((size_t)p * sizeof(double)));
+    o.kmin = reinterpret_cast<long long *>(take((size_t)p * sizeof(long long)));
+    o.kmax = reinterpret_cast<long long *>(take((size_t)p * sizeof(long long)));
+    o.expo = reinterpret_cast<int *>(take((size_t)p * sizeof(int)));
+    o.err = reinterpret_cast<int *>(take(sizeof(int)));
+    o.dig = reinterpret_cast<uint8_t *>(take((size_t)OZ_S * D.p_pad * (size_t)D.n_pad * sizeof(uint16_t)));
+    o.phi = reinterpret_cast<long long *>(take((size_t)D.splits * D.p_pad * (size_t)D.p_pad * sizeof(long long) * 2));
+    o.plo = o.phi ? o.phi + (size_t)D.splits * D.p_pad * (size_t)D.p_pad : nullptr;
+    o.bytes = off;
+    return o;
+}
 
-    cudaError_t e = corr_partial_means(X, dtype, n, p, ldx, partial, mean, s);
+size_t corr_tc_workspace_bytes(long long n, int p, int num_sms) {
+    const OzDims D = oz_dims(n, p, num_sms);
+    return oz_carve(nullptr, n, p, D).bytes;
+}
+
+// Stage 1: column statistics, exponents and the digit tiles (FP64 / integer work).
+cudaError_t corr_tc_digits(const void *X, int dtype, long long n, int p, long long ldx, void *ws, size_t ws_bytes,
+                           int num_sms, cudaStream_t s) {
+    const OzDims D = oz_dims(n, p, num_sms);
+    const OzWs o = oz_carve(ws, n, p, D);
+    if (ws_bytes < o.bytes) return cudaErrorInvalidValue;
+    const long long chunks = (n + OZ_STAT_ROWS - 1) / OZ_STAT_ROWS;
+    cudaError_t e = cudaMemsetAsync(o.err, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(err, 0, sizeof(int), s);
-    if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(maxbits, 0, (size_t)p * sizeof(unsigned long long), s);
-    if (e != cudaSuccess) return e;
-    const dim3 gm((p + 31) / 32, (unsigned)((n + 255) / 256));
+    colstats_init_kernel<<<(p + 255) / 256, 256, 0, s>>>(p, o.kmin, o.kmax);
+    note_launch(1);
+    const dim3 gs((p + 31) / 32, (unsigned)chunks);
     const dim3 gd((unsigned)(D.n_pad / 32), (unsigned)(D.p_pad / 32));
-    if (dtype == GCSL_DTYPE_F64) {
-        col_absdev_max_kernel<double><<<gm, 256, 0, s>>>(static_cast<const double *>(X), n, p, ldx, mean, maxbits);
-    } else {
-        col_absdev_max_kernel<float><<<gm, 256, 0, s>>>(static_cast<const float *>(X), n, p, ldx, mean, maxbits);
-    }
+    if (dtype == GCSL_DTYPE_F64)
+        colstats_kernel<double><<<gs, 256, 0, s>>>(static_cast<const double *>(X), n, p, ldx, o.partial, o.kmin,
+                                                   o.kmax);
+    else
+        colstats_kernel<float><<<gs, 256, 0, s>>>(static_cast<const float *>(X), n, p, ldx, o.partial, o.kmin,
+                                                  o.kmax);
     note_launch(1);
-    col_exponent_kernel<<<(p + 255) / 256, 256, 0, s>>>(maxbits, p, expo);
+    col_mean_exp_kernel<<<(p + 255) / 256, 256, 0, s>>>(o.partial, n, p, (int)chunks, o.kmin, o.kmax, o.mean,
+                                                        o.expo);
     note_launch(1);
-    if (dtype == GCSL_DTYPE_F64) {
-        digit_split_kernel<double><<<gd, 256, 0, s>>>(static_cast<const double *>(X), n, p, ldx, mean, expo,
-                                                       D.p_pad, D.n_pad, dig);
-    } else {
-        digit_split_kernel<float><<<gd, 256, 0, s>>>(static_cast<const float *>(X), n, p, ldx, mean, expo, D.p_pad,
-                                                      D.n_pad, dig);
-    }
+    if (dtype == GCSL_DTYPE_F64)
+        digit_split_kernel<double><<<gd, 256, 0, s>>>(static_cast<const double *>(X), n, p, ldx, o.mean, o.expo,
+                                                       D.p_pad, D.n_pad, o.dig);
+    else
+        digit_split_kernel<float><<<gd, 256, 0, s>>>(static_cast<const float *>(X), n, p, ldx, o.mean, o.expo,
+                                                      D.p_pad, D.n_pad, o.dig);
     note_launch(1);
+    return cudaGetLastError();
+}
+
+// Stage 2: exact digit products on the tensor cores, reduction, normalisation.
+cudaError_t corr_tc_product(long long n, int p, double *C, void *ws, size_t ws_bytes, int num_sms, cudaStream_t s) {
+    const OzDims D = oz_dims(n, p, num_sms);
+    const OzWs o = oz_carve(ws, n, p, D);
+    if (ws_bytes < o.bytes) return cudaErrorInvalidValue;
     const int smem = OZ_NST * OZ_STAGE_BYTES;
     static bool attr = false;
     if (!attr) {
@@ -472,13 +548,22 @@ cudaError_t corr_tc(const void *X, int dtype, long long n, int p, long long ldx,
         attr = true;
     }
     dim3 grid(oz_tiles(D), D.splits);
-    corr_ozaki_kernel<<<grid, OZ_THREADS, smem, s>>>(dig, D, phi, plo, err);
+    corr_ozaki_kernel<<<grid, OZ_THREADS, smem, s>>>(o.dig, D, o.phi, o.plo, o.err);
     note_launch(1);
-    ozaki_finish_kernel<<<num_sms * 4, 256, 0, s>>>(phi, plo, D, expo, 1.0 / (double)(n - 1), err, C);
+    const double scale = 1.0 / (double)(n - 1);
+    ozaki_diag_kernel<<<(p + 255) / 256, 256, 0, s>>>(o.phi, o.plo, D, o.expo, scale, o.inv_sd);
     note_launch(1);
-    e = cudaGetLastError();
+    ozaki_finish_kernel<<<num_sms * 4, 256, 0, s>>>(o.phi, o.plo, D, o.expo, scale, o.inv_sd, o.err, C);
+    note_launch(1);
+    return cudaGetLastError();
+}
+
+cudaError_t corr_tc(const void *X, int dtype, long long n, int p, long long ldx, double *C, void *ws, size_t ws_bytes,
+                    int num_sms, int *unused, cudaStream_t s) {
+    (void)unused;
+    cudaError_t e = corr_tc_digits(X, dtype, n, p, ldx, ws, ws_bytes, num_sms, s);
     if (e != cudaSuccess) return e;
-    return corr_normalize(C, p, sd, num_sms, s);
+    return corr_tc_product(n, p, C, ws, ws_bytes, num_sms, s);
 }
 
 }  // namespace host

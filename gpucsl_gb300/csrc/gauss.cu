@@ -3,9 +3,9 @@
 //   level 0        gauss_level0_kernel     (reference: gpucsl/pc/cuda/gaussian_ci.cu:18-51)
 //   compaction     compact_kernel          (reference: gpucsl/pc/cuda/helpers/graph_helpers.cu:35-56)
 //   edge prefix    row_scan_kernel
-//   level l <= 8   gauss_level_reg_kernel  (reference: gaussian_ci.cu:66-120,
+//   level l <= 12  gauss_level_reg_kernel  (reference: gaussian_ci.cu:66-120,
 //                                           helpers/gaussian_helpers.cu:240-262)
-//   level l > 8    gauss_level_smem_kernel
+//   level l > 12   gauss_level_smem_kernel
 //   zmin -> pmax   pmax_kernel             (reference: gpucsl/pc/helpers.py:62-82)
 //
 // Work decomposition of a level: one warp owns one undirected edge {lo, hi} alive at
@@ -78,6 +78,38 @@ __global__ void compact_kernel(const uint16_t *__restrict__ G, int p, int *__res
     if (lane == 0 && st != nullptr) atomicMax(&st->max_degree[level], maxdeg);
 }
 
+// Levels >= 2: each warp refilters one row's previous neighbour list against G (rows
+// only shrink, so this touches deg entries instead of p), writing up[r] and the max
+// degree; row_scan_kernel then rebuilds the edge prefix.
+__global__ void recompact_kernel(const uint16_t *__restrict__ G, int p, int *__restrict__ adj, int *__restrict__ up,
+                                 DevState *st, int level) {
+    if (st->done) return;
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    int maxdeg = 0;
+    for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p; r += warps) {
+        int *row = adj + (size_t)r * p;
+        const int deg = row[0];
+        int cnt = 0, ups = 0;
+        for (int k0 = 0; k0 < deg; k0 += 32) {
+            const int k = k0 + lane;
+            const int c = k < deg ? row[1 + k] : 0;
+            const bool keep = k < deg && G[(size_t)r * p + c] != 0;
+            const unsigned b = __ballot_sync(GCSL_FULL_MASK, keep);
+            __syncwarp();  // every read of this 32-entry window precedes the writes below
+            if (keep) row[1 + cnt + __popc(b & ((1u << lane) - 1))] = c;
+            cnt += __popc(b);
+            ups += __popc(__ballot_sync(GCSL_FULL_MASK, keep && c > r));
+        }
+        if (lane == 0) {
+            row[0] = cnt;
+            up[r] = ups;
+        }
+        maxdeg = max(maxdeg, cnt);
+    }
+    if (lane == 0) atomicMax(&st->max_degree[level], maxdeg);
+}
+
 // Single-block exclusive scan of a per-row count (int or weighted long long) into
 // prefix[0..p]; prefix[p] is the total.
 template <typename T>
@@ -117,58 +149,69 @@ __global__ void row_scan_kernel(const T *__restrict__ cnt, int p, long long *__r
     if (tid == nt - 1) prefix[p] = base;
 }
 
-// ---------------------------------------------------------- level l, L <= 8
-// Partial-correlation statistic of one test from the augmented matrix
-// [[C_SS, C_S,vi, C_S,vj], [., 1, C_vi,vj], [., ., 1]]: L elimination steps leave the
-// trailing 2x2 block H = M0 - M1 M2^-1 M1^T of gaussian_helpers.cu:78-89.
+// ---------------------------------------------------------- level l, L <= 12
+// One CI test: Gaussian elimination without square roots on the lower triangle of the
+// augmented matrix [[C_SS, C_S,vi, C_S,vj], [., 1, C_vi,vj], [., ., 1]].  After the L
+// pivots of C_SS the trailing 2x2 block is H = M0 - M1 M2^-1 M1^T of
+// gaussian_helpers.cu:78-89, and rho^2 = H01^2 / (|H00| |H11|).
+//
+// The statistic Z = |0.5 (log|1 + rho| - log|1 - rho|)| increases with |rho| on [0, 1),
+// so "Z < tau" is "rho^2 < tanh(tau)^2" there and no logarithm is needed per test.  For
+// |rho| >= 1 (Z decreases again), NaN, or rho^2 within 1e-12 of the threshold, Z is
+// evaluated with the reference's formula and compared with tau directly.
+struct TestOut {
+    double rho2;   // rho^2 when the monotone branch decided, +inf otherwise
+    double zexact; // Z from the reference formula when evaluated, +inf otherwise (NaN kept)
+    bool remove;
+};
+
+__device__ __forceinline__ double z_of_rho(double rho) {
+    return fabs(0.5 * (log(fabs(1.0 + rho)) - log(fabs(1.0 - rho))));
+}
+
 template <int L>
-__device__ __forceinline__ double gauss_test_reg(const double *__restrict__ C, int p, int vi, int vj, const int *S) {
-    double A[L * (L + 1) / 2];  // lower triangle of C_SS, row-packed
-    double a[L], b[L];
+__device__ __forceinline__ TestOut gauss_test_reg(const double *__restrict__ C, int p, int vi, int vj, const int *S,
+                                                  double tau, double t2) {
+    constexpr int D = L + 2;
+    double A[D * (D + 1) / 2];  // row-packed lower triangle; rows 0..L-1 = S, L = v_i, L+1 = v_j
 #pragma unroll
     for (int r = 0; r < L; ++r) {
         const double *Cr = C + (size_t)S[r] * p;
 #pragma unroll
-        for (int c = 0; c < r; ++c) A[r * (r + 1) / 2 + c] = __ldg(Cr + S[c]);
-        A[r * (r + 1) / 2 + r] = __ldg(Cr + S[r]);
-        a[r] = __ldg(C + (size_t)vi * p + S[r]);
-        b[r] = __ldg(C + (size_t)vj * p + S[r]);
+        for (int c = 0; c <= r; ++c) A[r * (r + 1) / 2 + c] = __ldg(Cr + S[c]);
+        A[L * (L + 1) / 2 + r] = __ldg(C + (size_t)vi * p + S[r]);
+        A[(L + 1) * (L + 2) / 2 + r] = __ldg(C + (size_t)vj * p + S[r]);
     }
-    const double rij = __ldg(C + (size_t)vi * p + vj);
-    // Cholesky (left-looking) with the two extra rows solved alongside.
+    A[L * (L + 1) / 2 + L] = 1.0;
+    A[(L + 1) * (L + 2) / 2 + L] = __ldg(C + (size_t)vi * p + vj);
+    A[(L + 1) * (L + 2) / 2 + L + 1] = 1.0;
 #pragma unroll
     for (int j = 0; j < L; ++j) {
-        double d = A[j * (j + 1) / 2 + j];
+        const double inv = 1.0 / A[j * (j + 1) / 2 + j];
 #pragma unroll
-        for (int k = 0; k < j; ++k) d -= A[j * (j + 1) / 2 + k] * A[j * (j + 1) / 2 + k];
-        d = sqrt(d);
-        const double inv = 1.0 / d;
-        A[j * (j + 1) / 2 + j] = d;
+        for (int i = j + 1; i < D; ++i) {
+            const double t = A[i * (i + 1) / 2 + j] * inv;
 #pragma unroll
-        for (int i = j + 1; i < L; ++i) {
-            double s = A[i * (i + 1) / 2 + j];
-#pragma unroll
-            for (int k = 0; k < j; ++k) s -= A[i * (i + 1) / 2 + k] * A[j * (j + 1) / 2 + k];
-            A[i * (i + 1) / 2 + j] = s * inv;
+            for (int k = j + 1; k <= i; ++k) A[i * (i + 1) / 2 + k] -= t * A[k * (k + 1) / 2 + j];
         }
-        double sa = a[j], sb = b[j];
-#pragma unroll
-        for (int k = 0; k < j; ++k) {
-            sa -= a[k] * A[j * (j + 1) / 2 + k];
-            sb -= b[k] * A[j * (j + 1) / 2 + k];
-        }
-        a[j] = sa * inv;
-        b[j] = sb * inv;
     }
-    double h00 = 1.0, h11 = 1.0, h01 = rij;
-#pragma unroll
-    for (int k = 0; k < L; ++k) {
-        h00 -= a[k] * a[k];
-        h11 -= b[k] * b[k];
-        h01 -= a[k] * b[k];
+    const double h00 = A[L * (L + 1) / 2 + L];
+    const double h01 = A[(L + 1) * (L + 2) / 2 + L];
+    const double h11 = A[(L + 1) * (L + 2) / 2 + L + 1];
+    const double rho2 = (h01 * h01) / (fabs(h00) * fabs(h11));
+    TestOut o;
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    if (rho2 < 1.0 && fabs(rho2 - t2) > 1e-12 * t2) {
+        o.rho2 = rho2;
+        o.zexact = inf;
+        o.remove = rho2 < t2;
+    } else {
+        const double z = z_of_rho(h01 / (sqrt(fabs(h00)) * sqrt(fabs(h11))));
+        o.rho2 = inf;
+        o.zexact = z;
+        o.remove = z < tau;
     }
-    const double rho = h01 / (sqrt(fabs(h00)) * sqrt(fabs(h11)));
-    return fabs(0.5 * (log(fabs(1.0 + rho)) - log(fabs(1.0 - rho))));
+    return o;
 }
 
 struct EdgeJob {
@@ -253,31 +296,55 @@ __device__ __forceinline__ bool level_active(DevState *st, int level, bool tau_v
     return true;
 }
 
-template <int L>
+// Min over the G-lane group (aligned groups of G lanes inside the warp).
+template <int G>
+__device__ __forceinline__ double group_min(double v) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(GCSL_FULL_MASK, v, o));
+    return v;
+}
+
+// Level kernel: groups of G lanes each own one edge (32 / G edges per warp) and walk its
+// merged key sequence G keys at a time.  Small groups keep the FP64 pipe busy at the
+// upper levels, where an edge has only a handful of candidate sets, and stop at most
+// G - 1 tests past the first remover.
+template <int L, int G>
 __global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__restrict__ C, int p,
                                                              const int *__restrict__ adj, const int *__restrict__ up,
                                                              const long long *__restrict__ prefix, double tau,
-                                                             bool tau_valid, uint16_t *G, double *zmin,
+                                                             double t2, bool tau_valid, uint16_t *G_, double *zmin,
                                                              int *sep_dense, int max_level, int *rec_pool,
                                                              long long rec_cap, DevState *st) {
     if (!level_active(st, L, tau_valid)) return;
-    const int lane = threadIdx.x & 31;
+    constexpr int GPW = 32 / G;  // groups per warp
+    const int lane = threadIdx.x & 31, gl = lane & (G - 1), gw = lane / G;
+    const unsigned gshift = (unsigned)(gw * G);
+    const unsigned gbits = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
     const long long n_edges = prefix[p];
     const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
     unsigned long long n_tests = 0, n_full = 0, n_removed = 0;
-    for (long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n_edges; e += warps) {
+    for (long long e0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * GPW; e0 < n_edges;
+         e0 += warps * GPW) {
+        const long long e = e0 + gw;
         EdgeJob J;
-        if (!load_edge<L>(adj, up, prefix, p, e, L, J)) {
-            if (lane == 0) set_status(st, GCSL_ERR_UNSUPPORTED);
-            continue;
+        J.T = 0;
+        bool has = e < n_edges;
+        if (has && !load_edge<L>(adj, up, prefix, p, e, L, J)) {
+            if (gl == 0) set_status(st, GCSL_ERR_UNSUPPORTED);
+            J.T = 0;
         }
-        n_full += J.T;
-        double zl = __longlong_as_double(0x7ff0000000000000ll);
-        bool removed = false;
-        for (long long base = 0; base < J.T; base += 32) {
-            const long long m = base + lane;
-            const bool valid = m < J.T;
-            double z = __longlong_as_double(0x7ff8000000000000ll);
+        if (has && gl == 0) n_full += J.T;
+        double r2min = inf, zmin_exact = inf;
+        bool removed = false, done = !has || J.T == 0;
+        long long base = 0;
+        while (__any_sync(GCSL_FULL_MASK, !done)) {
+            const long long m = base + gl;
+            const bool valid = !done && m < J.T;
+            TestOut o;
+            o.rho2 = inf;
+            o.zexact = inf;
+            o.remove = false;
             int S[L];
             if (valid) {
                 long long rank;
@@ -290,31 +357,40 @@ __global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__re
                 const int *nbrs = adj + (size_t)vi * p + 1;
 #pragma unroll
                 for (int c = 0; c < L; ++c) S[c] = resolve_position(nbrs, vj, pos[c]);
-                z = gauss_test_reg<L>(C, p, vi, vj, S);
+                o = gauss_test_reg<L>(C, p, vi, vj, S, tau, t2);
             }
-            const bool rem = valid && (z < tau);
-            const unsigned bal = __ballot_sync(GCSL_FULL_MASK, rem);
-            const int first = bal ? (__ffs(bal) - 1) : 32;
-            const double zc = (valid && lane <= first && !isnan(z)) ? z : __longlong_as_double(0x7ff0000000000000ll);
-            zl = fmin(zl, warp_min(zc));
-            const long long left = J.T - base;
-            n_tests += (unsigned long long)(bal ? first + 1 : (left < 32 ? left : 32));
-            if (bal) {
-                if (lane == first) write_removal(J, L, S, p, max_level, G, sep_dense, rec_pool, rec_cap, st);
-                removed = true;
-                break;
+            const unsigned bal = (__ballot_sync(GCSL_FULL_MASK, o.remove) >> gshift) & gbits;
+            const int first = bal ? (__ffs(bal) - 1) : G;
+            const bool fold = valid && gl <= first;
+            const double r2 = group_min<G>(fold ? o.rho2 : inf);
+            const double ze = group_min<G>((fold && !isnan(o.zexact)) ? o.zexact : inf);
+            if (!done) {
+                r2min = fmin(r2min, r2);
+                zmin_exact = fmin(zmin_exact, ze);
+                const long long left = J.T - base;
+                if (gl == 0) n_tests += (unsigned long long)(bal ? first + 1 : (left < G ? left : G));
+                if (bal) {
+                    if (gl == first) write_removal(J, L, S, p, max_level, G_, sep_dense, rec_pool, rec_cap, st);
+                    removed = true;
+                    done = true;
+                } else {
+                    base += G;
+                    if (base >= J.T) done = true;
+                }
             }
         }
-        if (lane == 0) {
+        if (has && gl == 0 && J.T > 0) {
+            // one logarithm pair per edge: Z is increasing in rho^2 on the monotone branch
+            const double zl = fmin(r2min < inf ? z_of_rho(sqrt(r2min)) : inf, zmin_exact);
             double *zp = zmin + (size_t)J.lo * p + J.hi;
             *zp = fmin(*zp, zl);
             n_removed += removed;
         }
     }
-    if (lane == 0) {
-        atomicAdd(&st->tests[L], n_tests);
-        atomicAdd(&st->tests_full[L], n_full);
-        atomicAdd(&st->removed[L], n_removed);
+    if (gl == 0) {
+        if (n_tests) atomicAdd(&st->tests[L], n_tests);
+        if (n_full) atomicAdd(&st->tests_full[L], n_full);
+        if (n_removed) atomicAdd(&st->removed[L], n_removed);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) st->edges[L] = (unsigned long long)n_edges;
 }
@@ -462,6 +538,13 @@ cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState
     return cudaGetLastError();
 }
 
+cudaError_t launch_recompact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s) {
+    const int threads = 256, wpb = threads / 32;
+    recompact_kernel<<<(p + wpb - 1) / wpb, threads, 0, s>>>(G, p, adj, up, st, level);
+    note_launch(1);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_scan_int(const int *cnt, int p, long long *prefix, DevState *st, cudaStream_t s) {
     row_scan_kernel<int><<<1, 1024, 0, s>>>(cnt, p, prefix, st);
     note_launch(1);
@@ -479,9 +562,11 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
                                int *rec_pool, long long rec_cap, DevState *st, int num_sms, cudaStream_t s) {
     const int threads = 256;
     const int blocks = num_sms * 8;
+    const double th = tanh(tau);
+    const double t2 = th * th;  // Z < tau  <=>  rho^2 < tanh(tau)^2 for |rho| < 1
 #define GCSL_LVL(K)                                                                                               \
     case K:                                                                                                       \
-        gauss_level_reg_kernel<K><<<blocks, threads, 0, s>>>(C, p, adj, up, prefix, tau, tau_valid, G, zmin,     \
+        gauss_level_reg_kernel<K, 32><<<blocks, threads, 0, s>>>(C, p, adj, up, prefix, tau, t2, tau_valid, G, zmin, \
                                                              sep_dense, max_level, rec_pool, rec_cap, st);        \
         break;
     switch (L) {
@@ -493,6 +578,10 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
         GCSL_LVL(6)
         GCSL_LVL(7)
         GCSL_LVL(8)
+        GCSL_LVL(9)
+        GCSL_LVL(10)
+        GCSL_LVL(11)
+        GCSL_LVL(12)
     default: {
         const int t = 128, wpb = t / 32;
         const int D = L + 2;

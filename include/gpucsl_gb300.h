@@ -74,6 +74,12 @@ int gcsl_corr_f64(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ld
 size_t gcsl_corr_tc_workspace_bytes(int64_t n, int32_t p);
 int gcsl_corr_f64_tc(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ldx, double *C, void *workspace,
                      size_t workspace_bytes, void *stream);
+/* The two stages of gcsl_corr_f64_tc on the same workspace: column statistics and the
+ * integer digit tiles (FP64 / integer work), then the tensor-core digit products,
+ * their exact reduction and the normalisation into C. */
+int gcsl_corr_tc_digits(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ldx, void *workspace,
+                        size_t workspace_bytes, void *stream);
+int gcsl_corr_tc_product(int64_t n, int32_t p, double *C, void *workspace, size_t workspace_bytes, void *stream);
 
 /* --------------------------------------------------- Gaussian skeleton (b,c,e) */
 /* Replaces the level loop of gpucsl/pc/discover_skeleton_gaussian.py:30-113
