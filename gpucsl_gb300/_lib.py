@@ -60,6 +60,7 @@ class GcslStats(ct.Structure):
             "tests_full": [int(x) for x in self.tests_full[:n]],
             "removed": [int(x) for x in self.removed[:n]],
             "max_degree": [int(x) for x in self.max_degree[:n]],
+            "level_ms": [float(x) for x in self.level_ms[:GCSL_MAX_LEVELS] if x > 0],
         }
 
 

@@ -7,7 +7,9 @@
 // host only checks the sticky `done` flag between batches; levels enqueued past the
 // end return at their first instruction.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -21,9 +23,13 @@ cudaError_t launch_scan_int(const int *cnt, int p, long long *prefix, DevState *
 cudaError_t launch_recompact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s);
 cudaError_t launch_scan_ll(const long long *cnt, int p, long long *prefix, DevState *st, cudaStream_t s);
 cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, const int *up, const long long *prefix,
-                               double tau, bool tau_valid, uint16_t *G, double *zmin, int *sep_dense, int max_level,
-                               int *rec_pool, long long rec_cap, DevState *st, int num_sms, cudaStream_t s);
-cudaError_t launch_pmax(const double *zmin, int p, long long n_obs, double *pmax, int num_sms, cudaStream_t s);
+                               double tau, bool tau_valid, uint16_t *G, double *zmin, double *r2min, int *sep_dense,
+                               int max_level, int *rec_pool, long long rec_cap, DevState *st, int num_sms,
+                               cudaStream_t s);
+cudaError_t launch_pmax(const double *zmin, const double *r2min, int p, long long n_obs, double *pmax, int num_sms,
+                        cudaStream_t s);
+cudaError_t launch_pmax_level0(const double *C, const double *zmin, int p, long long n_obs, double *pmax,
+                               int num_sms, cudaStream_t s);
 size_t corr_workspace_bytes(long long n, int p);
 cudaError_t corr_f64(const void *X, int dtype, long long n, int p, long long ldx, double *C, void *ws,
                      size_t ws_bytes, int num_sms, cudaStream_t s);
@@ -85,6 +91,60 @@ int device_sms() {
 
 int map_cuda(cudaError_t e) { return e == cudaSuccess ? GCSL_OK : GCSL_ERR_DEVICE; }
 
+// A second, lowest-priority stream per device for work that can overlap the level loop
+// (its blocks yield SMs to the latency-bound level kernels); created once per device,
+// never allocates device memory.
+struct SideStream {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+// Per-level device timing (gcsl_stats.level_ms) when GCSL_LEVEL_TIMING=1: one event per
+// level boundary on the solve's stream, from a pool created once per device.
+struct LevelTimer {
+    cudaEvent_t ev[GCSL_MAX_LEVELS + 2] = {};
+    bool ok = false;
+};
+
+LevelTimer *level_timer() {
+    static const bool enabled = [] {
+        const char *e = getenv("GCSL_LEVEL_TIMING");
+        return e && e[0] == '1';
+    }();
+    if (!enabled) return nullptr;
+    static LevelTimer timers[64];
+    static std::mutex mu;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    LevelTimer &t = timers[dev];
+    if (!t.ok) {
+        for (auto &e : t.ev)
+            if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        t.ok = true;
+    }
+    return &t;
+}
+
+SideStream *side_stream() {
+    static SideStream streams[64];
+    static std::mutex mu;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    SideStream &s = streams[dev];
+    if (!s.stream) {
+        int lo = 0, hi = 0;  // numerically larger = lower priority
+        if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess) lo = 0;
+        if (cudaStreamCreateWithPriority(&s.stream, cudaStreamNonBlocking, lo) != cudaSuccess) return nullptr;
+        if (cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+        if (cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+    }
+    return &s;
+}
+
 // Copy the device state into the public stats struct.
 int finish_stats(const DevState *d_st, gcsl_stats *stats, cudaStream_t s, bool discrete_edges, long long p) {
     DevState h;
@@ -111,31 +171,60 @@ int finish_stats(const DevState *d_st, gcsl_stats *stats, cudaStream_t s, bool d
     return h.status;
 }
 
-// Run levels 1..max_level with the given per-level enqueue function, checking the
-// sticky done flag between batches of 1, 2, 4, then 8 levels.
+// Pinned host words per device for the level loop's control reads (a pageable copy
+// costs a staging round trip).
+struct HostCtl {
+    int32_t *words = nullptr;  // [0] done, [1] max degree of the last level
+};
+
+HostCtl *host_ctl() {
+    static HostCtl ctl[64];
+    static std::mutex mu;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    HostCtl &c = ctl[dev];
+    if (!c.words && cudaMallocHost(reinterpret_cast<void **>(&c.words), 2 * sizeof(int32_t)) != cudaSuccess)
+        return nullptr;
+    return &c;
+}
+
+// Run levels 1..max_level with the given per-level enqueue function.  Levels are
+// enqueued in batches; between batches the host reads the done flag and the last
+// level's maximum degree d, and since degrees only shrink, level l can only run while
+// d - 1 >= l: the next batch ends at min(d - 1, last + 8), so no level is launched
+// past the termination point once the degrees have settled.
 template <typename EnqueueLevel>
 int run_levels(int max_level, DevState *d_st, cudaStream_t s, EnqueueLevel enqueue) {
-    int level = 1, batch = 1;
-    const int last = std::min(max_level, GCSL_MAX_LEVELS - 1);
-    while (level <= last) {
-        for (int b = 0; b < batch && level <= last; ++b, ++level) {
+    HostCtl *hc = host_ctl();
+    if (!hc) return GCSL_ERR_DEVICE;
+    int level = 1;
+    int bound = std::min(max_level, GCSL_MAX_LEVELS - 1);  // highest level that may still run
+    int batch = 1;
+    while (level <= bound) {
+        const int last = std::min(bound, level + batch - 1);
+        for (; level <= last; ++level) {
             cudaError_t e = enqueue(level);
             if (e != cudaSuccess) return GCSL_ERR_DEVICE;
         }
-        if (level > last) break;
-        int32_t done = 0;
-        cudaError_t e = cudaMemcpyAsync(&done, &d_st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+        if (level > bound) break;
+        cudaError_t e = cudaMemcpyAsync(&hc->words[0], &d_st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&hc->words[1], &d_st->max_degree[last], sizeof(int32_t), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return GCSL_ERR_DEVICE;
-        if (done) break;
+        if (hc->words[0]) break;
+        bound = std::min(bound, hc->words[1] - 1);
         batch = std::min(batch * 2, 8);
+        if (bound - level + 1 <= 8) batch = bound - level + 1;  // finish in one batch when it fits
     }
-    if (max_level >= GCSL_MAX_LEVELS) {
+    if (max_level >= GCSL_MAX_LEVELS && bound >= GCSL_MAX_LEVELS - 1) {
         // levels beyond the state arrays: only an error if the loop had not finished
-        int32_t done = 0;
-        cudaMemcpyAsync(&done, &d_st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
-        if (!done) return GCSL_ERR_UNSUPPORTED_LEVEL;
+        if (cudaMemcpyAsync(&hc->words[0], &d_st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return GCSL_ERR_DEVICE;
+        if (!hc->words[0]) return GCSL_ERR_UNSUPPORTED_LEVEL;
     }
     return GCSL_OK;
 }
@@ -144,7 +233,7 @@ struct GaussWs {
     DevState *st;
     int *adj, *up;
     long long *prefix;
-    double *zmin;
+    double *zmin, *r2min;
     size_t bytes;
 };
 
@@ -156,6 +245,7 @@ GaussWs carve_gauss(void *ws, size_t cap, int p) {
     w.up = c.take<int>((size_t)p);
     w.prefix = c.take<long long>((size_t)p + 1);
     w.zmin = c.take<double>((size_t)p * p);
+    w.r2min = c.take<double>((size_t)p * p);
     w.bytes = c.off;
     return w;
 }
@@ -261,7 +351,23 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int sms = device_sms();
     if (cudaMemsetAsync(w.st, 0, sizeof(DevState), s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    // r2min starts at 0x7f7f... = 1.4e306, above every rho^2 < 1 the levels can store
+    if (cudaMemsetAsync(w.r2min, 0x7f, sizeof(double) * (size_t)p * p, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    LevelTimer *lt = stats ? level_timer() : nullptr;
+    int n_timed = 0;  // events recorded: ev[0 .. n_timed]
+    if (lt) cudaEventRecord(lt->ev[0], s);
     if (host::launch_level0(C, p, thresholds[0], G, w.zmin, w.st, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    if (lt) {
+        cudaEventRecord(lt->ev[1], s);
+        n_timed = 1;
+    }
+    // pmax of the pairs removed at level 0 overlaps the level loop on the side stream
+    SideStream *ss = side_stream();
+    if (!ss) return GCSL_ERR_DEVICE;
+    if (cudaEventRecord(ss->fork, s) != cudaSuccess || cudaStreamWaitEvent(ss->stream, ss->fork, 0) != cudaSuccess)
+        return GCSL_ERR_DEVICE;
+    if (host::launch_pmax_level0(C, w.zmin, p, n_obs, pmax, sms, ss->stream) != cudaSuccess) return GCSL_ERR_DEVICE;
+    if (cudaEventRecord(ss->join, ss->stream) != cudaSuccess) return GCSL_ERR_DEVICE;
     int rc = run_levels(max_level, w.st, s, [&](int level) -> cudaError_t {
         // level 1 compacts the full matrix; later levels only shrink the previous lists
         cudaError_t e = (level == 1) ? host::launch_compact(G, p, w.adj, w.up, w.st, level, s)
@@ -270,13 +376,28 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
         const bool tau_valid = level < n_thresholds;
         const double tau = tau_valid ? thresholds[level] : 0.0;
         if (e == cudaSuccess)
-            e = host::launch_gauss_level(level, C, p, w.adj, w.up, w.prefix, tau, tau_valid, G, w.zmin, sepsets,
-                                         max_level, rec_pool, rec_cap, w.st, sms, s);
+            e = host::launch_gauss_level(level, C, p, w.adj, w.up, w.prefix, tau, tau_valid, G, w.zmin, w.r2min,
+                                         sepsets, max_level, rec_pool, rec_cap, w.st, sms, s);
+        if (lt && level + 1 < GCSL_MAX_LEVELS + 2) {
+            cudaEventRecord(lt->ev[level + 1], s);
+            n_timed = level + 1;
+        }
         return e;
     });
+    if (cudaStreamWaitEvent(s, ss->join, 0) != cudaSuccess) return GCSL_ERR_DEVICE;
     if (rc != GCSL_OK) return rc;
-    if (host::launch_pmax(w.zmin, p, n_obs, pmax, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
-    return finish_stats(w.st, stats, s, false, p);
+    if (host::launch_pmax(w.zmin, w.r2min, p, n_obs, pmax, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    const int frc = finish_stats(w.st, stats, s, false, p);
+    if (lt) {
+        // level l spans events l .. l+1 (level 0 includes the state reset); levels that
+        // were enqueued but found the loop finished are reported as well
+        for (int l = 0; l < n_timed && l < GCSL_MAX_LEVELS; ++l) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, lt->ev[l], lt->ev[l + 1]) == cudaSuccess) stats->level_ms[l] = ms;
+        }
+        cudaGetLastError();  // a failed timing query must not surface in a later launch check
+    }
+    return frc;
 }
 
 size_t gcsl_disc_workspace_bytes(int32_t p, int64_t n, int32_t max_level, int32_t max_dim) {

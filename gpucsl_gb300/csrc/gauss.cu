@@ -20,30 +20,64 @@
 namespace gcsl {
 
 // ----------------------------------------------------------------- level 0
-// Warp per row i, lanes over j > i: Z = |0.5 log|(1+r)/(1-r)||, r = C[i*p + j];
-// remove iff Z < tau0; z*(i,j) = Z (NaN ignored); zero diagonal.
-__global__ void gauss_level0_kernel(const double *__restrict__ C, int p, double tau0, uint16_t *__restrict__ G,
-                                    double *__restrict__ zmin, DevState *st) {
-    const int lane = threadIdx.x & 31;
-    const int warps = (gridDim.x * blockDim.x) >> 5;
+// 32 x 32 tiles of the upper triangle (tile row bi <= tile column bj): for i < j,
+// Z = |0.5 log|(1+r)/(1-r)||, r = C[i*p + j]; remove iff Z < tau0.  Kept pairs store
+// z* = Z (NaN ignored); removed pairs store the marker -1: their z* is final and their
+// pmax is computed from C by pmax_level0_kernel, concurrently with the later levels.
+// The mirrored skeleton entries are written through a shared-memory transpose so both
+// triangles are stored row-contiguously; zero diagonal.
+__global__ void gauss_level0_kernel(const double *__restrict__ C, int p, double tau0, double t0sq,
+                                    uint16_t *__restrict__ G, double *__restrict__ zmin, DevState *st) {
+    __shared__ uint16_t tg[32][33];
+    const int nb = (p + 31) / 32;
+    int rem = blockIdx.x, bi = 0;
+    while (rem >= nb - bi) {
+        rem -= nb - bi;
+        ++bi;
+    }
+    const int bj = bi + rem;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 rows per pass
     unsigned long long removed = 0;
-    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p; i += warps) {
-        const double *Ci = C + (size_t)i * p;
-        for (int j = i + 1 + lane; j < p; j += 32) {
-            const double r = __ldg(Ci + j);
-            const double z = fabs(0.5 * log(fabs((1.0 + r) / (1.0 - r))));
-            const bool rem = z < tau0;
-            const uint16_t g = rem ? 0 : 1;
-            G[(size_t)i * p + j] = g;
-            G[(size_t)j * p + i] = g;
+    for (int r = ty; r < 32; r += 8) {
+        const int i = bi * 32 + r, j = bj * 32 + tx;
+        uint16_t g = 0;
+        if (i < p && j < p && i < j) {
+            const double c = __ldg(C + (size_t)i * p + j);
+            // Z0 = atanh-like in |r| on [0, 1): Z0 < tau0 <=> r^2 < tanh(tau0)^2; the knife
+            // edge, |r| >= 1 and NaN take the reference formula
+            const double r2 = c * c;
+            bool rem0;
+            double z = -1.0;  // marker: z* of a level-0 removal is finished on the side stream
+            if (r2 < 1.0 && fabs(r2 - t0sq) > 1e-12 * t0sq) {
+                rem0 = r2 < t0sq;
+                if (!rem0) z = fabs(0.5 * log(fabs((1.0 + c) / (1.0 - c))));
+            } else {
+                z = fabs(0.5 * log(fabs((1.0 + c) / (1.0 - c))));
+                rem0 = z < tau0;
+                if (rem0) z = -1.0;
+            }
+            g = rem0 ? 0 : 1;
             zmin[(size_t)i * p + j] = isnan(z) ? __longlong_as_double(0x7ff0000000000000ll) : z;
-            removed += rem;
+            removed += rem0;
         }
-        if (lane == 0) G[(size_t)i * p + i] = 0;
+        if (i < p && j < p && (bi != bj || i <= j)) G[(size_t)i * p + j] = g;  // includes the zero diagonal
+        tg[r][tx] = g;
+    }
+    __syncthreads();
+    if (bi != bj) {
+        for (int r = ty; r < 32; r += 8) {
+            const int j = bj * 32 + r, i = bi * 32 + tx;  // lower triangle (j, i), j > i
+            if (i < p && j < p) G[(size_t)j * p + i] = tg[tx][r];
+        }
+    } else {
+        for (int r = ty; r < 32; r += 8) {
+            const int j = bj * 32 + r, i = bi * 32 + tx;
+            if (i < p && j < p && j > i) G[(size_t)j * p + i] = tg[tx][r];
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) removed += __shfl_xor_sync(GCSL_FULL_MASK, removed, o);
-    if (lane == 0 && removed) atomicAdd(&st->removed[0], removed);
+    if ((threadIdx.x & 31) == 0 && removed) atomicAdd(&st->removed[0], removed);
 }
 
 // ------------------------------------------------------------- compaction
@@ -172,6 +206,32 @@ __device__ __forceinline__ double z_of_rho(double rho) {
 template <int L>
 __device__ __forceinline__ TestOut gauss_test_reg(const double *__restrict__ C, int p, int vi, int vj, const int *S,
                                                   double tau, double t2) {
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    if constexpr (L == 1) {
+        // closed form: with m = C_ss, a = C_vi,s, b = C_vj,s, r = C_vi,vj the trailing block
+        // times m is [[m - a^2, r m - a b], [., m - b^2]]; the decision compares
+        // num = (r m - a b)^2 with t^2 den, den = |m - a^2| |m - b^2|, without a division
+        const double m = __ldg(C + (size_t)S[0] * p + S[0]);
+        const double a = __ldg(C + (size_t)vi * p + S[0]);
+        const double b = __ldg(C + (size_t)vj * p + S[0]);
+        const double r = __ldg(C + (size_t)vi * p + vj);
+        const double d00 = fma(-a, a, m), d11 = fma(-b, b, m);
+        const double n01 = fma(r, m, -(a * b));
+        const double num = n01 * n01, den = fabs(d00) * fabs(d11);
+        TestOut o;
+        const double tden = t2 * den;
+        if (num < den && fabs(num - tden) > 1e-12 * tden) {
+            o.rho2 = num / den;
+            o.zexact = inf;
+            o.remove = num < tden;
+        } else {
+            const double z = z_of_rho(n01 / (sqrt(fabs(d00)) * sqrt(fabs(d11))));
+            o.rho2 = inf;
+            o.zexact = z;
+            o.remove = z < tau;
+        }
+        return o;
+    }
     constexpr int D = L + 2;
     double A[D * (D + 1) / 2];  // row-packed lower triangle; rows 0..L-1 = S, L = v_i, L+1 = v_j
 #pragma unroll
@@ -200,7 +260,6 @@ __device__ __forceinline__ TestOut gauss_test_reg(const double *__restrict__ C, 
     const double h11 = A[(L + 1) * (L + 2) / 2 + L + 1];
     const double rho2 = (h01 * h01) / (fabs(h00) * fabs(h11));
     TestOut o;
-    const double inf = __longlong_as_double(0x7ff0000000000000ll);
     if (rho2 < 1.0 && fabs(rho2 - t2) > 1e-12 * t2) {
         o.rho2 = rho2;
         o.zexact = inf;
@@ -313,8 +372,8 @@ __global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__re
                                                              const int *__restrict__ adj, const int *__restrict__ up,
                                                              const long long *__restrict__ prefix, double tau,
                                                              double t2, bool tau_valid, uint16_t *G_, double *zmin,
-                                                             int *sep_dense, int max_level, int *rec_pool,
-                                                             long long rec_cap, DevState *st) {
+                                                             double *r2min_pair, int *sep_dense, int max_level,
+                                                             int *rec_pool, long long rec_cap, DevState *st) {
     if (!level_active(st, L, tau_valid)) return;
     constexpr int GPW = 32 / G;  // groups per warp
     const int lane = threadIdx.x & 31, gl = lane & (G - 1), gw = lane / G;
@@ -380,10 +439,11 @@ __global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__re
             }
         }
         if (has && gl == 0 && J.T > 0) {
-            // one logarithm pair per edge: Z is increasing in rho^2 on the monotone branch
-            const double zl = fmin(r2min < inf ? z_of_rho(sqrt(r2min)) : inf, zmin_exact);
-            double *zp = zmin + (size_t)J.lo * p + J.hi;
-            *zp = fmin(*zp, zl);
+            // z* candidates: exact Z into zmin, the monotone branch's min rho^2 into r2min
+            // (converted to Z once per pair by pmax_kernel)
+            const size_t ix = (size_t)J.lo * p + J.hi;
+            if (zmin_exact < inf) zmin[ix] = fmin(zmin[ix], zmin_exact);
+            if (r2min < inf) r2min_pair[ix] = fmin(r2min_pair[ix], r2min);
             n_removed += removed;
         }
     }
@@ -497,17 +557,49 @@ __global__ void __launch_bounds__(128) gauss_level_smem_kernel(const double *__r
 // ------------------------------------------------------------ zmin -> pmax
 // pmax_ij = 2 * sf(sqrt(n - 3) * z*_ij) for i < j (0 when z* = +inf), -1 elsewhere.
 // 2 sf(x) = erfc(x / sqrt 2), written as scipy's ndtr does it (erf below 1/sqrt 2).
-__global__ void pmax_kernel(const double *__restrict__ zmin, int p, double sqrt_nm3, double *__restrict__ pmax) {
-    const long long total = (long long)p * p;
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
-         k += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(k / p), j = (int)(k - (long long)i * p);
-        double out = -1.0;
-        if (i < j) {
-            const double x = fabs(sqrt_nm3 * zmin[k]) * 0.70710678118654752440;
-            out = (x < 0.70710678118654752440) ? 1.0 - erf(x) : erfc(x);
+// Grid: (column blocks of 256, rows); no index division.
+__device__ __forceinline__ double two_sf(double x) {
+    x = fabs(x) * 0.70710678118654752440;
+    return (x < 0.70710678118654752440) ? 1.0 - erf(x) : erfc(x);
+}
+
+// Pairs whose z* may still change after level 0 (zmin >= 0) and the -1 fill; pairs
+// removed at level 0 (marker -1) are left to pmax_level0_kernel.
+__global__ void pmax_kernel(const double *__restrict__ zmin, const double *__restrict__ r2min, int p,
+                            double sqrt_nm3, double *__restrict__ pmax) {
+    const int i = blockIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= p) return;
+    const size_t k = (size_t)i * p + j;
+    if (i < j) {
+        double z = zmin[k];
+        if (!(z < 0.0)) {
+            const double r2 = r2min[k];
+            if (r2 < 1.0) z = fmin(z, z_of_rho(sqrt(r2)));  // Z increasing in rho^2 below 1
+            pmax[k] = two_sf(sqrt_nm3 * z);
         }
-        pmax[k] = out;
+    } else {
+        pmax[k] = -1.0;
+    }
+}
+
+// Pairs removed at level 0: z* = Z(r) with r = C[i*p + j] (gaussian_ci.cu:36-37), pmax.
+// Launched on a second stream right after level 0; the later levels never touch these
+// pairs, so it runs concurrently with them.
+__global__ void pmax_level0_kernel(const double *__restrict__ C, const double *__restrict__ zmin, int p,
+                                   double sqrt_nm3, double *__restrict__ pmax) {
+    // one block per SM, warps over rows, lanes over columns: a small footprint that
+    // fills the FP64 issue slots the latency-bound level kernels leave idle
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p; i += warps) {
+        for (int j = i + 1 + lane; j < p; j += 32) {
+            const size_t k = (size_t)i * p + j;
+            if (zmin[k] < 0.0) {
+                const double c = C[k];
+                pmax[k] = two_sf(sqrt_nm3 * fabs(0.5 * log(fabs((1.0 + c) / (1.0 - c)))));
+            }
+        }
     }
 }
 
@@ -523,9 +615,9 @@ namespace host {
 
 cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, DevState *st,
                           cudaStream_t s) {
-    const int threads = 256, warps_per_block = threads / 32;
-    int blocks = (p + warps_per_block - 1) / warps_per_block;
-    gauss_level0_kernel<<<blocks, threads, 0, s>>>(C, p, tau0, G, zmin, st);
+    const int nb = (p + 31) / 32;
+    const double t0 = tanh(tau0);
+    gauss_level0_kernel<<<nb * (nb + 1) / 2, 256, 0, s>>>(C, p, tau0, t0 * t0, G, zmin, st);
     note_launch(1);
     return cudaGetLastError();
 }
@@ -558,16 +650,18 @@ cudaError_t launch_scan_ll(const long long *cnt, int p, long long *prefix, DevSt
 }
 
 cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, const int *up, const long long *prefix,
-                               double tau, bool tau_valid, uint16_t *G, double *zmin, int *sep_dense, int max_level,
-                               int *rec_pool, long long rec_cap, DevState *st, int num_sms, cudaStream_t s) {
-    const int threads = 256;
-    const int blocks = num_sms * 8;
+                               double tau, bool tau_valid, uint16_t *G, double *zmin, double *r2min, int *sep_dense,
+                               int max_level, int *rec_pool, long long rec_cap, DevState *st, int num_sms,
+                               cudaStream_t s) {
+    // register-heavy upper levels run 128-thread blocks so a full wave of warps is resident
+    const int threads = L >= 4 ? 128 : 256;
+    const int blocks = num_sms * (L >= 4 ? 12 : 8);
     const double th = tanh(tau);
     const double t2 = th * th;  // Z < tau  <=>  rho^2 < tanh(tau)^2 for |rho| < 1
 #define GCSL_LVL(K)                                                                                               \
     case K:                                                                                                       \
         gauss_level_reg_kernel<K, 32><<<blocks, threads, 0, s>>>(C, p, adj, up, prefix, tau, t2, tau_valid, G, zmin, \
-                                                             sep_dense, max_level, rec_pool, rec_cap, st);        \
+                                                                 r2min, sep_dense, max_level, rec_pool, rec_cap, st);\
         break;
     switch (L) {
         GCSL_LVL(1)
@@ -605,9 +699,17 @@ cudaError_t launch_unrank(int K, int L, long long count, int *out, cudaStream_t 
     return cudaGetLastError();
 }
 
-cudaError_t launch_pmax(const double *zmin, int p, long long n_obs, double *pmax, int num_sms, cudaStream_t s) {
+cudaError_t launch_pmax_level0(const double *C, const double *zmin, int p, long long n_obs, double *pmax,
+                               int num_sms, cudaStream_t s) {
+    pmax_level0_kernel<<<num_sms, 256, 0, s>>>(C, zmin, p, sqrt((double)(n_obs - 3)), pmax);
+    note_launch(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pmax(const double *zmin, const double *r2min, int p, long long n_obs, double *pmax, int num_sms,
+                        cudaStream_t s) {
     const double sq = sqrt((double)(n_obs - 3));
-    pmax_kernel<<<num_sms * 4, 256, 0, s>>>(zmin, p, sq, pmax);
+    pmax_kernel<<<dim3((p + 255) / 256, p), 256, 0, s>>>(zmin, r2min, p, sq, pmax);
     note_launch(1);
     return cudaGetLastError();
 }
