@@ -16,7 +16,7 @@
 
 namespace gcsl {
 namespace host {
-cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, DevState *st,
+cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, int *kept, DevState *st,
                           cudaStream_t s);
 cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s);
 cudaError_t launch_scan_int(const int *cnt, int p, long long *prefix, DevState *st, cudaStream_t s);
@@ -26,7 +26,8 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
                                double tau, bool tau_valid, uint16_t *G, double *zmin, double *r2min, int *sep_dense,
                                int max_level, int *rec_pool, long long rec_cap, DevState *st, int num_sms,
                                cudaStream_t s);
-cudaError_t launch_pmax(const double *zmin, const double *r2min, int p, long long n_obs, double *pmax, int num_sms,
+cudaError_t launch_pmax(const int *kept, const DevState *st, const double *zmin, const double *r2min, int p,
+                        long long n_obs, double *pmax, int num_sms,
                         cudaStream_t s);
 cudaError_t launch_pmax_level0(const double *C, const double *zmin, int p, long long n_obs, double *pmax,
                                int num_sms, cudaStream_t s);
@@ -234,6 +235,7 @@ struct GaussWs {
     int *adj, *up;
     long long *prefix;
     double *zmin, *r2min;
+    int *kept;
     size_t bytes;
 };
 
@@ -246,6 +248,7 @@ GaussWs carve_gauss(void *ws, size_t cap, int p) {
     w.prefix = c.take<long long>((size_t)p + 1);
     w.zmin = c.take<double>((size_t)p * p);
     w.r2min = c.take<double>((size_t)p * p);
+    w.kept = c.take<int>((size_t)p * (p - 1) / 2 + 1);
     w.bytes = c.off;
     return w;
 }
@@ -345,6 +348,7 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
                         double *pmax, gcsl_stats *stats, void *workspace, size_t workspace_bytes, void *stream) {
     if (!C || !G || !pmax || p < 1 || n_obs < 4 || !thresholds || n_thresholds < 1 || max_level < 0)
         return GCSL_ERR_INVALID_ARG;
+    if (p > GCSL_GAUSS_MAX_P) return GCSL_ERR_UNSUPPORTED;
     if (rec_pool == nullptr) rec_cap = 0;
     GaussWs w = carve_gauss(workspace, workspace_bytes, p);
     if (!workspace || w.bytes > workspace_bytes) return GCSL_ERR_WORKSPACE;
@@ -356,7 +360,7 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
     LevelTimer *lt = stats ? level_timer() : nullptr;
     int n_timed = 0;  // events recorded: ev[0 .. n_timed]
     if (lt) cudaEventRecord(lt->ev[0], s);
-    if (host::launch_level0(C, p, thresholds[0], G, w.zmin, w.st, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    if (host::launch_level0(C, p, thresholds[0], G, w.zmin, w.kept, w.st, s) != cudaSuccess) return GCSL_ERR_DEVICE;
     if (lt) {
         cudaEventRecord(lt->ev[1], s);
         n_timed = 1;
@@ -386,7 +390,8 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
     });
     if (cudaStreamWaitEvent(s, ss->join, 0) != cudaSuccess) return GCSL_ERR_DEVICE;
     if (rc != GCSL_OK) return rc;
-    if (host::launch_pmax(w.zmin, w.r2min, p, n_obs, pmax, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    if (host::launch_pmax(w.kept, w.st, w.zmin, w.r2min, p, n_obs, pmax, sms, s) != cudaSuccess)
+        return GCSL_ERR_DEVICE;
     const int frc = finish_stats(w.st, stats, s, false, p);
     if (lt) {
         // level l spans events l .. l+1 (level 0 includes the state reset); levels that

@@ -27,7 +27,7 @@ struct DevState {
     int32_t status;                          // first error code seen on the device
     int32_t done;                            // level loop finished (sticky)
     int32_t last_level;                      // highest level whose tests ran
-    int32_t pad;
+    int32_t n_kept;                          // pairs kept at level 0 (Gaussian)
     int32_t max_degree[GCSL_MAX_LEVELS];     // max compacted degree at level start
     unsigned long long edges[GCSL_MAX_LEVELS];
     unsigned long long tests[GCSL_MAX_LEVELS];

@@ -6,7 +6,7 @@
 //   level l <= 12  gauss_level_reg_kernel  (reference: gaussian_ci.cu:66-120,
 //                                           helpers/gaussian_helpers.cu:240-262)
 //   level l > 12   gauss_level_smem_kernel
-//   zmin -> pmax   pmax_kernel             (reference: gpucsl/pc/helpers.py:62-82)
+//   zmin -> pmax   pmax_level0_kernel, pmax_kept_kernel (reference: gpucsl/pc/helpers.py:62-82)
 //
 // Work decomposition of a level: one warp owns one undirected edge {lo, hi} alive at
 // level start and walks the merged key sequence of both directions, key = (rank, dir)
@@ -22,12 +22,14 @@ namespace gcsl {
 // ----------------------------------------------------------------- level 0
 // 32 x 32 tiles of the upper triangle (tile row bi <= tile column bj): for i < j,
 // Z = |0.5 log|(1+r)/(1-r)||, r = C[i*p + j]; remove iff Z < tau0.  Kept pairs store
-// z* = Z (NaN ignored); removed pairs store the marker -1: their z* is final and their
-// pmax is computed from C by pmax_level0_kernel, concurrently with the later levels.
+// z* = Z (NaN ignored) and append i * p + j to `kept`; removed pairs store the marker
+// -1: their z* is final and their pmax is computed from C by pmax_level0_kernel,
+// concurrently with the later levels.
 // The mirrored skeleton entries are written through a shared-memory transpose so both
 // triangles are stored row-contiguously; zero diagonal.
 __global__ void gauss_level0_kernel(const double *__restrict__ C, int p, double tau0, double t0sq,
-                                    uint16_t *__restrict__ G, double *__restrict__ zmin, DevState *st) {
+                                    uint16_t *__restrict__ G, double *__restrict__ zmin, int *__restrict__ kept,
+                                    DevState *st) {
     __shared__ uint16_t tg[32][33];
     const int nb = (p + 31) / 32;
     int rem = blockIdx.x, bi = 0;
@@ -59,6 +61,14 @@ __global__ void gauss_level0_kernel(const double *__restrict__ C, int p, double 
             g = rem0 ? 0 : 1;
             zmin[(size_t)i * p + j] = isnan(z) ? __longlong_as_double(0x7ff0000000000000ll) : z;
             removed += rem0;
+        }
+        // kept pairs join the list whose pmax is finished after the last level
+        const unsigned km = __ballot_sync(GCSL_FULL_MASK, g != 0 && i < j);
+        if (km) {
+            int base = 0;
+            if (tx == 0) base = atomicAdd(&st->n_kept, __popc(km));
+            base = __shfl_sync(GCSL_FULL_MASK, base, 0);
+            if (g != 0 && i < j) kept[base + __popc(km & ((1u << tx) - 1u))] = i * p + j;
         }
         if (i < p && j < p && (bi != bj || i <= j)) G[(size_t)i * p + j] = g;  // includes the zero diagonal
         tg[r][tx] = g;
@@ -558,47 +568,99 @@ __global__ void __launch_bounds__(128) gauss_level_smem_kernel(const double *__r
 // pmax_ij = 2 * sf(sqrt(n - 3) * z*_ij) for i < j (0 when z* = +inf), -1 elsewhere.
 // 2 sf(x) = erfc(x / sqrt 2), written as scipy's ndtr does it (erf below 1/sqrt 2).
 // Grid: (column blocks of 256, rows); no index division.
-__device__ __forceinline__ double two_sf(double x) {
-    x = fabs(x) * 0.70710678118654752440;
-    return (x < 0.70710678118654752440) ? 1.0 - erf(x) : erfc(x);
-}
+// ------------------------------------------------------------------ p-values
+// 2 sf(z) = erfc(z / sqrt 2) from Taylor expansions of erfc about the centres
+// c_m = (m + 1/2) / 8, m < 32, which cover [0, 4):  erfc(c + t) = sum_k a_k t^k with
+// a_0 = erfc(c) and a_{k+1} = b_k / (k + 1), where b_k are the Taylor coefficients of
+// erfc'(c + t) = erfc'(c) exp(-2 c t - t^2):  b_0 = -(2 / sqrt pi) exp(-c^2) and
+// (k + 1) b_{k+1} = -2 c b_k - 2 b_{k-1} (from E' = -(2c + 2t) E for E = exp(-2ct - t^2)).
+// With |t| <= 1/16, 13 terms leave a truncation error below 1e-18 of the value on the
+// whole range; arguments from 4 on (and NaN) go to the library erfc.  One Horner chain
+// replaces erf/erfc, which matters on a GPU whose FP64 pipe is 1/64 of its FP32 pipe.
+constexpr int SF_CENTRES = 32, SF_TERMS = 13;
 
-// Pairs whose z* may still change after level 0 (zmin >= 0) and the -1 fill; pairs
-// removed at level 0 (marker -1) are left to pmax_level0_kernel.
-__global__ void pmax_kernel(const double *__restrict__ zmin, const double *__restrict__ r2min, int p,
-                            double sqrt_nm3, double *__restrict__ pmax) {
-    const int i = blockIdx.y;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= p) return;
-    const size_t k = (size_t)i * p + j;
-    if (i < j) {
-        double z = zmin[k];
-        if (!(z < 0.0)) {
-            const double r2 = r2min[k];
-            if (r2 < 1.0) z = fmin(z, z_of_rho(sqrt(r2)));  // Z increasing in rho^2 below 1
-            pmax[k] = two_sf(sqrt_nm3 * z);
+// Built by each block into shared memory (one thread per centre).
+__device__ void sf_table_build(double (*a)[SF_TERMS]) {
+    for (int m = threadIdx.x; m < SF_CENTRES; m += blockDim.x) {
+        const double c = (m + 0.5) * 0.125;
+        double bprev = 0.0, b = -1.12837916709551257390 * exp(-c * c);  // 2 / sqrt(pi)
+        a[m][0] = erfc(c);
+        for (int k = 0; k + 1 < SF_TERMS; ++k) {
+            a[m][k + 1] = b / (k + 1);
+            const double bn = (-2.0 * c * b - 2.0 * bprev) / (k + 1);
+            bprev = b;
+            b = bn;
         }
-    } else {
-        pmax[k] = -1.0;
     }
 }
 
-// Pairs removed at level 0: z* = Z(r) with r = C[i*p + j] (gaussian_ci.cu:36-37), pmax.
-// Launched on a second stream right after level 0; the later levels never touch these
-// pairs, so it runs concurrently with them.
+__device__ __forceinline__ double two_sf_tab(double z, const double (*a)[SF_TERMS]) {
+    const double x = fabs(z) * 0.70710678118654752440;
+    if (!(x < 4.0)) return erfc(x);
+    const int m = (int)(x * 8.0);
+    const double t = x - (m + 0.5) * 0.125;
+    double v = a[m][SF_TERMS - 1];
+#pragma unroll
+    for (int k = SF_TERMS - 2; k >= 0; --k) v = fma(v, t, a[m][k]);
+    return v;
+}
+
+// Z(r) = |atanh r|: for r^2 < 1/100 the series |r| sum_{k<10} r^{2k} / (2k + 1)
+// (truncation below 1e-20 of the value), else the reference's form
+// |0.5 ln|(1 + r) / (1 - r)|| (gaussian_ci.cu:36-37).
+__device__ __forceinline__ double fisher_z(double r) {
+    const double u = r * r;
+    if (u < 0.01) {
+        double s = 1.0 / 19.0;
+        s = fma(s, u, 1.0 / 17.0);
+        s = fma(s, u, 1.0 / 15.0);
+        s = fma(s, u, 1.0 / 13.0);
+        s = fma(s, u, 1.0 / 11.0);
+        s = fma(s, u, 1.0 / 9.0);
+        s = fma(s, u, 1.0 / 7.0);
+        s = fma(s, u, 1.0 / 5.0);
+        s = fma(s, u, 1.0 / 3.0);
+        s = fma(s, u, 1.0);
+        return fabs(r) * s;
+    }
+    return fabs(0.5 * log(fabs((1.0 + r) / (1.0 - r))));
+}
+
+// Pairs kept at level 0 (the list the level-0 kernel appended): z* = min(zmin, Z of the
+// smallest rho^2 any later level stored), pmax = 2 sf(sqrt(n - 3) z*)
+// (helpers.py:62-82 with the FP64 z*).
+__global__ void pmax_kept_kernel(const int *__restrict__ kept, const DevState *__restrict__ st,
+                                 const double *__restrict__ zmin, const double *__restrict__ r2min, double sqrt_nm3,
+                                 double *__restrict__ pmax) {
+    __shared__ double tab[SF_CENTRES][SF_TERMS];
+    sf_table_build(tab);
+    __syncthreads();
+    const int count = st->n_kept;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        const int k = kept[t];
+        double z = zmin[k];
+        const double r2 = r2min[k];
+        if (r2 < 1.0) z = fmin(z, fisher_z(sqrt(r2)));  // Z increasing in rho^2 below 1
+        pmax[k] = two_sf_tab(sqrt_nm3 * z, tab);
+    }
+}
+
+// Every other entry: pairs removed at level 0 (marker zmin = -1) get z* = Z(r) with
+// r = C[i*p + j] (gaussian_ci.cu:36-37), the lower triangle and diagonal -1.  Launched on
+// a second stream right after level 0; the later levels never touch these entries, so it
+// runs concurrently with them.
 __global__ void pmax_level0_kernel(const double *__restrict__ C, const double *__restrict__ zmin, int p,
                                    double sqrt_nm3, double *__restrict__ pmax) {
-    // one block per SM, warps over rows, lanes over columns: a small footprint that
-    // fills the FP64 issue slots the latency-bound level kernels leave idle
-    const int lane = threadIdx.x & 31;
-    const int warps = (gridDim.x * blockDim.x) >> 5;
-    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p; i += warps) {
-        for (int j = i + 1 + lane; j < p; j += 32) {
-            const size_t k = (size_t)i * p + j;
-            if (zmin[k] < 0.0) {
-                const double c = C[k];
-                pmax[k] = two_sf(sqrt_nm3 * fabs(0.5 * log(fabs((1.0 + c) / (1.0 - c)))));
-            }
+    __shared__ double tab[SF_CENTRES][SF_TERMS];
+    sf_table_build(tab);
+    __syncthreads();
+    const unsigned total = (unsigned)p * (unsigned)p;  // p <= 46340: fits in 31 bits
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+        const int i = (int)(k / (unsigned)p), j = (int)(k - (unsigned)i * (unsigned)p);
+        if (i >= j) {
+            pmax[k] = -1.0;
+        } else if (zmin[k] < 0.0) {
+            pmax[k] = two_sf_tab(sqrt_nm3 * fisher_z(C[k]), tab);
         }
     }
 }
@@ -613,11 +675,11 @@ __global__ void unrank_kernel(int K, int L, long long count, int *out) {
 // ------------------------------------------------------------- host launchers
 namespace host {
 
-cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, DevState *st,
+cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, int *kept, DevState *st,
                           cudaStream_t s) {
     const int nb = (p + 31) / 32;
     const double t0 = tanh(tau0);
-    gauss_level0_kernel<<<nb * (nb + 1) / 2, 256, 0, s>>>(C, p, tau0, t0 * t0, G, zmin, st);
+    gauss_level0_kernel<<<nb * (nb + 1) / 2, 256, 0, s>>>(C, p, tau0, t0 * t0, G, zmin, kept, st);
     note_launch(1);
     return cudaGetLastError();
 }
@@ -701,15 +763,20 @@ cudaError_t launch_unrank(int K, int L, long long count, int *out, cudaStream_t 
 
 cudaError_t launch_pmax_level0(const double *C, const double *zmin, int p, long long n_obs, double *pmax,
                                int num_sms, cudaStream_t s) {
-    pmax_level0_kernel<<<num_sms, 256, 0, s>>>(C, zmin, p, sqrt((double)(n_obs - 3)), pmax);
+    const long long total = (long long)p * p;
+    const long long want = (total + 255) / 256;
+    const int blocks = (int)(want < (long long)num_sms * 4 ? want : (long long)num_sms * 4);
+    pmax_level0_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(C, zmin, p, sqrt((double)(n_obs - 3)), pmax);
     note_launch(1);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pmax(const double *zmin, const double *r2min, int p, long long n_obs, double *pmax, int num_sms,
-                        cudaStream_t s) {
-    const double sq = sqrt((double)(n_obs - 3));
-    pmax_kernel<<<dim3((p + 255) / 256, p), 256, 0, s>>>(zmin, r2min, p, sq, pmax);
+cudaError_t launch_pmax(const int *kept, const DevState *st, const double *zmin, const double *r2min, int p,
+                        long long n_obs, double *pmax, int num_sms, cudaStream_t s) {
+    const long long pairs = (long long)p * (p - 1) / 2;
+    const long long want = (pairs + 255) / 256;
+    const int blocks = (int)(want < (long long)num_sms * 2 ? want : (long long)num_sms * 2);
+    pmax_kept_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(kept, st, zmin, r2min, sqrt((double)(n_obs - 3)), pmax);
     note_launch(1);
     return cudaGetLastError();
 }

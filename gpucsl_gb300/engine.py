@@ -34,7 +34,7 @@ def records_to_dense(rec: np.ndarray, n_ints: int, p: int, max_level: int) -> np
     return out
 
 
-def correlation(X, out=None, workspace=None, method: str = "dfma"):
+def correlation(X, out=None, workspace=None, method: str = "tc"):
     """FP64 correlation matrix of device samples X (n x p, float64/float32, row-major).
 
     method "dfma": FP64 GEMM on the CUDA cores; "tc": exact integer-digit products on

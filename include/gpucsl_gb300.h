@@ -93,7 +93,10 @@ int gcsl_corr_tc_product(int64_t n, int32_t p, double *C, void *workspace, size_
  *                by the caller), or NULL
  *   rec_pool     optional int32 record pool of rec_cap ints, or NULL
  *   pmax         p x p FP64 out (upper triangle p-values, -1 on/below the diagonal)
- *   stats        optional host struct; when given the call synchronises `stream`. */
+ *   stats        optional host struct; when given the call synchronises `stream`.
+ * p > GCSL_GAUSS_MAX_P (pair indices i * p + j must fit in int32) returns
+ * GCSL_ERR_UNSUPPORTED. */
+#define GCSL_GAUSS_MAX_P 46340
 size_t gcsl_gauss_workspace_bytes(int32_t p, int32_t max_level);
 int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double *thresholds, int32_t n_thresholds,
                         int32_t max_level, uint16_t *G, int32_t *sepsets, int32_t *rec_pool, int64_t rec_cap,
@@ -108,7 +111,7 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
  * up the array's address (make it before any stream capture); calls share the array,
  * so calls whose device work overlaps race and must be serialised. */
 #define GCSL_NOALLOC_MAX_P 512
-#define GCSL_NOALLOC_SCRATCH_BYTES 3211264
+#define GCSL_NOALLOC_SCRATCH_BYTES 5775360
 int gcsl_gauss_skeleton_noalloc(const double *C, int32_t p, int64_t n_obs, const double *thresholds,
                                 int32_t n_thresholds, int32_t max_level, uint16_t *G, int32_t *sepsets,
                                 int32_t *rec_pool, int64_t rec_cap, double *pmax, gcsl_stats *stats, void *stream);

@@ -60,3 +60,31 @@ def test_workspace_queries(built_lib):
     assert b >= 1000 * 1000 * (4 + 8)
     assert L.gcsl_corr_workspace_bytes(10000, 1000) >= 1000 * 8
     assert L.gcsl_disc_workspace_bytes(200, 50000, 3, 5) >= 200 * 200 * (4 + 8)
+
+
+def header_define(name: str) -> int:
+    m = re.search(rf"#define\s+{name}\s+(\d+)", HEADER.read_text())
+    assert m, name
+    return int(m.group(1))
+
+
+def test_noalloc_scratch_holds_the_largest_problem(built_lib):
+    """The static scratch of gcsl_gauss_skeleton_noalloc must hold the workspace of
+    p = GCSL_NOALLOC_MAX_P (the query is host arithmetic only)."""
+    from gpucsl_gb300 import _lib
+
+    L = _lib.lib()
+    pmax = header_define("GCSL_NOALLOC_MAX_P")
+    need = L.gcsl_gauss_workspace_bytes(pmax, 64)
+    assert need <= header_define("GCSL_NOALLOC_SCRATCH_BYTES"), need
+
+
+def test_gauss_rejects_pair_index_overflow(built_lib):
+    from gpucsl_gb300 import _lib
+
+    L = _lib.lib()
+    p = header_define("GCSL_GAUSS_MAX_P") + 1
+    thr = (ct.c_double * 1)(0.1)
+    dummy = ct.c_void_p(16)  # never dereferenced: the size check comes first
+    rc = L.gcsl_gauss_skeleton(dummy, p, 100, thr, 1, 0, dummy, None, None, 0, dummy, None, dummy, 1 << 40, None)
+    assert rc == _lib.GCSL_ERR_UNSUPPORTED

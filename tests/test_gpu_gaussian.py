@@ -85,7 +85,7 @@ def test_correlation_kernel_matches_numpy(cuda):
     for (p, n, dt) in [(20, 1000, np.float64), (257, 3001, np.float64), (130, 777, np.float32), (1, 5, np.float64)]:
         w = gaussian_dag_data(p, n, 2, p + n)
         X = w.data.astype(dt)
-        C = engine.correlation(torch.from_numpy(X).cuda()).cpu().numpy()
+        C = engine.correlation(torch.from_numpy(X).cuda(), method="dfma").cpu().numpy()
         ref = np.corrcoef(X, rowvar=False) if p > 1 else np.array([[1.0]])
         assert np.allclose(C, np.atleast_2d(ref), rtol=0, atol=5e-14), float(np.abs(C - ref).max())
         assert (C <= 1).all() and (C >= -1).all()
