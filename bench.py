@@ -52,7 +52,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpucsl_gb300", choices=["gpucsl_gb300", "reference"])
-    ap.add_argument("--no-extras", action="store_true", help="skip the discrete and CPU-baseline legs")
+    ap.add_argument("--no-extras", action="store_true", help="skip the discrete, batched and CPU-baseline legs")
+    ap.add_argument("--batched-only", action="store_true", help="run only the batched-instances leg")
     return ap.parse_args()
 
 
@@ -209,6 +210,94 @@ def blas_threads() -> int:
     except Exception:
         pass
     return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------ batched leg
+BATCH_COUNT, BATCH_ALPHA, BATCH_L = 512, 0.01, 4
+
+
+def batched_leg(reps: int = 10) -> dict:
+    """512 uneven Gaussian instances (p ~ U{50..400}, n ~ U{500..20000}, degree ~ U[2, 4],
+    seeds 1000 + k, alpha 0.01, levels <= 4): batched tensor-core correlation + batched
+    level loop replayed as one CUDA graph, split precision (FP32 tests, FP64 re-test in
+    the guard band) and FP64; against the plain per-instance path on the same samples."""
+    import numpy as np
+    import torch
+
+    from gpucsl_gb300 import engine
+    from gpucsl_gb300.batch import GaussianBatch
+    from gpucsl_gb300.synthetic import batch_instance_sizes, gaussian_dag_data_device
+
+    sizes = batch_instance_sizes(BATCH_COUNT)
+    ps, ns = [s[0] for s in sizes], [s[1] for s in sizes]
+    Xs = [gaussian_dag_data_device(p, n, d, seed) for (p, n, d, seed) in sizes]
+    torch.cuda.synchronize()
+
+    def timed(fn, k):
+        ts = []
+        for _ in range(k):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        return ts
+
+    out = {"workload": f"gaussian_batch_{BATCH_COUNT}_p50-400_n500-20000_deg2-4_alpha{BATCH_ALPHA}_L{BATCH_L}",
+           "unit": "skeletons/s", "data": "synthetic (DAG from numpy seed 1000+k, noise from torch on the device)",
+           "sample_bytes": int(sum(p * n * 8 for p, n in zip(ps, ns)))}
+    results = {}
+    for prec in ("split", "f64"):
+        b = GaussianBatch(ps, ns, BATCH_ALPHA, BATCH_L, prec)
+        b.bind_samples(Xs)
+        res = b.run(graph=False)
+        lanes = b.autotune(reps=3)
+        b.capture()
+        for _ in range(2):
+            b.graph.replay()
+        ts = timed(b.graph.replay, reps)
+        res = b.collect()
+        tests = sum(r.tests for r in res)
+        results[prec] = [b.to_host(k) for k in range(BATCH_COUNT)]
+        out[prec] = {"value": round(BATCH_COUNT / statistics.median(ts), 2), "ms_per_batch":
+                     round(1e3 * statistics.median(ts), 3), "tests_per_batch": tests,
+                     "tests_per_s": round(tests / statistics.median(ts), 1),
+                     "retests": sum(r.retests for r in res), "lanes_per_level": lanes,
+                     "status_nonzero": sum(1 for r in res if r.status != 0)}
+        del b
+        torch.cuda.empty_cache()
+    # decisions and pmax of split against FP64
+    mism_g = mism_s = 0
+    max_abs = max_rel = 0.0
+    for (G1, S1, P1), (G2, S2, P2) in zip(results["split"], results["f64"]):
+        mism_g += int((G1 != G2).sum())
+        mism_s += int((S1 != S2).any(axis=2).sum())
+        iu = np.triu_indices(G1.shape[0], 1)
+        if iu[0].size:
+            d = np.abs(P1[iu] - P2[iu])
+            max_abs = max(max_abs, float(d.max()))
+            max_rel = max(max_rel, float((d / np.maximum(np.abs(P2[iu]), 1e-300)).max()))
+    out["split_vs_f64"] = {"skeleton_mismatches": mism_g, "sepset_mismatches": mism_s,
+                           "pmax_max_abs_err": max_abs, "pmax_max_rel_err": max_rel}
+    # plain per-instance path (single-problem API, no host sync inside the loop)
+    solvers = [engine.GaussianSolver(p, BATCH_L, record_cap=4 * p * p) for p in ps]  # no pool growth
+    Cs = [torch.empty((p, p), dtype=torch.float64, device="cuda") for p in ps]
+    corr_ws = torch.empty(max(int(engine._lib.lib().gcsl_corr_tc_workspace_bytes(n, p)) for p, n in zip(ps, ns)),
+                          dtype=torch.uint8, device="cuda")
+    thr = [engine.gaussian_thresholds(n, BATCH_ALPHA) for n in ns]
+
+    def plain():
+        for k in range(BATCH_COUNT):
+            engine.correlation(Xs[k], out=Cs[k], workspace=corr_ws)
+            solvers[k].run(Cs[k], ns[k], thr[k], sync=False)
+
+    plain()
+    tp = timed(plain, 3)
+    out["plain_f64"] = {"value": round(BATCH_COUNT / statistics.median(tp), 2),
+                        "ms_per_batch": round(1e3 * statistics.median(tp), 3)}
+    out["speedup_split_vs_plain"] = round(out["split"]["value"] / out["plain_f64"]["value"], 2)
+    return out
 
 
 # ------------------------------------------------------------------ our arm
@@ -391,6 +480,10 @@ def run_ours(args, world, rank, local):
                            "ms_per_solve": round(1e3 * statistics.mean(td), 3), "tests_per_solve": Ed,
                            "levels_run": std.raw["levels_run"]}
 
+    # ---- batched instances (split precision and FP64) against the plain per-instance path
+    if not args.no_extras and rank == 0:
+        out["batched"] = batched_leg()
+
     # ---- CPU baseline: the oracle on the host cores (rank 0, N = 1 only)
     if not args.no_extras and rank == 0 and world == 1:
         t0 = time.perf_counter()
@@ -448,6 +541,14 @@ def main():
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.batched_only:
+        import torch
+
+        from gpucsl_gb300 import build as gbuild
+
+        gbuild.build()
+        torch.cuda.set_device(local)
+        print(json.dumps({"batched": batched_leg()}), flush=True)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

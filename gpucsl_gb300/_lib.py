@@ -27,13 +27,20 @@ GCSL_DTYPE_F32 = 1
 
 # every symbol the header declares (checked by the CPU test-suite)
 EXPORTED = [
-    "gcsl_version", "gcsl_status_string", "gcsl_kernel_launches",
+    "gcsl_version", "gcsl_last_error", "gcsl_status_string", "gcsl_kernel_launches",
     "gcsl_corr_workspace_bytes", "gcsl_corr_f64", "gcsl_corr_tc_workspace_bytes", "gcsl_corr_f64_tc",
     "gcsl_corr_tc_digits", "gcsl_corr_tc_product",
     "gcsl_gauss_workspace_bytes", "gcsl_gauss_skeleton", "gcsl_gauss_skeleton_noalloc",
     "gcsl_disc_workspace_bytes", "gcsl_disc_skeleton",
     "gcsl_compact", "gcsl_unrank", "gcsl_pchisq", "gcsl_disc_table", "gcsl_tc_gemm_bf16",
+    "gcsl_gauss_batch_workspace_bytes", "gcsl_gauss_batch_prepare", "gcsl_gauss_batch_run",
+    "gcsl_gauss_batch_collect", "gcsl_gauss_batch_set_lanes",
+    "gcsl_corr_tc_batch_workspace_bytes", "gcsl_corr_tc_batch_prepare", "gcsl_corr_tc_batch_run",
 ]
+
+GCSL_PREC_F64 = 0
+GCSL_PREC_SPLIT = 1
+GCSL_BATCH_MAX_LEVEL = 12
 
 
 class GcslStats(ct.Structure):
@@ -64,10 +71,43 @@ class GcslStats(ct.Structure):
         }
 
 
+class GaussInstance(ct.Structure):
+    """gcsl_gauss_instance: one problem of a batch (device pointers, host thresholds)."""
+    _fields_ = [
+        ("C", ct.c_void_p),
+        ("C32", ct.c_void_p),
+        ("p", ct.c_int32),
+        ("n_obs", ct.c_int64),
+        ("thresholds", ct.POINTER(ct.c_double)),
+        ("n_thresholds", ct.c_int32),
+        ("band_lo", ct.POINTER(ct.c_double)),
+        ("band_hi", ct.POINTER(ct.c_double)),
+        ("G", ct.c_void_p),
+        ("pmax", ct.c_void_p),
+        ("rec_pool", ct.c_void_p),
+        ("rec_cap", ct.c_int64),
+        ("status", ct.c_int32),
+        ("levels_run", ct.c_int32),
+        ("n_records", ct.c_int64),
+        ("tests", ct.c_int64),
+        ("retests", ct.c_int64),
+    ]
+
+
+class BatchPlan(ct.Structure):
+    _fields_ = [("w", ct.c_int64 * 48)]
+
+
 class GcslError(RuntimeError):
     def __init__(self, code: int, what: str):
         self.code = code
-        super().__init__(f"{what}: {status_string(code)} (status {code})")
+        detail = ""
+        if code == GCSL_ERR_DEVICE:
+            try:
+                detail = lib().gcsl_last_error().decode()
+            except Exception:
+                detail = ""
+        super().__init__(f"{what}: {status_string(code)} (status {code})" + (f" [{detail}]" if detail else ""))
 
 
 _vp = ct.c_void_p
@@ -88,6 +128,8 @@ def lib() -> ct.CDLL:
     L.gcsl_version.argtypes = []
     L.gcsl_kernel_launches.restype = ct.c_int64
     L.gcsl_kernel_launches.argtypes = []
+    L.gcsl_last_error.restype = ct.c_char_p
+    L.gcsl_last_error.argtypes = []
     L.gcsl_status_string.restype = ct.c_char_p
     L.gcsl_status_string.argtypes = [ct.c_int]
     L.gcsl_corr_workspace_bytes.restype = _sz
@@ -125,6 +167,25 @@ def lib() -> ct.CDLL:
     L.gcsl_disc_table.argtypes = [_vp, _i64, _i64, _vp, _i32, _i32, ct.POINTER(_i32), _i32, _vp, _i64, _vp, _vp]
     L.gcsl_tc_gemm_bf16.restype = ct.c_int
     L.gcsl_tc_gemm_bf16.argtypes = [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp]
+    L.gcsl_gauss_batch_workspace_bytes.restype = _sz
+    L.gcsl_gauss_batch_workspace_bytes.argtypes = [ct.POINTER(_i32), _i32]
+    L.gcsl_gauss_batch_prepare.restype = ct.c_int
+    L.gcsl_gauss_batch_prepare.argtypes = [ct.POINTER(GaussInstance), _i32, _i32, _i32, _vp, _sz,
+                                           ct.POINTER(BatchPlan), _vp]
+    L.gcsl_gauss_batch_run.restype = ct.c_int
+    L.gcsl_gauss_batch_run.argtypes = [ct.POINTER(BatchPlan), _vp]
+    L.gcsl_gauss_batch_collect.restype = ct.c_int
+    L.gcsl_gauss_batch_collect.argtypes = [ct.POINTER(BatchPlan), ct.POINTER(GaussInstance), _i32, _vp]
+    L.gcsl_gauss_batch_set_lanes.restype = ct.c_int
+    L.gcsl_gauss_batch_set_lanes.argtypes = [ct.POINTER(BatchPlan), _i32, _i32]
+    L.gcsl_corr_tc_batch_workspace_bytes.restype = _sz
+    L.gcsl_corr_tc_batch_workspace_bytes.argtypes = [ct.POINTER(_i64), ct.POINTER(_i32), _i32]
+    L.gcsl_corr_tc_batch_prepare.restype = ct.c_int
+    L.gcsl_corr_tc_batch_prepare.argtypes = [ct.POINTER(_vp), _i32, ct.POINTER(_i64), ct.POINTER(_i32),
+                                             ct.POINTER(_i64), ct.POINTER(_vp), ct.POINTER(_vp), _i32, _vp, _sz,
+                                             ct.POINTER(BatchPlan), _vp]
+    L.gcsl_corr_tc_batch_run.restype = ct.c_int
+    L.gcsl_corr_tc_batch_run.argtypes = [ct.POINTER(BatchPlan), _vp]
     if L.gcsl_version() != 1:
         raise RuntimeError("libgpucsl_gb300.so ABI version mismatch")
     return L

@@ -7,6 +7,7 @@
 // host only checks the sticky `done` flag between batches; levels enqueued past the
 // end return at their first instruction.
 #include <algorithm>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -54,6 +55,17 @@ cudaError_t corr_tc(const void *X, int dtype, long long n, int p, long long ldx,
 cudaError_t corr_tc_digits(const void *X, int dtype, long long n, int p, long long ldx, void *ws, size_t ws_bytes,
                            int num_sms, cudaStream_t s);
 cudaError_t corr_tc_product(long long n, int p, double *C, void *ws, size_t ws_bytes, int num_sms, cudaStream_t s);
+size_t corr_tc_batch_workspace_bytes(const long long *n, const int *p, int count);
+cudaError_t corr_tc_batch_prepare(const void *const *X, const long long *n, const int *p, const long long *ldx,
+                                  double *const *C, float *const *C32, int count, void *ws, size_t ws_bytes,
+                                  long long *stage_totals, cudaStream_t s);
+cudaError_t corr_tc_batch_run(void *ws, int count, const long long *stage_totals, int dtype, cudaStream_t s);
+size_t gauss_batch_workspace_bytes(const int *p, int count);
+int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level, int precision, void *ws,
+                        size_t ws_bytes, long long *plan, int sms, cudaStream_t s);
+int gauss_batch_set_lanes(long long *plan, int level, int lanes);
+int gauss_batch_run(const long long *plan, cudaStream_t s);
+int gauss_batch_collect(const long long *plan, gcsl_gauss_instance *out, int count, cudaStream_t s);
 cudaError_t launch_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, float *D, int M, int N, int K, int *err,
                                 cudaStream_t s);
 }  // namespace host
@@ -64,6 +76,14 @@ using namespace gcsl;
 #include <atomic>
 static std::atomic<long long> g_kernel_launches{0};
 void gcsl::host::note_launch(int kernels) { g_kernel_launches.fetch_add(kernels, std::memory_order_relaxed); }
+
+static thread_local char g_last_error[256] = "";
+cudaError_t gcsl::host::note_error(const char *where, cudaError_t e) {
+    if (e != cudaSuccess)
+        std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s (%s)", where, cudaGetErrorName(e),
+                      cudaGetErrorString(e));
+    return e;
+}
 
 namespace {
 
@@ -90,7 +110,10 @@ int device_sms() {
     return sms > 0 ? sms : 1;
 }
 
-int map_cuda(cudaError_t e) { return e == cudaSuccess ? GCSL_OK : GCSL_ERR_DEVICE; }
+int map_cuda(cudaError_t e) {
+    if (e != cudaSuccess && g_last_error[0] == '\0') host::note_error("CUDA call", e);
+    return e == cudaSuccess ? GCSL_OK : GCSL_ERR_DEVICE;
+}
 
 // A second, lowest-priority stream per device for work that can overlap the level loop
 // (its blocks yield SMs to the latency-bound level kernels); created once per device,
@@ -280,6 +303,8 @@ extern "C" {
 int gcsl_version(void) { return GCSL_ABI_VERSION; }
 
 int64_t gcsl_kernel_launches(void) { return (int64_t)g_kernel_launches.load(std::memory_order_relaxed); }
+
+const char *gcsl_last_error(void) { return g_last_error; }
 
 const char *gcsl_status_string(int status) {
     switch (status) {
@@ -487,6 +512,102 @@ int gcsl_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, float *D, int32_t M,
         reinterpret_cast<uintptr_t>(A) % 16 || reinterpret_cast<uintptr_t>(B) % 16)
         return GCSL_ERR_INVALID_ARG;
     return map_cuda(host::launch_tc_gemm_bf16(A, B, D, M, N, K, err, static_cast<cudaStream_t>(stream)));
+}
+
+
+// ------------------------------------------------------------------ batches
+size_t gcsl_gauss_batch_workspace_bytes(const int32_t *p, int32_t count) {
+    if (!p || count < 1) return 0;
+    for (int k = 0; k < count; ++k)
+        if (p[k] < 1 || p[k] > GCSL_GAUSS_MAX_P) return 0;
+    return host::gauss_batch_workspace_bytes(p, count);
+}
+
+int gcsl_gauss_batch_prepare(const gcsl_gauss_instance *inst, int32_t count, int32_t max_level, int32_t precision,
+                             void *workspace, size_t workspace_bytes, gcsl_batch_plan *plan, void *stream) {
+    if (!inst || count < 1 || !plan || !workspace || max_level < 0 || max_level > GCSL_BATCH_MAX_LEVEL ||
+        (precision != GCSL_PREC_F64 && precision != GCSL_PREC_SPLIT))
+        return GCSL_ERR_INVALID_ARG;
+    for (int k = 0; k < count; ++k) {
+        const gcsl_gauss_instance &I = inst[k];
+        if (!I.C || !I.G || !I.pmax || I.p < 1 || I.n_obs < 4 || !I.thresholds || I.n_thresholds < 1)
+            return GCSL_ERR_INVALID_ARG;
+        if (I.p > GCSL_GAUSS_MAX_P) return GCSL_ERR_UNSUPPORTED;
+        if (precision == GCSL_PREC_SPLIT && (!I.C32 || !I.band_lo || !I.band_hi)) return GCSL_ERR_INVALID_ARG;
+    }
+    std::vector<int> ps((size_t)count);
+    for (int k = 0; k < count; ++k) ps[(size_t)k] = inst[k].p;
+    if (workspace_bytes < host::gauss_batch_workspace_bytes(ps.data(), count)) return GCSL_ERR_WORKSPACE;
+    return host::gauss_batch_prepare(inst, count, max_level, precision, workspace, workspace_bytes,
+                                     reinterpret_cast<long long *>(plan->w), device_sms(),
+                                     static_cast<cudaStream_t>(stream));
+}
+
+int gcsl_gauss_batch_run(const gcsl_batch_plan *plan, void *stream) {
+    if (!plan) return GCSL_ERR_INVALID_ARG;
+    return host::gauss_batch_run(reinterpret_cast<const long long *>(plan->w), static_cast<cudaStream_t>(stream));
+}
+
+int gcsl_gauss_batch_collect(const gcsl_batch_plan *plan, gcsl_gauss_instance *inst, int32_t count, void *stream) {
+    if (!plan || !inst) return GCSL_ERR_INVALID_ARG;
+    return host::gauss_batch_collect(reinterpret_cast<const long long *>(plan->w), inst, count,
+                                     static_cast<cudaStream_t>(stream));
+}
+
+int gcsl_gauss_batch_set_lanes(gcsl_batch_plan *plan, int32_t level, int32_t lanes) {
+    if (!plan) return GCSL_ERR_INVALID_ARG;
+    return host::gauss_batch_set_lanes(reinterpret_cast<long long *>(plan->w), level, lanes);
+}
+
+// plan words of a correlation batch: [magic, workspace, count, dtype, stage totals...]
+static const long long kCorrPlanMagic = 0x4743534c434f5252ll;  // "GCSLCORR"
+
+size_t gcsl_corr_tc_batch_workspace_bytes(const int64_t *n, const int32_t *p, int32_t count) {
+    if (!n || !p || count < 1) return 0;
+    std::vector<long long> nn((size_t)count);
+    std::vector<int> pp((size_t)count);
+    for (int k = 0; k < count; ++k) {
+        if (n[k] < 2 || p[k] < 1) return 0;
+        nn[(size_t)k] = n[k];
+        pp[(size_t)k] = p[k];
+    }
+    return host::corr_tc_batch_workspace_bytes(nn.data(), pp.data(), count);
+}
+
+int gcsl_corr_tc_batch_prepare(const void *const *X, int32_t dtype, const int64_t *n, const int32_t *p,
+                               const int64_t *ldx, double *const *C, float *const *C32, int32_t count,
+                               void *workspace, size_t workspace_bytes, gcsl_batch_plan *plan, void *stream) {
+    if (!X || !n || !p || !ldx || !C || count < 1 || !workspace || !plan ||
+        (dtype != GCSL_DTYPE_F64 && dtype != GCSL_DTYPE_F32))
+        return GCSL_ERR_INVALID_ARG;
+    std::vector<long long> nn((size_t)count), ll((size_t)count);
+    std::vector<int> pp((size_t)count);
+    for (int k = 0; k < count; ++k) {
+        if (!X[k] || !C[k] || n[k] < 2 || p[k] < 1 || ldx[k] < p[k]) return GCSL_ERR_INVALID_ARG;
+        nn[(size_t)k] = n[k];
+        pp[(size_t)k] = p[k];
+        ll[(size_t)k] = ldx[k];
+    }
+    if (workspace_bytes < host::corr_tc_batch_workspace_bytes(nn.data(), pp.data(), count)) return GCSL_ERR_WORKSPACE;
+    long long *w = reinterpret_cast<long long *>(plan->w);
+    std::memset(w, 0, sizeof(plan->w));
+    const cudaError_t e =
+        host::corr_tc_batch_prepare(X, nn.data(), pp.data(), ll.data(), C, C32, count, workspace, workspace_bytes,
+                                    w + 4, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return GCSL_ERR_DEVICE;
+    w[0] = kCorrPlanMagic;
+    w[1] = (long long)reinterpret_cast<uintptr_t>(workspace);
+    w[2] = count;
+    w[3] = dtype;
+    return GCSL_OK;
+}
+
+int gcsl_corr_tc_batch_run(const gcsl_batch_plan *plan, void *stream) {
+    if (!plan) return GCSL_ERR_INVALID_ARG;
+    const long long *w = reinterpret_cast<const long long *>(plan->w);
+    if (w[0] != kCorrPlanMagic) return GCSL_ERR_INVALID_ARG;
+    return map_cuda(host::corr_tc_batch_run(reinterpret_cast<void *>(static_cast<uintptr_t>(w[1])), (int)w[2], w + 4,
+                                            (int)w[3], static_cast<cudaStream_t>(stream)));
 }
 
 }  // extern "C"

@@ -19,6 +19,9 @@ namespace gcsl {
 namespace host {
 // Count of kernels this library has launched (process-wide, for instrumentation).
 void note_launch(int kernels);
+// Records the first failing CUDA call of the calling thread's current entry point (kept
+// for gcsl_last_error) and returns e.
+cudaError_t note_error(const char *where, cudaError_t e);
 }  // namespace host
 
 // Device-side state of one skeleton solve.  Per-level slots are written once per
@@ -34,6 +37,7 @@ struct DevState {
     unsigned long long tests_full[GCSL_MAX_LEVELS];
     unsigned long long removed[GCSL_MAX_LEVELS];
     unsigned long long n_rec_ints;           // ints used in the record pool
+    unsigned long long retests;              // FP64 re-tests of the split-precision path
 };
 
 // Arguments of one discrete test-kernel launch.

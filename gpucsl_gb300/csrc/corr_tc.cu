@@ -21,6 +21,8 @@
 // the rounding of an FP64 GEMM.  Tile: 128 rows (i) x 64 columns (j), 7 accumulators
 // = 448 TMEM columns, K staged 32 samples at a time into two shared-memory buffers
 // (84 KB each) while the tensor core consumes the other.
+#include <vector>
+
 #include "common.cuh"
 #include "tc.cuh"
 
@@ -28,7 +30,6 @@ namespace gcsl {
 
 constexpr int OZ_S = 7;                 // digits per value
 constexpr int OZ_G = 7;                 // accumulator groups g = k + l <= 6
-constexpr int OZ_PAIRS = 28;            // pairs with k + l <= 6
 constexpr int OZ_TM = 128, OZ_TN = 64;  // output tile
 constexpr int OZ_KS = 32;               // sample padding granule
 constexpr int OZ_CHUNK_STEPS = 28;      // 448 samples (28 MMA K steps) between exact drains
@@ -41,6 +42,46 @@ constexpr unsigned long long OZ_WAIT_NS = 2000000000ull;
 
 struct OzDims {
     int p, p_pad, n_pad, n_tiles_j, splits, slabs_per_split;  // slabs_per_split counts 16-sample K steps
+};
+
+// One correlation job: input samples, its dimensions and its slice of the workspace.
+struct OzJob {
+    const void *X;
+    long long n, ldx;
+    int p, chunks, tiles, pad;
+    OzDims D;
+    double *partial, *mean, *inv_sd;
+    long long *kmin, *kmax;
+    int *expo, *err;
+    uint8_t *dig;
+    long long *phi, *plo;
+    double *C;
+    float *C32;  // optional FP32 copy of C
+};
+
+// Kernel stages of a job; each has its own count of blocks per job.
+enum OzStage { OZ_INIT = 0, OZ_STATS, OZ_MEAN, OZ_DIGITS, OZ_PRODUCT, OZ_DIAG, OZ_FINISH, OZ_NSTAGES };
+constexpr int OZ_FINISH_ENTRIES = 4096;  // entries of C per finish block
+
+// Where a kernel finds its job: one job passed by value (block b of the stage is block b
+// of the job), or a device table of jobs with each stage's exclusive block offsets
+// (block b belongs to the job k with off[k] <= b < off[k + 1]).
+struct OneJob {
+    OzJob job;
+    __device__ __forceinline__ OzJob get(long long b, long long &lb) const {
+        lb = b;
+        return job;
+    }
+};
+struct JobTable {
+    const OzJob *jobs;
+    const long long *off;
+    int count;
+    __device__ __forceinline__ OzJob get(long long b, long long &lb) const {
+        const int k = upper_row(off, count, b);
+        lb = b - off[k];
+        return jobs[k];
+    }
 };
 
 // ------------------------------------------------------------ preparation
@@ -56,25 +97,37 @@ __device__ __forceinline__ double key_value(long long k) {
 
 constexpr int OZ_STAT_ROWS = 512;  // samples per column-statistics block
 
-__global__ void colstats_init_kernel(int p, long long *__restrict__ kmin, long long *__restrict__ kmax) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < p) {
-        kmin[j] = 0x7fffffffffffffffll;
-        kmax[j] = (long long)0x8000000000000000ull;
+template <class Src>
+__global__ void colstats_init_kernel(Src src) {
+    long long lb;
+    const OzJob &J = src.get(blockIdx.x, lb);
+    const int j = (int)lb * blockDim.x + threadIdx.x;
+    if (j < J.p) {
+        J.kmin[j] = 0x7fffffffffffffffll;
+        J.kmax[j] = (long long)0x8000000000000000ull;
+        if (j == 0) *J.err = 0;
     }
 }
 
 // One read of X: per (512-sample chunk, column) FP64 partial sum in a fixed order, and
 // column min / max through ordered-key atomics.
-template <typename T>
-__global__ void colstats_kernel(const T *__restrict__ X, long long n, int p, long long ldx,
-                                double *__restrict__ partial, long long *__restrict__ kmin,
-                                long long *__restrict__ kmax) {
+template <typename T, class Src>
+__global__ void colstats_kernel(Src src) {
     __shared__ double ssum[8][32];
     __shared__ long long smin[8][32], smax[8][32];
+    long long lb;
+    const OzJob &Jb = src.get(blockIdx.x, lb);
+    const T *__restrict__ X = static_cast<const T *>(Jb.X);
+    const long long n = Jb.n, ldx = Jb.ldx;
+    const int p = Jb.p;
+    double *__restrict__ partial = Jb.partial;
+    long long *__restrict__ kmin = Jb.kmin;
+    long long *__restrict__ kmax = Jb.kmax;
+    const int nbx = (p + 31) / 32;
+    const int bx = (int)(lb % nbx), by = (int)(lb / nbx);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int j = blockIdx.x * 32 + lane;
-    const long long t0 = (long long)blockIdx.y * OZ_STAT_ROWS, t1 = min(n, t0 + OZ_STAT_ROWS);
+    const int j = bx * 32 + lane;
+    const long long t0 = (long long)by * OZ_STAT_ROWS, t1 = min(n, t0 + OZ_STAT_ROWS);
     double sum = 0.0;
     long long mn = 0x7fffffffffffffffll, mx = (long long)0x8000000000000000ull;
     if (j < p) {
@@ -96,7 +149,7 @@ __global__ void colstats_kernel(const T *__restrict__ X, long long n, int p, lon
             mn = smin[q][lane] < mn ? smin[q][lane] : mn;
             mx = smax[q][lane] > mx ? smax[q][lane] : mx;
         }
-        partial[(size_t)blockIdx.y * p + j] = sum;
+        partial[(size_t)by * p + j] = sum;
         atomicMin(&kmin[j], mn);
         atomicMax(&kmax[j], mx);
     }
@@ -104,19 +157,21 @@ __global__ void colstats_kernel(const T *__restrict__ X, long long n, int p, lon
 
 // mean = (chunk sums in order) / n; E = exponent of max |fl(x - mean)| =
 // max(fl(max - mean), fl(mean - min)) (rounding is monotone), so |x - mean| < 2^E.
-__global__ void col_mean_exp_kernel(const double *__restrict__ partial, long long n, int p, int chunks,
-                                    const long long *__restrict__ kmin, const long long *__restrict__ kmax,
-                                    double *__restrict__ mean, int *__restrict__ expo) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+template <class Src>
+__global__ void col_mean_exp_kernel(Src src) {
+    long long lb;
+    const OzJob &J = src.get(blockIdx.x, lb);
+    const int p = J.p;
+    const int j = (int)lb * blockDim.x + threadIdx.x;
     if (j >= p) return;
     double s = 0.0;
-    for (int c = 0; c < chunks; ++c) s += partial[(size_t)c * p + j];
-    const double mu = s / (double)n;
-    mean[j] = mu;
-    const double dev = fmax(key_value(kmax[j]) - mu, mu - key_value(kmin[j]));
+    for (int c = 0; c < J.chunks; ++c) s += J.partial[(size_t)c * p + j];
+    const double mu = s / (double)J.n;
+    J.mean[j] = mu;
+    const double dev = fmax(key_value(J.kmax[j]) - mu, mu - key_value(J.kmin[j]));
     int e = 0;
     if (dev > 0.0) frexp(dev, &e);
-    expo[j] = e;
+    J.expo[j] = e;
 }
 
 // Digits of X_c in the tensor-core tile layout: for digit k, 128-row block I and
@@ -124,13 +179,21 @@ __global__ void col_mean_exp_kernel(const double *__restrict__ partial, long lon
 // (byte ((k * nI + I) * nq + q) * 4096 + kmajor_offset(row % 128, sample % 16)), zero
 // padded to (p_pad, n_pad).  A 64-row operand tile is the first or second 2 KB half of a
 // block.  One CTA handles 32 samples x 32 columns.
-template <typename T>
-__global__ void digit_split_kernel(const T *__restrict__ X, long long n, int p, long long ldx,
-                                   const double *__restrict__ mean, const int *__restrict__ expo, int p_pad,
-                                   long long n_pad, uint8_t *__restrict__ dig) {
+template <typename T, class Src>
+__global__ void digit_split_kernel(Src src) {
     __shared__ int16_t tile[OZ_S][32][33];  // [digit][sample][column]
-    const long long t0 = (long long)blockIdx.x * 32;
-    const int j0 = blockIdx.y * 32;
+    long long lb;
+    const OzJob &Jb = src.get(blockIdx.x, lb);
+    const T *__restrict__ X = static_cast<const T *>(Jb.X);
+    const long long n = Jb.n, ldx = Jb.ldx;
+    const int p = Jb.p, p_pad = Jb.D.p_pad;
+    const long long n_pad = Jb.D.n_pad;
+    const double *__restrict__ mean = Jb.mean;
+    const int *__restrict__ expo = Jb.expo;
+    uint8_t *__restrict__ dig = Jb.dig;
+    const long long nbx = n_pad / 32;
+    const long long t0 = (lb % nbx) * 32;
+    const int j0 = (int)(lb / nbx) * 32;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 warps
     for (int r = ty; r < 32; r += 8) {
         const long long t = t0 + r;
@@ -250,17 +313,28 @@ constexpr int OZ_THREADS = (OZ_DRAIN_WARPS + 2) * 32;    // + producer warp + MM
 // copies; warp 17 (lane 0) issues the tensor-core MMAs.  They synchronise only through
 // mbarriers: full (copy landed), empty (MMAs done reading a stage), chunk (MMAs of a
 // chunk done), drained (TMEM read, accumulators may be overwritten).
-__global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(const uint8_t *__restrict__ dig, OzDims D,
-                                                                  long long *__restrict__ part_hi,
-                                                                  long long *__restrict__ part_lo, int *err) {
+template <class Src>
+__global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t full_bar[OZ_NST], empty_bar[OZ_NST], chunk_bar, drained_bar;
     __shared__ uint32_t tmem_slot;
     __shared__ int s_fail;
+    // the job lives in shared memory: each role reads its fields where it uses them, so
+    // they hold no registers across the drain loop
+    __shared__ OzJob s_job;
+    __shared__ long long s_lb;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        long long lb0;
+        s_job = src.get(blockIdx.x, lb0);
+        s_lb = lb0;
+    }
+    __syncthreads();
+    const long long lb = s_lb;
+    const OzDims &D = s_job.D;
     int I, J;
-    oz_tile_of(blockIdx.x, D.n_tiles_j, I, J);
-    const int split = blockIdx.y;
+    oz_tile_of((int)(lb % s_job.tiles), D.n_tiles_j, I, J);
+    const int split = (int)(lb / s_job.tiles);
     const int nI = D.p_pad / OZ_TM;
     const long long nq = D.n_pad / 16;
     const long long q0 = (long long)split * D.slabs_per_split;
@@ -297,10 +371,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(const uint8_t
                 mbar_expect_tx(&full_bar[b], (uint32_t)OZ_STAGE_BYTES);
                 const long long q = q0 + st;
                 for (int k = 0; k < OZ_S; ++k) {
-                    bulk_g2s(sA + k * 4096, dig + (((size_t)k * nI + I) * nq + q) * 4096, 4096u, &full_bar[b]);
-                    bulk_g2s(sB + k * 2048,
-                             dig + (((size_t)k * nI + (J >> 1)) * nq + q) * 4096 + (size_t)(J & 1) * 2048, 2048u,
+                    bulk_g2s(sA + k * 4096, s_job.dig + (((size_t)k * nI + I) * nq + q) * 4096, 4096u,
                              &full_bar[b]);
+                    bulk_g2s(sB + k * 2048,
+                             s_job.dig + (((size_t)k * nI + (J >> 1)) * nq + q) * 4096 + (size_t)(J & 1) * 2048,
+                             2048u, &full_bar[b]);
                 }
             }
         }
@@ -386,6 +461,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(const uint8_t
             const int row = qd * 32 + lane;
             const size_t base = ((size_t)split * D.p_pad + (size_t)(I * OZ_TM + row)) * D.p_pad + J * OZ_TN + cq * 16;
 #pragma unroll
+            long long *__restrict__ part_hi = s_job.phi;
+            long long *__restrict__ part_lo = s_job.plo;
             for (int e = 0; e < 16; ++e) {
                 part_hi[base + e] = acc_hi[e];
                 part_lo[base + e] = acc_lo[e];
@@ -394,7 +471,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(const uint8_t
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (tid == 0 && s_fail) atomicExch(err, 1);
+    if (tid == 0 && s_fail) atomicExch(s_job.err, 1);
     if (warp == 0) tc::tmem_dealloc(tmem, OZ_TMEM_COLS);
 }
 
@@ -413,35 +490,48 @@ __device__ __forceinline__ double oz_cov(const long long *__restrict__ part_hi, 
     return (val * pow2(expo[i] + expo[j] - 56)) * scale;
 }
 
-__global__ void ozaki_diag_kernel(const long long *__restrict__ part_hi, const long long *__restrict__ part_lo,
-                                  OzDims D, const int *__restrict__ expo, double scale, double *__restrict__ inv_sd) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < D.p) inv_sd[i] = 1.0 / sqrt(oz_cov(part_hi, part_lo, D, expo, scale, i, i));
+template <class Src>
+__global__ void ozaki_diag_kernel(Src src) {
+    long long lb;
+    const OzJob &J = src.get(blockIdx.x, lb);
+    const int i = (int)lb * blockDim.x + threadIdx.x;
+    const double scale = 1.0 / (double)(J.n - 1);
+    if (i < J.p) J.inv_sd[i] = 1.0 / sqrt(oz_cov(J.phi, J.plo, J.D, J.expo, scale, i, i));
 }
 
 // C_ij = clip(cov_ij / s_i / s_j, -1, 1) for i <= j, written to both triangles (the
 // normalisation of numpy's corrcoef, with reciprocals of the standard deviations).
-__global__ void ozaki_finish_kernel(const long long *__restrict__ part_hi, const long long *__restrict__ part_lo,
-                                    OzDims D, const int *__restrict__ expo, double scale,
-                                    const double *__restrict__ inv_sd, const int *__restrict__ err,
-                                    double *__restrict__ C) {
-    const long long total = (long long)D.p * D.p;
-    const bool failed = *err != 0;  // a tensor-core wait timed out: poison the output
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
-         k += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(k / D.p), j = (int)(k - (long long)i * D.p);
+// C_ij = clip(cov_ij / s_i / s_j, -1, 1) for i <= j, written to both triangles (the
+// normalisation of numpy's corrcoef, with reciprocals of the standard deviations), and
+// to the FP32 copy when the job has one.  A block covers OZ_FINISH_ENTRIES entries.
+template <class Src>
+__global__ void ozaki_finish_kernel(Src src) {
+    long long lb;
+    const OzJob &J = src.get(blockIdx.x, lb);
+    const int p = J.p;
+    const long long total = (long long)p * p;
+    const double scale = 1.0 / (double)(J.n - 1);
+    const bool failed = *J.err != 0;  // a tensor-core wait timed out: poison the output
+    const long long k0 = lb * OZ_FINISH_ENTRIES, k1 = min(total, k0 + OZ_FINISH_ENTRIES);
+    for (long long k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const int i = (int)(k / p), j = (int)(k - (long long)i * p);
         if (i > j) continue;
-        double v = oz_cov(part_hi, part_lo, D, expo, scale, i, j) * inv_sd[i] * inv_sd[j];
+        double v = oz_cov(J.phi, J.plo, J.D, J.expo, scale, i, j) * J.inv_sd[i] * J.inv_sd[j];
         v = fmin(fmax(v, -1.0), 1.0);
         if (failed) v = __longlong_as_double(0x7ff8000000000000ll);
-        C[(size_t)i * D.p + j] = v;
-        C[(size_t)j * D.p + i] = v;
+        J.C[(size_t)i * p + j] = v;
+        J.C[(size_t)j * p + i] = v;
+        if (J.C32 != nullptr) {
+            J.C32[(size_t)i * p + j] = (float)v;
+            J.C32[(size_t)j * p + i] = (float)v;
+        }
     }
 }
 
 namespace host {
 
-static OzDims oz_dims(long long n, int p, int num_sms) {
+// splits: K splits of the tile grid; 0 chooses one wave over num_sms SMs
+static OzDims oz_dims(long long n, int p, int num_sms, int splits_req = 0) {
     OzDims D;
     D.p = p;
     D.p_pad = (p + OZ_TM - 1) / OZ_TM * OZ_TM;
@@ -451,7 +541,7 @@ static OzDims oz_dims(long long n, int p, int num_sms) {
     int tiles = 0;
     for (int i = 0; i < n_tiles_i; ++i) tiles += D.n_tiles_j - 2 * i;
     const long long steps = D.n_pad / 16;
-    int splits = num_sms / tiles;  // one wave: tiles x splits <= SMs (one CTA per SM holds all TMEM)
+    int splits = splits_req > 0 ? splits_req : num_sms / tiles;  // one wave: tiles x splits <= SMs
     if (splits < 1) splits = 1;
     if (splits > steps) splits = (int)steps;
     D.slabs_per_split = (int)((steps + splits - 1) / splits);
@@ -465,17 +555,18 @@ static int oz_tiles(const OzDims &D) {
     return tiles;
 }
 
-struct OzWs {
-    double *partial, *mean, *inv_sd;
-    long long *kmin, *kmax;
-    int *expo, *err;
-    uint8_t *dig;
-    long long *phi, *plo;
-    size_t bytes;
-};
-
-static OzWs oz_carve(void *ws, long long n, int p, const OzDims &D) {
-    const long long chunks = (n + OZ_STAT_ROWS - 1) / OZ_STAT_ROWS;
+// Carve one job's workspace; with ws == nullptr only the size is computed.
+static size_t oz_job(OzJob &J, void *ws, const void *X, long long n, int p, long long ldx, int num_sms,
+                     int splits_req) {
+    J.X = X;
+    J.n = n;
+    J.ldx = ldx;
+    J.p = p;
+    J.chunks = (int)((n + OZ_STAT_ROWS - 1) / OZ_STAT_ROWS);
+    J.D = oz_dims(n, p, num_sms, splits_req);
+    J.tiles = oz_tiles(J.D);
+    J.pad = 0;
+    const OzDims &D = J.D;
     char *w = static_cast<char *>(ws);
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -483,79 +574,101 @@ static OzWs oz_carve(void *ws, long long n, int p, const OzDims &D) {
         off += (bytes + 255) / 256 * 256;
         return r;
     };
-    OzWs o;
-    o.partial = reinterpret_cast<double *>(take((size_t)(chunks * p) * sizeof(double)));
-    o.mean = reinterpret_cast<double *>(take((size_t)p * sizeof(double)));
-    o.inv_sd = reinterpret_cast<double *>(take((size_t)p * sizeof(double)));
-    o.kmin = reinterpret_cast<long long *>(take((size_t)p * sizeof(long long)));
-    o.kmax = reinterpret_cast<long long *>(take((size_t)p * sizeof(long long)));
-    o.expo = reinterpret_cast<int *>(take((size_t)p * sizeof(int)));
-    o.err = reinterpret_cast<int *>(take(sizeof(int)));
-    o.dig = reinterpret_cast<uint8_t *>(take((size_t)OZ_S * D.p_pad * (size_t)D.n_pad * sizeof(uint16_t)));
-    o.phi = reinterpret_cast<long long *>(take((size_t)D.splits * D.p_pad * (size_t)D.p_pad * sizeof(long long) * 2));
-    o.plo = o.phi ? o.phi + (size_t)D.splits * D.p_pad * (size_t)D.p_pad : nullptr;
-    o.bytes = off;
-    return o;
+    J.partial = reinterpret_cast<double *>(take((size_t)J.chunks * p * sizeof(double)));
+    J.mean = reinterpret_cast<double *>(take((size_t)p * sizeof(double)));
+    J.inv_sd = reinterpret_cast<double *>(take((size_t)p * sizeof(double)));
+    J.kmin = reinterpret_cast<long long *>(take((size_t)p * sizeof(long long)));
+    J.kmax = reinterpret_cast<long long *>(take((size_t)p * sizeof(long long)));
+    J.expo = reinterpret_cast<int *>(take((size_t)p * sizeof(int)));
+    J.err = reinterpret_cast<int *>(take(sizeof(int)));
+    J.dig = reinterpret_cast<uint8_t *>(take((size_t)OZ_S * D.p_pad * (size_t)D.n_pad * sizeof(uint16_t)));
+    J.phi = reinterpret_cast<long long *>(take((size_t)D.splits * D.p_pad * (size_t)D.p_pad * sizeof(long long) * 2));
+    J.plo = J.phi ? J.phi + (size_t)D.splits * D.p_pad * (size_t)D.p_pad : nullptr;
+    J.C = nullptr;
+    J.C32 = nullptr;
+    return off;
+}
+
+// Blocks of each stage for one job (launch geometry of the kernels above).
+static void oz_stage_blocks(const OzJob &J, long long *nb) {
+    nb[OZ_INIT] = (J.p + 255) / 256;
+    nb[OZ_STATS] = (long long)((J.p + 31) / 32) * J.chunks;
+    nb[OZ_MEAN] = (J.p + 255) / 256;
+    nb[OZ_DIGITS] = (long long)(J.D.n_pad / 32) * (J.D.p_pad / 32);
+    nb[OZ_PRODUCT] = (long long)J.tiles * J.D.splits;
+    nb[OZ_DIAG] = (J.p + 255) / 256;
+    nb[OZ_FINISH] = ((long long)J.p * J.p + OZ_FINISH_ENTRIES - 1) / OZ_FINISH_ENTRIES;
 }
 
 size_t corr_tc_workspace_bytes(long long n, int p, int num_sms) {
-    const OzDims D = oz_dims(n, p, num_sms);
-    return oz_carve(nullptr, n, p, D).bytes;
+    OzJob J;
+    return oz_job(J, nullptr, nullptr, n, p, p, num_sms, 0);
+}
+
+template <class Src>
+static cudaError_t set_ozaki_smem() {
+    static bool done = false;  // per instantiation
+    if (done) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(corr_ozaki_kernel<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               OZ_NST * OZ_STAGE_BYTES);
+    done = e == cudaSuccess;
+    return e;
+}
+
+// Stage launches shared by the single-job and batched paths; nb[] = blocks per stage.
+template <class Src>
+static cudaError_t launch_digits(const Src &src, const long long *nb, int dtype, cudaStream_t s) {
+    note_launch(4);
+    colstats_init_kernel<Src><<<(unsigned)nb[OZ_INIT], 256, 0, s>>>(src);
+    cudaError_t e = note_error("colstats_init_kernel launch", cudaGetLastError());
+    if (e != cudaSuccess) return e;
+    if (dtype == GCSL_DTYPE_F64) colstats_kernel<double, Src><<<(unsigned)nb[OZ_STATS], 256, 0, s>>>(src);
+    else colstats_kernel<float, Src><<<(unsigned)nb[OZ_STATS], 256, 0, s>>>(src);
+    if ((e = note_error("colstats_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    col_mean_exp_kernel<Src><<<(unsigned)nb[OZ_MEAN], 256, 0, s>>>(src);
+    if ((e = note_error("col_mean_exp_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    if (dtype == GCSL_DTYPE_F64) digit_split_kernel<double, Src><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(src);
+    else digit_split_kernel<float, Src><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(src);
+    return note_error("digit_split_kernel launch", cudaGetLastError());
+}
+
+template <class Src>
+static cudaError_t launch_product(const Src &src, const long long *nb, cudaStream_t s) {
+    note_launch(3);
+    cudaError_t e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<Src>());
+    if (e != cudaSuccess) return e;
+    corr_ozaki_kernel<Src><<<(unsigned)nb[OZ_PRODUCT], OZ_THREADS, OZ_NST * OZ_STAGE_BYTES, s>>>(src);
+    if ((e = note_error("corr_ozaki_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    ozaki_diag_kernel<Src><<<(unsigned)nb[OZ_DIAG], 256, 0, s>>>(src);
+    if ((e = note_error("ozaki_diag_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    ozaki_finish_kernel<Src><<<(unsigned)nb[OZ_FINISH], 256, 0, s>>>(src);
+    return note_error("ozaki_finish_kernel launch", cudaGetLastError());
+}
+
+static bool one_job(OneJob &o, long long *nb, const void *X, long long n, int p, long long ldx, double *C, void *ws,
+                    size_t ws_bytes, int num_sms) {
+    const size_t need = oz_job(o.job, ws, X, n, p, ldx, num_sms, 0);
+    if (ws_bytes < need) return false;
+    o.job.C = C;
+    oz_stage_blocks(o.job, nb);
+    return true;
 }
 
 // Stage 1: column statistics, exponents and the digit tiles (FP64 / integer work).
 cudaError_t corr_tc_digits(const void *X, int dtype, long long n, int p, long long ldx, void *ws, size_t ws_bytes,
                            int num_sms, cudaStream_t s) {
-    const OzDims D = oz_dims(n, p, num_sms);
-    const OzWs o = oz_carve(ws, n, p, D);
-    if (ws_bytes < o.bytes) return cudaErrorInvalidValue;
-    const long long chunks = (n + OZ_STAT_ROWS - 1) / OZ_STAT_ROWS;
-    cudaError_t e = cudaMemsetAsync(o.err, 0, sizeof(int), s);
-    if (e != cudaSuccess) return e;
-    colstats_init_kernel<<<(p + 255) / 256, 256, 0, s>>>(p, o.kmin, o.kmax);
-    note_launch(1);
-    const dim3 gs((p + 31) / 32, (unsigned)chunks);
-    const dim3 gd((unsigned)(D.n_pad / 32), (unsigned)(D.p_pad / 32));
-    if (dtype == GCSL_DTYPE_F64)
-        colstats_kernel<double><<<gs, 256, 0, s>>>(static_cast<const double *>(X), n, p, ldx, o.partial, o.kmin,
-                                                   o.kmax);
-    else
-        colstats_kernel<float><<<gs, 256, 0, s>>>(static_cast<const float *>(X), n, p, ldx, o.partial, o.kmin,
-                                                  o.kmax);
-    note_launch(1);
-    col_mean_exp_kernel<<<(p + 255) / 256, 256, 0, s>>>(o.partial, n, p, (int)chunks, o.kmin, o.kmax, o.mean,
-                                                        o.expo);
-    note_launch(1);
-    if (dtype == GCSL_DTYPE_F64)
-        digit_split_kernel<double><<<gd, 256, 0, s>>>(static_cast<const double *>(X), n, p, ldx, o.mean, o.expo,
-                                                       D.p_pad, D.n_pad, o.dig);
-    else
-        digit_split_kernel<float><<<gd, 256, 0, s>>>(static_cast<const float *>(X), n, p, ldx, o.mean, o.expo,
-                                                      D.p_pad, D.n_pad, o.dig);
-    note_launch(1);
-    return cudaGetLastError();
+    OneJob o;
+    long long nb[OZ_NSTAGES];
+    if (!one_job(o, nb, X, n, p, ldx, nullptr, ws, ws_bytes, num_sms)) return cudaErrorInvalidValue;
+    return launch_digits(o, nb, dtype, s);
 }
 
 // Stage 2: exact digit products on the tensor cores, reduction, normalisation.
 cudaError_t corr_tc_product(long long n, int p, double *C, void *ws, size_t ws_bytes, int num_sms, cudaStream_t s) {
-    const OzDims D = oz_dims(n, p, num_sms);
-    const OzWs o = oz_carve(ws, n, p, D);
-    if (ws_bytes < o.bytes) return cudaErrorInvalidValue;
-    const int smem = OZ_NST * OZ_STAGE_BYTES;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(corr_ozaki_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        attr = true;
-    }
-    dim3 grid(oz_tiles(D), D.splits);
-    corr_ozaki_kernel<<<grid, OZ_THREADS, smem, s>>>(o.dig, D, o.phi, o.plo, o.err);
-    note_launch(1);
-    const double scale = 1.0 / (double)(n - 1);
-    ozaki_diag_kernel<<<(p + 255) / 256, 256, 0, s>>>(o.phi, o.plo, D, o.expo, scale, o.inv_sd);
-    note_launch(1);
-    ozaki_finish_kernel<<<num_sms * 4, 256, 0, s>>>(o.phi, o.plo, D, o.expo, scale, o.inv_sd, o.err, C);
-    note_launch(1);
-    return cudaGetLastError();
+    OneJob o;
+    long long nb[OZ_NSTAGES];
+    if (!one_job(o, nb, nullptr, n, p, p, C, ws, ws_bytes, num_sms)) return cudaErrorInvalidValue;
+    return launch_product(o, nb, s);
 }
 
 cudaError_t corr_tc(const void *X, int dtype, long long n, int p, long long ldx, double *C, void *ws, size_t ws_bytes,
@@ -564,6 +677,86 @@ cudaError_t corr_tc(const void *X, int dtype, long long n, int p, long long ldx,
     cudaError_t e = corr_tc_digits(X, dtype, n, p, ldx, ws, ws_bytes, num_sms, s);
     if (e != cudaSuccess) return e;
     return corr_tc_product(n, p, C, ws, ws_bytes, num_sms, s);
+}
+
+// ------------------------------------------------------------------ batches
+// Workspace: [job table | stage offsets (OZ_NSTAGES x (count + 1)) | job slices].  The
+// plan (host) keeps the block totals per stage so the run needs no device reads.
+static size_t batch_header_bytes(int count) {
+    const size_t a = ((size_t)count * sizeof(OzJob) + 255) / 256 * 256;
+    return a + ((size_t)OZ_NSTAGES * (count + 1) * sizeof(long long) + 255) / 256 * 256;
+}
+
+size_t corr_tc_batch_workspace_bytes(const long long *n, const int *p, int count) {
+    size_t total = batch_header_bytes(count);
+    for (int k = 0; k < count; ++k) {
+        OzJob J;
+        total += oz_job(J, nullptr, nullptr, n[k], p[k], p[k], 1, 1);
+    }
+    return total;
+}
+
+cudaError_t corr_tc_batch_prepare(const void *const *X, const long long *n, const int *p, const long long *ldx,
+                                  double *const *C, float *const *C32, int count, void *ws, size_t ws_bytes,
+                                  long long *stage_totals, cudaStream_t s) {
+    if (ws_bytes < corr_tc_batch_workspace_bytes(n, p, count)) return cudaErrorInvalidValue;
+    std::vector<OzJob> jobs((size_t)count);
+    std::vector<long long> off((size_t)OZ_NSTAGES * (count + 1), 0);
+    char *base = static_cast<char *>(ws);
+    size_t cur = batch_header_bytes(count);
+    for (int k = 0; k < count; ++k) {
+        OzJob &J = jobs[(size_t)k];
+        cur += oz_job(J, base + cur, X[k], n[k], p[k], ldx[k], 1, 1);
+        J.C = C[k];
+        J.C32 = C32 ? C32[k] : nullptr;
+        long long nb[OZ_NSTAGES];
+        oz_stage_blocks(J, nb);
+        for (int st = 0; st < OZ_NSTAGES; ++st)
+            off[(size_t)st * (count + 1) + k + 1] = off[(size_t)st * (count + 1) + k] + nb[st];
+    }
+    for (int st = 0; st < OZ_NSTAGES; ++st) stage_totals[st] = off[(size_t)st * (count + 1) + count];
+    const size_t a = ((size_t)count * sizeof(OzJob) + 255) / 256 * 256;
+    cudaError_t e = cudaMemcpyAsync(base, jobs.data(), (size_t)count * sizeof(OzJob), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(base + a, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host vectors die with this call
+    return e;
+}
+
+cudaError_t corr_tc_batch_run(void *ws, int count, const long long *stage_totals, int dtype, cudaStream_t s) {
+    char *base = static_cast<char *>(ws);
+    const size_t a = ((size_t)count * sizeof(OzJob) + 255) / 256 * 256;
+    const OzJob *jobs = reinterpret_cast<const OzJob *>(base);
+    const long long *off = reinterpret_cast<const long long *>(base + a);
+    long long nb[OZ_NSTAGES];
+    for (int st = 0; st < OZ_NSTAGES; ++st) {
+        nb[st] = stage_totals[st];
+        if (nb[st] <= 0 || nb[st] > 0x7fffffffll) return cudaErrorInvalidValue;
+    }
+    // one JobTable per stage (the offsets differ); the stage launchers take the table of
+    // their first kernel, so launch stage by stage
+    JobTable t[OZ_NSTAGES];
+    for (int st = 0; st < OZ_NSTAGES; ++st) t[st] = JobTable{jobs, off + (size_t)st * (count + 1), count};
+    note_launch(7);
+    cudaError_t e;
+    colstats_init_kernel<JobTable><<<(unsigned)nb[OZ_INIT], 256, 0, s>>>(t[OZ_INIT]);
+    if ((e = note_error("colstats_init_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    if (dtype == GCSL_DTYPE_F64) colstats_kernel<double, JobTable><<<(unsigned)nb[OZ_STATS], 256, 0, s>>>(t[OZ_STATS]);
+    else colstats_kernel<float, JobTable><<<(unsigned)nb[OZ_STATS], 256, 0, s>>>(t[OZ_STATS]);
+    if ((e = note_error("colstats_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    col_mean_exp_kernel<JobTable><<<(unsigned)nb[OZ_MEAN], 256, 0, s>>>(t[OZ_MEAN]);
+    if ((e = note_error("col_mean_exp_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    if (dtype == GCSL_DTYPE_F64)
+        digit_split_kernel<double, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
+    else digit_split_kernel<float, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
+    if ((e = note_error("digit_split_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    if ((e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<JobTable>())) != cudaSuccess) return e;
+    corr_ozaki_kernel<JobTable><<<(unsigned)nb[OZ_PRODUCT], OZ_THREADS, OZ_NST * OZ_STAGE_BYTES, s>>>(t[OZ_PRODUCT]);
+    if ((e = note_error("corr_ozaki_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    ozaki_diag_kernel<JobTable><<<(unsigned)nb[OZ_DIAG], 256, 0, s>>>(t[OZ_DIAG]);
+    if ((e = note_error("ozaki_diag_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    ozaki_finish_kernel<JobTable><<<(unsigned)nb[OZ_FINISH], 256, 0, s>>>(t[OZ_FINISH]);
+    return note_error("ozaki_finish_kernel launch", cudaGetLastError());
 }
 
 }  // namespace host

@@ -1,0 +1,533 @@
+// Batches of independent Gaussian skeletons: every kernel of the level loop runs once
+// for all instances of a batch, so a batch of hundreds of small problems costs a few
+// dozen launches instead of a few dozen per problem, and the whole sequence (no host
+// reads between levels) can be captured into one CUDA graph.
+//
+// Work is mapped to instances through exclusive offset arrays: level-0 tiles, rows and
+// p^2 chunks per instance are fixed by the sizes (computed on the host at prepare
+// time); the edges of a level are counted on the device and scanned between the
+// compaction and the test kernel.  Each instance keeps its own DevState, adjacency,
+// zmin / r2min and kept-pair list, exactly as a single solve does, so the results of
+// an instance do not depend on the rest of the batch.
+//
+// Precision GCSL_PREC_F64 runs the FP64 tests of the single-instance path.  Precision
+// GCSL_PREC_SPLIT first tests in FP32 on an FP32 copy of C and decides there when the
+// FP32 rho^2 is outside the guard band (tanh^2 of the thresholds at 1.1 alpha and
+// 0.9 alpha, i.e. the test's p-value is not within 10 % of alpha) and every pivot of the
+// elimination is at least 1e-3; otherwise the test is repeated in FP64 from C.  The
+// skeleton and sepsets then equal the FP64 ones; z* (and pmax) carry the FP32 error.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gauss_dev.cuh"
+
+namespace gcsl {
+
+constexpr int BATCH_MAX_LEVEL = GCSL_GAUSS_REG_LEVELS;
+constexpr int BATCH_P2_CHUNK = 4096;  // entries of a p x p array per init / pmax block
+constexpr float SPLIT_MIN_PIVOT = 1e-3f;
+
+struct BInst {
+    const double *C;
+    const float *C32;
+    uint16_t *G;
+    double *pmax;
+    int *rec;
+    long long rec_cap;
+    int *adj, *up, *kept;
+    long long *prefix;
+    double *zmin, *r2min;
+    DevState *st;
+    long long n_obs;
+    int p, n_thr;
+    double sqrt_nm3;
+    double tau[BATCH_MAX_LEVEL + 1], t2[BATCH_MAX_LEVEL + 1];
+    float t2lo[BATCH_MAX_LEVEL + 1], t2hi[BATCH_MAX_LEVEL + 1];
+};
+
+// ------------------------------------------------------------- FP32 test
+// The elimination of gauss_test_reg in FP32 on the FP32 copy of C.  Returns false when a
+// pivot (including the trailing H00, H11) is below SPLIT_MIN_PIVOT or the result is not
+// finite: the FP32 rho^2 is then not trusted.
+template <int L>
+__device__ __forceinline__ bool gauss_test_f32(const float *__restrict__ C32, int p, int vi, int vj, const int *S,
+                                               float &rho2) {
+    if constexpr (L == 1) {
+        const float m = __ldg(C32 + (size_t)S[0] * p + S[0]);
+        const float a = __ldg(C32 + (size_t)vi * p + S[0]);
+        const float b = __ldg(C32 + (size_t)vj * p + S[0]);
+        const float r = __ldg(C32 + (size_t)vi * p + vj);
+        const float d00 = fmaf(-a, a, m), d11 = fmaf(-b, b, m);
+        const float n01 = fmaf(r, m, -(a * b));
+        rho2 = (n01 * n01) / (d00 * d11);
+        const float lim = SPLIT_MIN_PIVOT * m;
+        return m >= SPLIT_MIN_PIVOT && d00 >= lim && d11 >= lim && rho2 < 0.99f;
+    }
+    constexpr int D = L + 2;
+    float A[D * (D + 1) / 2];
+#pragma unroll
+    for (int r = 0; r < L; ++r) {
+        const float *Cr = C32 + (size_t)S[r] * p;
+#pragma unroll
+        for (int c = 0; c <= r; ++c) A[r * (r + 1) / 2 + c] = __ldg(Cr + S[c]);
+        A[L * (L + 1) / 2 + r] = __ldg(C32 + (size_t)vi * p + S[r]);
+        A[(L + 1) * (L + 2) / 2 + r] = __ldg(C32 + (size_t)vj * p + S[r]);
+    }
+    A[L * (L + 1) / 2 + L] = 1.0f;
+    A[(L + 1) * (L + 2) / 2 + L] = __ldg(C32 + (size_t)vi * p + vj);
+    A[(L + 1) * (L + 2) / 2 + L + 1] = 1.0f;
+    float minpiv = 1.0f;
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+        const float piv = A[j * (j + 1) / 2 + j];
+        minpiv = fminf(minpiv, piv);
+        const float inv = 1.0f / piv;
+#pragma unroll
+        for (int i = j + 1; i < D; ++i) {
+            const float t = A[i * (i + 1) / 2 + j] * inv;
+#pragma unroll
+            for (int k = j + 1; k <= i; ++k) A[i * (i + 1) / 2 + k] = fmaf(-t, A[k * (k + 1) / 2 + j], A[i * (i + 1) / 2 + k]);
+        }
+    }
+    const float h00 = A[L * (L + 1) / 2 + L];
+    const float h01 = A[(L + 1) * (L + 2) / 2 + L];
+    const float h11 = A[(L + 1) * (L + 2) / 2 + L + 1];
+    minpiv = fminf(minpiv, fminf(h00, h11));
+    rho2 = (h01 * h01) / (h00 * h11);
+    return minpiv >= SPLIT_MIN_PIVOT && rho2 < 0.99f;  // NaN fails both
+}
+
+template <int L>
+struct SplitTest {
+    const double *__restrict__ C;
+    const float *__restrict__ C32;
+    int p;
+    double tau, t2;
+    float t2lo, t2hi;
+    unsigned long long *retests;
+    __device__ __forceinline__ TestOut operator()(int vi, int vj, const int *S) const {
+        float r2;
+        const bool ok = gauss_test_f32<L>(C32, p, vi, vj, S, r2);
+        if (ok && (r2 < t2lo || r2 > t2hi)) {
+            TestOut o;
+            o.rho2 = (double)r2;
+            o.zexact = __longlong_as_double(0x7ff0000000000000ll);
+            o.remove = r2 < t2lo;
+            return o;
+        }
+        ++*retests;
+        return gauss_test_reg<L>(C, p, vi, vj, S, tau, t2);
+    }
+};
+
+// ------------------------------------------------------------------ kernels
+// Instance of block b under exclusive offsets off[0..count].
+__device__ __forceinline__ int inst_of(const long long *__restrict__ off, int count, long long b, long long &lb) {
+    const int k = upper_row(off, count, b);
+    lb = b - off[k];
+    return k;
+}
+
+// Per p^2 chunk: r2min = 1.4e306 (above every stored rho^2); chunk 0 also clears the
+// instance's DevState.
+__global__ void batch_init_kernel(const BInst *__restrict__ inst, const long long *__restrict__ off_p2, int count) {
+    long long lb;
+    const BInst &I = inst[inst_of(off_p2, count, blockIdx.x, lb)];
+    const long long total = (long long)I.p * I.p;
+    const long long k0 = lb * BATCH_P2_CHUNK, k1 = min(total, k0 + BATCH_P2_CHUNK);
+    const double big = __longlong_as_double(0x7f7f7f7f7f7f7f7fll);
+    for (long long k = k0 + threadIdx.x; k < k1; k += blockDim.x) I.r2min[k] = big;
+    if (lb == 0) {
+        unsigned *w = reinterpret_cast<unsigned *>(I.st);
+        for (int k = threadIdx.x; k < (int)(sizeof(DevState) / sizeof(unsigned)); k += blockDim.x) w[k] = 0u;
+    }
+}
+
+__global__ void batch_level0_kernel(const BInst *__restrict__ inst, const long long *__restrict__ off_tiles,
+                                    int count) {
+    long long lb;
+    const BInst &I = inst[inst_of(off_tiles, count, blockIdx.x, lb)];
+    level0_tile(I.C, I.p, I.tau[0], I.t2[0], I.G, I.zmin, I.kept, I.st, (int)lb);
+}
+
+// Warp per (instance, row); level 1 compacts G, later levels refilter the lists.
+__global__ void batch_compact_kernel(const BInst *__restrict__ inst, const long long *__restrict__ off_rows,
+                                     int count, int level) {
+    const int lane = threadIdx.x & 31;
+    const long long rows = off_rows[count];
+    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < rows; g += warps) {
+        long long r;
+        const BInst &I = inst[inst_of(off_rows, count, g, r)];
+        if (I.st->done) continue;
+        const int deg = (level == 1) ? compact_row(I.G, I.p, I.adj, I.up, (int)r, lane)
+                                     : recompact_row(I.G, I.p, I.adj, I.up, (int)r, lane);
+        if (lane == 0) atomicMax(&I.st->max_degree[level], deg);
+    }
+}
+
+// Block per instance: decide whether the instance runs this level (the reference's stop
+// rule max degree - 1 < level, and the level cap), scan its rows into the edge prefix
+// and publish its edge count.
+__global__ void batch_scan_kernel(const BInst *__restrict__ inst, int count, int level, int max_level,
+                                  long long *__restrict__ edges) {
+    const BInst &I = inst[blockIdx.x];
+    DevState *st = I.st;
+    __shared__ int s_run;
+    if (threadIdx.x == 0) {
+        int run = !st->done;
+        if (run && st->max_degree[level] - 1 < level) run = 0;
+        if (run && level >= I.n_thr) {
+            set_status(st, GCSL_ERR_UNSUPPORTED_LEVEL);
+            run = 0;
+        }
+        if (run && level > max_level) run = 0;
+        if (!run) st->done = 1;
+        else st->last_level = level;
+        s_run = run;
+    }
+    __syncthreads();
+    if (!s_run) {
+        if (threadIdx.x == 0) edges[blockIdx.x] = 0;
+        return;
+    }
+    block_scan_rows(I.up, I.p, I.prefix);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        edges[blockIdx.x] = I.prefix[I.p];
+        st->edges[level] = (unsigned long long)I.prefix[I.p];
+    }
+}
+
+// One block: exclusive scan of the per-instance edge counts into off[0..count].
+__global__ void batch_edge_offsets_kernel(const long long *__restrict__ edges, int count, long long *__restrict__ off) {
+    block_scan_rows(edges, count, off);
+}
+
+template <int L, int G, bool SPLIT>
+__global__ void __launch_bounds__(256) batch_level_kernel(const BInst *__restrict__ inst,
+                                                         const long long *__restrict__ edge_off, int count) {
+    constexpr int GPW = 32 / G;
+    const int lane = threadIdx.x & 31, gl = lane & (G - 1), gw = lane / G;
+    const unsigned gshift = (unsigned)(gw * G);
+    const unsigned gbits = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
+    const long long n_edges = edge_off[count];
+    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    for (long long e0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * GPW; e0 < n_edges;
+         e0 += warps * GPW) {
+        const long long e = e0 + gw;
+        const bool has = e < n_edges;
+        long long le = 0;
+        const int k = has ? inst_of(edge_off, count, e, le) : 0;
+        const BInst &I = inst[k];
+        EdgeJob J;
+        J.T = 0;
+        if (has && !load_edge<L>(I.adj, I.up, I.prefix, I.p, le, L, J)) {
+            if (gl == 0) set_status(I.st, GCSL_ERR_UNSUPPORTED);
+            J.T = 0;
+        }
+        double r2min = inf, zmin_exact = inf;
+        bool removed = false;
+        unsigned long long n_tests = 0, retests = 0;
+        if constexpr (SPLIT) {
+            walk_edge<L, G>(J, has, I.adj, I.p, gl, gshift, gbits,
+                            SplitTest<L>{I.C, I.C32, I.p, I.tau[L], I.t2[L], I.t2lo[L], I.t2hi[L], &retests}, I.G,
+                            nullptr, BATCH_MAX_LEVEL, I.rec, I.rec_cap, I.st, r2min, zmin_exact, removed, n_tests);
+        } else {
+            walk_edge<L, G>(J, has, I.adj, I.p, gl, gshift, gbits, F64Test<L>{I.C, I.p, I.tau[L], I.t2[L]}, I.G,
+                            nullptr, BATCH_MAX_LEVEL, I.rec, I.rec_cap, I.st, r2min, zmin_exact, removed, n_tests);
+        }
+        if (SPLIT && retests) atomicAdd(&I.st->retests, retests);
+        if (has && gl == 0 && J.T > 0) {
+            const size_t ix = (size_t)J.lo * I.p + J.hi;
+            if (zmin_exact < inf) I.zmin[ix] = fmin(I.zmin[ix], zmin_exact);
+            if (r2min < inf) I.r2min[ix] = fmin(I.r2min[ix], r2min);
+            atomicAdd(&I.st->tests[L], n_tests);
+            atomicAdd(&I.st->tests_full[L], (unsigned long long)J.T);
+            if (removed) atomicAdd(&I.st->removed[L], 1ull);
+        }
+    }
+}
+
+// pmax of the pairs removed at level 0 and the -1 fill, per p^2 chunk.
+__global__ void batch_pmax_removed_kernel(const BInst *__restrict__ inst, const long long *__restrict__ off_p2,
+                                          int count) {
+    __shared__ double tab[SF_CENTRES][SF_TERMS];
+    sf_table_build(tab);
+    __syncthreads();
+    long long lb;
+    const BInst &I = inst[inst_of(off_p2, count, blockIdx.x, lb)];
+    const unsigned p = (unsigned)I.p;
+    const unsigned total = p * p;
+    const unsigned k0 = (unsigned)lb * BATCH_P2_CHUNK, k1 = min(total, k0 + (unsigned)BATCH_P2_CHUNK);
+    for (unsigned k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const unsigned i = k / p, j = k - i * p;
+        if (i >= j) I.pmax[k] = -1.0;
+        else if (I.zmin[k] < 0.0) I.pmax[k] = two_sf_tab(I.sqrt_nm3 * fisher_z(I.C[k]), tab);
+    }
+}
+
+// pmax of the pairs kept at level 0, block per instance.
+__global__ void batch_pmax_kept_kernel(const BInst *__restrict__ inst) {
+    __shared__ double tab[SF_CENTRES][SF_TERMS];
+    sf_table_build(tab);
+    __syncthreads();
+    const BInst &I = inst[blockIdx.x];
+    const int n = I.st->n_kept;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int k = I.kept[t];
+        double z = I.zmin[k];
+        const double r2 = I.r2min[k];
+        if (r2 < 1.0) z = fmin(z, fisher_z(sqrt(r2)));
+        I.pmax[k] = two_sf_tab(I.sqrt_nm3 * z, tab);
+    }
+}
+
+// ---------------------------------------------------------------------- host
+namespace host {
+
+namespace {
+
+struct BatchLayout {
+    size_t table, off_tiles, off_rows, off_p2, edges, edge_off, slices, total;
+};
+
+size_t al(size_t x) { return (x + 255) / 256 * 256; }
+
+size_t slice_bytes(int p) {
+    const size_t pp = (size_t)p * p;
+    return al(sizeof(DevState)) + al(pp * sizeof(int)) + al((size_t)p * sizeof(int)) +
+           al(((size_t)p + 1) * sizeof(long long)) + 2 * al(pp * sizeof(double)) +
+           al(((size_t)p * (p - 1) / 2 + 1) * sizeof(int));
+}
+
+BatchLayout layout(const int *p, int count) {
+    BatchLayout L;
+    size_t off = 0;
+    L.table = off;
+    off += al((size_t)count * sizeof(BInst));
+    L.off_tiles = off;
+    off += al(((size_t)count + 1) * sizeof(long long));
+    L.off_rows = off;
+    off += al(((size_t)count + 1) * sizeof(long long));
+    L.off_p2 = off;
+    off += al(((size_t)count + 1) * sizeof(long long));
+    L.edges = off;
+    off += al((size_t)count * sizeof(long long));
+    L.edge_off = off;
+    off += al(((size_t)count + 1) * sizeof(long long));
+    L.slices = off;
+    for (int k = 0; k < count; ++k) off += slice_bytes(p[k]);
+    L.total = off;
+    return L;
+}
+
+// plan words
+enum {
+    PW_MAGIC = 0, PW_WS, PW_COUNT, PW_MAXL, PW_PREC, PW_TILES, PW_ROWS, PW_P2, PW_SMS, PW_LANES  // PW_LANES + level
+};
+constexpr long long PLAN_MAGIC = 0x4743534c42415443ll;  // "GCSLBATC"
+
+template <int L, int G, bool SPLIT>
+void launch_level_t(const BInst *inst, const long long *eoff, int count, int sms, cudaStream_t s) {
+    const int threads = L >= 4 ? 128 : 256;
+    const int blocks = sms * (L >= 4 ? 12 : 8);
+    batch_level_kernel<L, G, SPLIT><<<blocks, threads, 0, s>>>(inst, eoff, count);
+}
+
+template <bool SPLIT>
+cudaError_t launch_level(int L, int lanes, const BInst *inst, const long long *eoff, int count, int sms,
+                         cudaStream_t s) {
+    const bool g8 = lanes == 8 && L <= 4;
+    switch (L) {
+#define GCSL_BL(K)                                                                 \
+    case K:                                                                        \
+        if (g8 && K <= 4) launch_level_t<K, (K <= 4 ? 8 : 32), SPLIT>(inst, eoff, count, sms, s); \
+        else launch_level_t<K, 32, SPLIT>(inst, eoff, count, sms, s);             \
+        break;
+        GCSL_BL(1) GCSL_BL(2) GCSL_BL(3) GCSL_BL(4) GCSL_BL(5) GCSL_BL(6)
+        GCSL_BL(7) GCSL_BL(8) GCSL_BL(9) GCSL_BL(10) GCSL_BL(11) GCSL_BL(12)
+#undef GCSL_BL
+    default:
+        return cudaErrorInvalidValue;
+    }
+    note_launch(1);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t gauss_batch_workspace_bytes(const int *p, int count) { return layout(p, count).total; }
+
+// Builds the instance table on the host and uploads it with the offset arrays
+// (synchronous: outside any stream capture).  thresholds / band arrays are host arrays.
+int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level, int precision, void *ws,
+                        size_t ws_bytes, long long *plan, int sms, cudaStream_t s) {
+    std::vector<int> ps((size_t)count);
+    for (int k = 0; k < count; ++k) ps[(size_t)k] = in[k].p;
+    const BatchLayout Ly = layout(ps.data(), count);
+    if (ws_bytes < Ly.total) return GCSL_ERR_WORKSPACE;
+    char *base = static_cast<char *>(ws);
+    std::vector<BInst> tab((size_t)count);
+    std::vector<long long> ot((size_t)count + 1, 0), orow((size_t)count + 1, 0), op2((size_t)count + 1, 0);
+    size_t cur = Ly.slices;
+    for (int k = 0; k < count; ++k) {
+        const gcsl_gauss_instance &X = in[k];
+        BInst &I = tab[(size_t)k];
+        std::memset(&I, 0, sizeof(I));
+        const int p = X.p;
+        const size_t pp = (size_t)p * p;
+        I.C = X.C;
+        I.C32 = X.C32;
+        I.G = X.G;
+        I.pmax = X.pmax;
+        I.rec = X.rec_pool;
+        I.rec_cap = X.rec_pool ? X.rec_cap : 0;
+        I.n_obs = X.n_obs;
+        I.p = p;
+        I.n_thr = X.n_thresholds;
+        I.sqrt_nm3 = std::sqrt((double)(X.n_obs - 3));
+        char *c = base + cur;
+        I.st = reinterpret_cast<DevState *>(c);
+        c += al(sizeof(DevState));
+        I.adj = reinterpret_cast<int *>(c);
+        c += al(pp * sizeof(int));
+        I.up = reinterpret_cast<int *>(c);
+        c += al((size_t)p * sizeof(int));
+        I.prefix = reinterpret_cast<long long *>(c);
+        c += al(((size_t)p + 1) * sizeof(long long));
+        I.zmin = reinterpret_cast<double *>(c);
+        c += al(pp * sizeof(double));
+        I.r2min = reinterpret_cast<double *>(c);
+        c += al(pp * sizeof(double));
+        I.kept = reinterpret_cast<int *>(c);
+        cur += slice_bytes(p);
+        for (int l = 0; l <= BATCH_MAX_LEVEL; ++l) {
+            const double tau = l < X.n_thresholds ? X.thresholds[l] : 0.0;
+            const double t = std::tanh(tau);
+            I.tau[l] = tau;
+            I.t2[l] = t * t;
+            if (precision == GCSL_PREC_SPLIT) {
+                const double lo = std::tanh(l < X.n_thresholds ? X.band_lo[l] : 0.0);
+                const double hi = std::tanh(l < X.n_thresholds ? X.band_hi[l] : 0.0);
+                // round outward so the FP32 comparisons never narrow the band
+                I.t2lo[l] = std::nextafter((float)(lo * lo), 0.0f);
+                I.t2hi[l] = std::nextafter((float)(hi * hi), 2.0f);
+            }
+        }
+        const long long nb = (p + 31) / 32;
+        ot[(size_t)k + 1] = ot[(size_t)k] + nb * (nb + 1) / 2;
+        orow[(size_t)k + 1] = orow[(size_t)k] + p;
+        op2[(size_t)k + 1] = op2[(size_t)k] + ((long long)pp + BATCH_P2_CHUNK - 1) / BATCH_P2_CHUNK;
+    }
+    if (ot[(size_t)count] > 0x7fffffffll || op2[(size_t)count] > 0x7fffffffll) return GCSL_ERR_UNSUPPORTED;
+    cudaError_t e = cudaMemcpyAsync(base + Ly.table, tab.data(), tab.size() * sizeof(BInst), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(base + Ly.off_tiles, ot.data(), ot.size() * sizeof(long long), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(base + Ly.off_rows, orow.data(), orow.size() * sizeof(long long), cudaMemcpyHostToDevice,
+                            s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(base + Ly.off_p2, op2.data(), op2.size() * sizeof(long long), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host vectors die with this call
+    if (e != cudaSuccess) return GCSL_ERR_DEVICE;
+    std::memset(plan, 0, sizeof(long long) * 48);
+    plan[PW_MAGIC] = PLAN_MAGIC;
+    plan[PW_WS] = (long long)reinterpret_cast<uintptr_t>(ws);
+    plan[PW_COUNT] = count;
+    plan[PW_MAXL] = max_level;
+    plan[PW_PREC] = precision;
+    plan[PW_TILES] = ot[(size_t)count];
+    plan[PW_ROWS] = orow[(size_t)count];
+    plan[PW_P2] = op2[(size_t)count];
+    plan[PW_SMS] = sms;
+    for (int l = 0; l <= BATCH_MAX_LEVEL; ++l) plan[PW_LANES + l] = 32;
+    return GCSL_OK;
+}
+
+bool gauss_batch_plan_ok(const long long *plan) { return plan && plan[PW_MAGIC] == PLAN_MAGIC; }
+
+int gauss_batch_set_lanes(long long *plan, int level, int lanes) {
+    if (!gauss_batch_plan_ok(plan) || level < 1 || level > BATCH_MAX_LEVEL || (lanes != 32 && lanes != 8))
+        return GCSL_ERR_INVALID_ARG;
+    plan[PW_LANES + level] = lanes;
+    return GCSL_OK;
+}
+
+// Enqueues the whole batch: init, level 0, levels 1..max_level, pmax.  No host reads:
+// the sequence can be captured into a CUDA graph.
+int gauss_batch_run(const long long *plan, cudaStream_t s) {
+    if (!gauss_batch_plan_ok(plan)) return GCSL_ERR_INVALID_ARG;
+    char *base = reinterpret_cast<char *>(static_cast<uintptr_t>(plan[PW_WS]));
+    const int count = (int)plan[PW_COUNT], max_level = (int)plan[PW_MAXL], sms = (int)plan[PW_SMS];
+    const bool split = plan[PW_PREC] == GCSL_PREC_SPLIT;
+    BatchLayout Ly;
+    Ly.table = 0;
+    Ly.off_tiles = al((size_t)count * sizeof(BInst));
+    Ly.off_rows = Ly.off_tiles + al(((size_t)count + 1) * sizeof(long long));
+    Ly.off_p2 = Ly.off_rows + al(((size_t)count + 1) * sizeof(long long));
+    Ly.edges = Ly.off_p2 + al(((size_t)count + 1) * sizeof(long long));
+    Ly.edge_off = Ly.edges + al((size_t)count * sizeof(long long));
+    const BInst *inst = reinterpret_cast<const BInst *>(base + Ly.table);
+    const long long *ot = reinterpret_cast<const long long *>(base + Ly.off_tiles);
+    const long long *orow = reinterpret_cast<const long long *>(base + Ly.off_rows);
+    const long long *op2 = reinterpret_cast<const long long *>(base + Ly.off_p2);
+    long long *edges = reinterpret_cast<long long *>(base + Ly.edges);
+    long long *eoff = reinterpret_cast<long long *>(base + Ly.edge_off);
+
+    batch_init_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count);
+    batch_level0_kernel<<<(unsigned)plan[PW_TILES], 256, 0, s>>>(inst, ot, count);
+    note_launch(2);
+    const long long rows = plan[PW_ROWS];
+    const int cblocks = (int)std::min<long long>((rows + 7) / 8, (long long)sms * 16);
+    for (int level = 1; level <= max_level; ++level) {
+        batch_compact_kernel<<<cblocks, 256, 0, s>>>(inst, orow, count, level);
+        batch_scan_kernel<<<count, 256, 0, s>>>(inst, count, level, max_level, edges);
+        batch_edge_offsets_kernel<<<1, 1024, 0, s>>>(edges, count, eoff);
+        note_launch(3);
+        const int lanes = (int)plan[PW_LANES + level];
+        const cudaError_t e = split ? launch_level<true>(level, lanes, inst, eoff, count, sms, s)
+                                    : launch_level<false>(level, lanes, inst, eoff, count, sms, s);
+        if (e != cudaSuccess) return GCSL_ERR_DEVICE;
+    }
+    batch_pmax_removed_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count);
+    batch_pmax_kept_kernel<<<count, 256, 0, s>>>(inst);
+    note_launch(2);
+    return cudaGetLastError() == cudaSuccess ? GCSL_OK : GCSL_ERR_DEVICE;
+}
+
+// Synchronises the stream and copies every instance's state back into the outputs.
+int gauss_batch_collect(const long long *plan, gcsl_gauss_instance *out, int count, cudaStream_t s) {
+    if (!gauss_batch_plan_ok(plan) || count != (int)plan[PW_COUNT]) return GCSL_ERR_INVALID_ARG;
+    char *base = reinterpret_cast<char *>(static_cast<uintptr_t>(plan[PW_WS]));
+    std::vector<BInst> tab((size_t)count);
+    if (cudaMemcpyAsync(tab.data(), base, tab.size() * sizeof(BInst), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return GCSL_ERR_DEVICE;
+    std::vector<DevState> st((size_t)count);
+    for (int k = 0; k < count; ++k)
+        if (cudaMemcpyAsync(&st[(size_t)k], tab[(size_t)k].st, sizeof(DevState), cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess)
+            return GCSL_ERR_DEVICE;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    int first = GCSL_OK;
+    for (int k = 0; k < count; ++k) {
+        const DevState &h = st[(size_t)k];
+        gcsl_gauss_instance &o = out[k];
+        o.status = h.status;
+        o.levels_run = h.last_level + 1;
+        o.n_records = (int64_t)h.n_rec_ints;
+        long long tests = (long long)o.p * (o.p - 1) / 2;
+        for (int l = 1; l <= BATCH_MAX_LEVEL; ++l) tests += (long long)h.tests[l];
+        o.tests = tests;
+        o.retests = (int64_t)h.retests;
+        if (first == GCSL_OK && h.status != GCSL_OK) first = h.status;
+    }
+    return first;
+}
+
+}  // namespace host
+}  // namespace gcsl

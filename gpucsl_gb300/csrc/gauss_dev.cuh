@@ -1,0 +1,479 @@
+// Device helpers of the Gaussian CI tests shared by the single-instance level loop
+// (gauss.cu) and the batched one (gauss_batch.cu): the test arithmetic, the edge /
+// key bookkeeping of a level, the sepset write-back and the p-value functions.
+#pragma once
+
+#include "common.cuh"
+
+namespace gcsl {
+
+// ----------------------------------------------------------------- level 0
+// 32 x 32 tiles of the upper triangle (tile row bi <= tile column bj): for i < j,
+// Z = |0.5 log|(1+r)/(1-r)||, r = C[i*p + j]; remove iff Z < tau0.  Kept pairs store
+// z* = Z (NaN ignored) and append i * p + j to `kept`; removed pairs store the marker
+// -1: their z* is final and their pmax is computed from C by pmax_level0_kernel,
+// concurrently with the later levels.
+// The mirrored skeleton entries are written through a shared-memory transpose so both
+// triangles are stored row-contiguously; zero diagonal.
+// One block of 256 threads per tile; `tile` enumerates the upper-triangle tiles row by row.
+__device__ __forceinline__ void level0_tile(const double *__restrict__ C, int p, double tau0, double t0sq,
+                                            uint16_t *__restrict__ G, double *__restrict__ zmin,
+                                            int *__restrict__ kept, DevState *st, int tile) {
+    __shared__ uint16_t tg[32][33];
+    const int nb = (p + 31) / 32;
+    int rem = tile, bi = 0;
+    while (rem >= nb - bi) {
+        rem -= nb - bi;
+        ++bi;
+    }
+    const int bj = bi + rem;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 rows per pass
+    unsigned long long removed = 0;
+    for (int r = ty; r < 32; r += 8) {
+        const int i = bi * 32 + r, j = bj * 32 + tx;
+        uint16_t g = 0;
+        if (i < p && j < p && i < j) {
+            const double c = __ldg(C + (size_t)i * p + j);
+            // Z0 = atanh-like in |r| on [0, 1): Z0 < tau0 <=> r^2 < tanh(tau0)^2; the knife
+            // edge, |r| >= 1 and NaN take the reference formula
+            const double r2 = c * c;
+            bool rem0;
+            double z = -1.0;  // marker: z* of a level-0 removal is finished on the side stream
+            if (r2 < 1.0 && fabs(r2 - t0sq) > 1e-12 * t0sq) {
+                rem0 = r2 < t0sq;
+                if (!rem0) z = fabs(0.5 * log(fabs((1.0 + c) / (1.0 - c))));
+            } else {
+                z = fabs(0.5 * log(fabs((1.0 + c) / (1.0 - c))));
+                rem0 = z < tau0;
+                if (rem0) z = -1.0;
+            }
+            g = rem0 ? 0 : 1;
+            zmin[(size_t)i * p + j] = isnan(z) ? __longlong_as_double(0x7ff0000000000000ll) : z;
+            removed += rem0;
+        }
+        // kept pairs join the list whose pmax is finished after the last level
+        const unsigned km = __ballot_sync(GCSL_FULL_MASK, g != 0 && i < j);
+        if (km) {
+            int base = 0;
+            if (tx == 0) base = atomicAdd(&st->n_kept, __popc(km));
+            base = __shfl_sync(GCSL_FULL_MASK, base, 0);
+            if (g != 0 && i < j) kept[base + __popc(km & ((1u << tx) - 1u))] = i * p + j;
+        }
+        if (i < p && j < p && (bi != bj || i <= j)) G[(size_t)i * p + j] = g;  // includes the zero diagonal
+        tg[r][tx] = g;
+    }
+    __syncthreads();
+    if (bi != bj) {
+        for (int r = ty; r < 32; r += 8) {
+            const int j = bj * 32 + r, i = bi * 32 + tx;  // lower triangle (j, i), j > i
+            if (i < p && j < p) G[(size_t)j * p + i] = tg[tx][r];
+        }
+    } else {
+        for (int r = ty; r < 32; r += 8) {
+            const int j = bj * 32 + r, i = bi * 32 + tx;
+            if (i < p && j < p && j > i) G[(size_t)j * p + i] = tg[tx][r];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) removed += __shfl_xor_sync(GCSL_FULL_MASK, removed, o);
+    if ((threadIdx.x & 31) == 0 && removed) atomicAdd(&st->removed[0], removed);
+}
+
+// ------------------------------------------------------------- compaction
+// One warp compacts row r: adj[r*p] = degree, adj[r*p + 1 ..] = ascending neighbour ids
+// (entries past the degree keep stale values, as in the reference); also writes
+// up[r] = #neighbours > r.  Returns the degree.
+__device__ __forceinline__ int compact_row(const uint16_t *__restrict__ G, int p, int *__restrict__ adj,
+                                           int *__restrict__ up, int r, int lane) {
+    {
+        const uint16_t *Gr = G + (size_t)r * p;
+        int *row = adj + (size_t)r * p;
+        int cnt = 0, ups = 0;
+        for (int c0 = 0; c0 < p; c0 += 32) {
+            const int c = c0 + lane;
+            const bool e = (c < p) && (c != r) && (Gr[c] != 0);
+            const unsigned b = __ballot_sync(GCSL_FULL_MASK, e);
+            if (e) row[1 + cnt + __popc(b & ((1u << lane) - 1))] = c;
+            cnt += __popc(b);
+            ups += __popc(__ballot_sync(GCSL_FULL_MASK, e && c > r));
+        }
+        if (lane == 0) {
+            row[0] = cnt;
+            if (up != nullptr) up[r] = ups;
+        }
+        return cnt;
+    }
+}
+
+// Levels >= 2: one warp refilters row r's previous neighbour list against G (rows only
+// shrink, so this touches deg entries instead of p) and writes up[r]; the row scan then
+// rebuilds the edge prefix.  Returns the degree.
+__device__ __forceinline__ int recompact_row(const uint16_t *__restrict__ G, int p, int *__restrict__ adj,
+                                             int *__restrict__ up, int r, int lane) {
+    {
+        int *row = adj + (size_t)r * p;
+        const int deg = row[0];
+        int cnt = 0, ups = 0;
+        for (int k0 = 0; k0 < deg; k0 += 32) {
+            const int k = k0 + lane;
+            const int c = k < deg ? row[1 + k] : 0;
+            const bool keep = k < deg && G[(size_t)r * p + c] != 0;
+            const unsigned b = __ballot_sync(GCSL_FULL_MASK, keep);
+            __syncwarp();  // every read of this 32-entry window precedes the writes below
+            if (keep) row[1 + cnt + __popc(b & ((1u << lane) - 1))] = c;
+            cnt += __popc(b);
+            ups += __popc(__ballot_sync(GCSL_FULL_MASK, keep && c > r));
+        }
+        if (lane == 0) {
+            row[0] = cnt;
+            up[r] = ups;
+        }
+        return cnt;
+    }
+}
+
+// Exclusive scan by one whole block of a per-row count (int or weighted long long) into
+// prefix[0..p]; prefix[p] is the total.
+template <typename T>
+__device__ __forceinline__ void block_scan_rows(const T *__restrict__ cnt, int p, long long *__restrict__ prefix) {
+    __shared__ long long warp_tot[32];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int per = (p + nt - 1) / nt;
+    const int b = tid * per, e = min(p, b + per);
+    long long s = 0;
+    for (int i = b; i < e; ++i) s += (long long)cnt[i];
+    // inclusive scan of s across the block
+    long long v = s;
+    const int lane = tid & 31, w = tid >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        long long t = __shfl_up_sync(GCSL_FULL_MASK, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) warp_tot[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        long long t = (lane < (nt >> 5)) ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            long long u = __shfl_up_sync(GCSL_FULL_MASK, t, o);
+            if (lane >= o) t += u;
+        }
+        warp_tot[lane] = t;
+    }
+    __syncthreads();
+    long long base = v - s + (w > 0 ? warp_tot[w - 1] : 0);
+    for (int i = b; i < e; ++i) {
+        prefix[i] = base;
+        base += (long long)cnt[i];
+    }
+    if (tid == nt - 1) prefix[p] = base;
+}
+
+// ---------------------------------------------------------- level l, L <= 12
+// One CI test: Gaussian elimination without square roots on the lower triangle of the
+// augmented matrix [[C_SS, C_S,vi, C_S,vj], [., 1, C_vi,vj], [., ., 1]].  After the L
+// pivots of C_SS the trailing 2x2 block is H = M0 - M1 M2^-1 M1^T of
+// gaussian_helpers.cu:78-89, and rho^2 = H01^2 / (|H00| |H11|).
+//
+// The statistic Z = |0.5 (log|1 + rho| - log|1 - rho|)| increases with |rho| on [0, 1),
+// so "Z < tau" is "rho^2 < tanh(tau)^2" there and no logarithm is needed per test.  For
+// |rho| >= 1 (Z decreases again), NaN, or rho^2 within 1e-12 of the threshold, Z is
+// evaluated with the reference's formula and compared with tau directly.
+struct TestOut {
+    double rho2;   // rho^2 when the monotone branch decided, +inf otherwise
+    double zexact; // Z from the reference formula when evaluated, +inf otherwise (NaN kept)
+    bool remove;
+};
+
+__device__ __forceinline__ double z_of_rho(double rho) {
+    return fabs(0.5 * (log(fabs(1.0 + rho)) - log(fabs(1.0 - rho))));
+}
+
+template <int L>
+__device__ __forceinline__ TestOut gauss_test_reg(const double *__restrict__ C, int p, int vi, int vj, const int *S,
+                                                  double tau, double t2) {
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    if constexpr (L == 1) {
+        // closed form: with m = C_ss, a = C_vi,s, b = C_vj,s, r = C_vi,vj the trailing block
+        // times m is [[m - a^2, r m - a b], [., m - b^2]]; the decision compares
+        // num = (r m - a b)^2 with t^2 den, den = |m - a^2| |m - b^2|, without a division
+        const double m = __ldg(C + (size_t)S[0] * p + S[0]);
+        const double a = __ldg(C + (size_t)vi * p + S[0]);
+        const double b = __ldg(C + (size_t)vj * p + S[0]);
+        const double r = __ldg(C + (size_t)vi * p + vj);
+        const double d00 = fma(-a, a, m), d11 = fma(-b, b, m);
+        const double n01 = fma(r, m, -(a * b));
+        const double num = n01 * n01, den = fabs(d00) * fabs(d11);
+        TestOut o;
+        const double tden = t2 * den;
+        if (num < den && fabs(num - tden) > 1e-12 * tden) {
+            o.rho2 = num / den;
+            o.zexact = inf;
+            o.remove = num < tden;
+        } else {
+            const double z = z_of_rho(n01 / (sqrt(fabs(d00)) * sqrt(fabs(d11))));
+            o.rho2 = inf;
+            o.zexact = z;
+            o.remove = z < tau;
+        }
+        return o;
+    }
+    constexpr int D = L + 2;
+    double A[D * (D + 1) / 2];  // row-packed lower triangle; rows 0..L-1 = S, L = v_i, L+1 = v_j
+#pragma unroll
+    for (int r = 0; r < L; ++r) {
+        const double *Cr = C + (size_t)S[r] * p;
+#pragma unroll
+        for (int c = 0; c <= r; ++c) A[r * (r + 1) / 2 + c] = __ldg(Cr + S[c]);
+        A[L * (L + 1) / 2 + r] = __ldg(C + (size_t)vi * p + S[r]);
+        A[(L + 1) * (L + 2) / 2 + r] = __ldg(C + (size_t)vj * p + S[r]);
+    }
+    A[L * (L + 1) / 2 + L] = 1.0;
+    A[(L + 1) * (L + 2) / 2 + L] = __ldg(C + (size_t)vi * p + vj);
+    A[(L + 1) * (L + 2) / 2 + L + 1] = 1.0;
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+        const double inv = 1.0 / A[j * (j + 1) / 2 + j];
+#pragma unroll
+        for (int i = j + 1; i < D; ++i) {
+            const double t = A[i * (i + 1) / 2 + j] * inv;
+#pragma unroll
+            for (int k = j + 1; k <= i; ++k) A[i * (i + 1) / 2 + k] -= t * A[k * (k + 1) / 2 + j];
+        }
+    }
+    const double h00 = A[L * (L + 1) / 2 + L];
+    const double h01 = A[(L + 1) * (L + 2) / 2 + L];
+    const double h11 = A[(L + 1) * (L + 2) / 2 + L + 1];
+    const double rho2 = (h01 * h01) / (fabs(h00) * fabs(h11));
+    TestOut o;
+    if (rho2 < 1.0 && fabs(rho2 - t2) > 1e-12 * t2) {
+        o.rho2 = rho2;
+        o.zexact = inf;
+        o.remove = rho2 < t2;
+    } else {
+        const double z = z_of_rho(h01 / (sqrt(fabs(h00)) * sqrt(fabs(h11))));
+        o.rho2 = inf;
+        o.zexact = z;
+        o.remove = z < tau;
+    }
+    return o;
+}
+
+struct EdgeJob {
+    int lo, hi, deg_lo, deg_hi;
+    long long R0, R1, T, Rmin;
+    int longer;
+};
+
+template <int KMAX>
+__device__ __forceinline__ bool load_edge(const int *__restrict__ adj, const int *__restrict__ up,
+                                          const long long *__restrict__ prefix, int p, long long e, int L,
+                                          EdgeJob &J) {
+    const int i = upper_row(prefix, p, e);
+    const long long k = e - prefix[i];
+    const int *row = adj + (size_t)i * p;
+    const int deg = row[0];
+    const int j = row[1 + (deg - up[i]) + (int)k];
+    J.lo = i;
+    J.hi = j;
+    J.deg_lo = deg;
+    J.deg_hi = adj[(size_t)j * p];
+    const int K0 = J.deg_lo - 1, K1 = J.deg_hi - 1;
+    J.R0 = (K0 >= L) ? (KMAX > 0 ? binom_small<KMAX>(K0, L) : binom_rt(K0, L)) : 0;
+    J.R1 = (K1 >= L) ? (KMAX > 0 ? binom_small<KMAX>(K1, L) : binom_rt(K1, L)) : 0;
+    J.T = J.R0 + J.R1;
+    J.Rmin = J.R0 < J.R1 ? J.R0 : J.R1;
+    J.longer = J.R0 > J.R1 ? 0 : 1;
+    return J.R0 < GCSL_RANK_LIMIT && J.R1 < GCSL_RANK_LIMIT;
+}
+
+// merged key index m -> (rank, dir)
+__device__ __forceinline__ void key_of(const EdgeJob &J, long long m, long long &rank, int &dir) {
+    if (m < 2 * J.Rmin) {
+        rank = m >> 1;
+        dir = (int)(m & 1);
+    } else {
+        rank = m - J.Rmin;
+        dir = J.longer;
+    }
+}
+
+__device__ __forceinline__ void write_removal(const EdgeJob &J, int L, const int *S, int p, int max_level,
+                                              uint16_t *G, int *sep_dense, int *rec_pool, long long rec_cap,
+                                              DevState *st) {
+    G[(size_t)J.lo * p + J.hi] = 0;
+    G[(size_t)J.hi * p + J.lo] = 0;
+    if (sep_dense != nullptr && L <= max_level) {
+        for (int k = 0; k < L; ++k) {
+            sep_dense[((size_t)J.lo * p + J.hi) * max_level + k] = S[k];
+            sep_dense[((size_t)J.hi * p + J.lo) * max_level + k] = S[k];
+        }
+    }
+    if (rec_pool != nullptr) {
+        const unsigned long long off = atomicAdd(&st->n_rec_ints, (unsigned long long)(3 + L));
+        if ((long long)(off + 3 + L) <= rec_cap) {
+            rec_pool[off] = J.lo;
+            rec_pool[off + 1] = J.hi;
+            rec_pool[off + 2] = L;
+            for (int k = 0; k < L; ++k) rec_pool[off + 3 + k] = S[k];
+        } else {
+            set_status(st, GCSL_ERR_CAPACITY);
+        }
+    }
+}
+
+// Common level entry: stop when the loop is finished or the level cannot run.
+__device__ __forceinline__ bool level_active(DevState *st, int level, bool tau_valid) {
+    if (st->done) return false;
+    const int md = st->max_degree[level];
+    if (md - 1 < level) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->done = 1;
+        return false;
+    }
+    if (!tau_valid) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            set_status(st, GCSL_ERR_UNSUPPORTED_LEVEL);
+            st->done = 1;
+        }
+        return false;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->last_level = level;
+    return true;
+}
+
+// Min over the G-lane group (aligned groups of G lanes inside the warp).
+template <int G>
+__device__ __forceinline__ double group_min(double v) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(GCSL_FULL_MASK, v, o));
+    return v;
+}
+
+// The FP64 test of the plain path as a functor for walk_edge.
+template <int L>
+struct F64Test {
+    const double *__restrict__ C;
+    int p;
+    double tau, t2;
+    __device__ __forceinline__ TestOut operator()(int vi, int vj, const int *S) const {
+        return gauss_test_reg<L>(C, p, vi, vj, S, tau, t2);
+    }
+};
+
+// One G-lane group walks edge J's merged key sequence G keys at a time: each lane tests
+// one key, the lowest removing lane is the canonical remover (its set is written back),
+// and the keys up to it fold into the group's minima of rho^2 (r2min) and of the exactly
+// evaluated Z (zmin_exact).  Every lane of the warp must call this (warp-wide votes); a
+// lane with has == false takes part without testing.
+template <int L, int G, class Test>
+__device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int *__restrict__ adj, int p, int gl,
+                                          unsigned gshift, unsigned gbits, const Test &test, uint16_t *G_,
+                                          int *sep_dense, int max_level, int *rec_pool, long long rec_cap,
+                                          DevState *st, double &r2min, double &zmin_exact, bool &removed,
+                                          unsigned long long &n_tests) {
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    bool done = !has || J.T == 0;
+    long long base = 0;
+    while (__any_sync(GCSL_FULL_MASK, !done)) {
+        const long long m = base + gl;
+        const bool valid = !done && m < J.T;
+        TestOut o;
+        o.rho2 = inf;
+        o.zexact = inf;
+        o.remove = false;
+        int S[L];
+        if (valid) {
+            long long rank;
+            int dir;
+            key_of(J, m, rank, dir);
+            const int vi = dir ? J.hi : J.lo, vj = dir ? J.lo : J.hi;
+            const int K = (dir ? J.deg_hi : J.deg_lo) - 1;
+            int pos[L];
+            unrank_positions<L>(K, rank, pos);
+            const int *nbrs = adj + (size_t)vi * p + 1;
+#pragma unroll
+            for (int c = 0; c < L; ++c) S[c] = resolve_position(nbrs, vj, pos[c]);
+            o = test(vi, vj, S);
+        }
+        const unsigned bal = (__ballot_sync(GCSL_FULL_MASK, o.remove) >> gshift) & gbits;
+        const int first = bal ? (__ffs(bal) - 1) : G;
+        const bool fold = valid && gl <= first;
+        const double r2 = group_min<G>(fold ? o.rho2 : inf);
+        const double ze = group_min<G>((fold && !isnan(o.zexact)) ? o.zexact : inf);
+        if (!done) {
+            r2min = fmin(r2min, r2);
+            zmin_exact = fmin(zmin_exact, ze);
+            const long long left = J.T - base;
+            if (gl == 0) n_tests += (unsigned long long)(bal ? first + 1 : (left < G ? left : G));
+            if (bal) {
+                if (gl == first) write_removal(J, L, S, p, max_level, G_, sep_dense, rec_pool, rec_cap, st);
+                removed = true;
+                done = true;
+            } else {
+                base += G;
+                if (base >= J.T) done = true;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ p-values
+// 2 sf(z) = erfc(z / sqrt 2) from Taylor expansions of erfc about the centres
+// c_m = (m + 1/2) / 8, m < 32, which cover [0, 4):  erfc(c + t) = sum_k a_k t^k with
+// a_0 = erfc(c) and a_{k+1} = b_k / (k + 1), where b_k are the Taylor coefficients of
+// erfc'(c + t) = erfc'(c) exp(-2 c t - t^2):  b_0 = -(2 / sqrt pi) exp(-c^2) and
+// (k + 1) b_{k+1} = -2 c b_k - 2 b_{k-1} (from E' = -(2c + 2t) E for E = exp(-2ct - t^2)).
+// With |t| <= 1/16, 13 terms leave a truncation error below 1e-18 of the value on the
+// whole range; arguments from 4 on (and NaN) go to the library erfc.  One Horner chain
+// replaces erf/erfc, which matters on a GPU whose FP64 pipe is 1/64 of its FP32 pipe.
+constexpr int SF_CENTRES = 32, SF_TERMS = 13;
+
+// Built by each block into shared memory (one thread per centre).
+__device__ __forceinline__ void sf_table_build(double (*a)[SF_TERMS]) {
+    for (int m = threadIdx.x; m < SF_CENTRES; m += blockDim.x) {
+        const double c = (m + 0.5) * 0.125;
+        double bprev = 0.0, b = -1.12837916709551257390 * exp(-c * c);  // 2 / sqrt(pi)
+        a[m][0] = erfc(c);
+        for (int k = 0; k + 1 < SF_TERMS; ++k) {
+            a[m][k + 1] = b / (k + 1);
+            const double bn = (-2.0 * c * b - 2.0 * bprev) / (k + 1);
+            bprev = b;
+            b = bn;
+        }
+    }
+}
+
+__device__ __forceinline__ double two_sf_tab(double z, const double (*a)[SF_TERMS]) {
+    const double x = fabs(z) * 0.70710678118654752440;
+    if (!(x < 4.0)) return erfc(x);
+    const int m = (int)(x * 8.0);
+    const double t = x - (m + 0.5) * 0.125;
+    double v = a[m][SF_TERMS - 1];
+#pragma unroll
+    for (int k = SF_TERMS - 2; k >= 0; --k) v = fma(v, t, a[m][k]);
+    return v;
+}
+
+// Z(r) = |atanh r|: for r^2 < 1/100 the series |r| sum_{k<10} r^{2k} / (2k + 1)
+// (truncation below 1e-20 of the value), else the reference's form
+// |0.5 ln|(1 + r) / (1 - r)|| (gaussian_ci.cu:36-37).
+__device__ __forceinline__ double fisher_z(double r) {
+    const double u = r * r;
+    if (u < 0.01) {
+        double s = 1.0 / 19.0;
+        s = fma(s, u, 1.0 / 17.0);
+        s = fma(s, u, 1.0 / 15.0);
+        s = fma(s, u, 1.0 / 13.0);
+        s = fma(s, u, 1.0 / 11.0);
+        s = fma(s, u, 1.0 / 9.0);
+        s = fma(s, u, 1.0 / 7.0);
+        s = fma(s, u, 1.0 / 5.0);
+        s = fma(s, u, 1.0 / 3.0);
+        s = fma(s, u, 1.0);
+        return fabs(r) * s;
+    }
+    return fabs(0.5 * log(fabs((1.0 + r) / (1.0 - r))));
+}
+
+}  // namespace gcsl

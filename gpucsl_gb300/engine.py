@@ -7,6 +7,7 @@ memory until `to_host` is called.  All work is enqueued on the current torch str
 from __future__ import annotations
 
 import ctypes as ct
+import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -31,6 +32,18 @@ def records_to_dense(rec: np.ndarray, n_ints: int, p: int, max_level: int) -> np
             out[lo, hi, :lev] = s
             out[hi, lo, :lev] = s
         k += 3 + lev
+    return out
+
+
+def gaussian_thresholds(n_obs: int, alpha: float) -> list[float]:
+    """The 50 Fisher-z thresholds of helpers.py:42-50: |Phi^-1(alpha/2)| / sqrt(n - l - 4)
+    for the levels the table covers, 0.0 after."""
+    from scipy.stats import norm
+
+    out = [0.0] * 50
+    q = norm.ppf(alpha / 2, loc=0, scale=1)
+    for i in range(1, min(50, n_obs - 3) - 1):
+        out[i - 1] = abs(q / math.sqrt(n_obs - i - 3))
     return out
 
 

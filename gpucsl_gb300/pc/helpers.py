@@ -42,12 +42,9 @@ def timed(f: Callable[..., U]) -> Callable[..., TimedReturnT[U]]:
 def get_gaussian_thresholds(data: np.ndarray, alpha: float = 0.05):
     """Fisher-z thresholds per level (helpers.py:42-50): entry l is
     |Phi^-1(alpha/2)| / sqrt(n - l - 4) for the levels the 50-entry table covers, 0.0 after."""
-    num_observations = data.shape[0]
-    out = [0.0] * NUMBER_OF_THRESHOLDS
-    q = norm.ppf(alpha / 2, loc=0, scale=1)
-    for i in range(1, min(NUMBER_OF_THRESHOLDS, num_observations - 3) - 1):
-        out[i - 1] = abs(q / sqrt(num_observations - i - 3))
-    return out
+    from ..engine import gaussian_thresholds
+
+    return gaussian_thresholds(data.shape[0], alpha)
 
 
 def init_pc_graph(data: np.ndarray) -> np.ndarray:

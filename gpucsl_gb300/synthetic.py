@@ -102,3 +102,41 @@ def discrete_bn_data(p: int, n: int, expected_degree: float, seed: int, max_in_d
     dag = np.zeros((p, p), np.uint8)
     dag[np.ix_(order, order)] = kept.astype(np.uint8)
     return DiscreteWorkload(np.ascontiguousarray(data), dag, card, seed)
+
+
+def gaussian_dag_data_device(p: int, n: int, expected_degree: float, seed: int, device="cuda"):
+    """gaussian_dag_data's law with the samples drawn on the device: the order, DAG and
+    weights come from numpy.random.default_rng(seed) as above, the N(0, 1) noise from a
+    torch generator seeded with `seed`, and X = E (I - W)^-1 in topological positions by
+    one triangular solve (FP64).  Returns an (n, p) float64 device tensor."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(p)
+    prob = 0.0 if p < 2 else min(1.0, expected_degree / (p - 1))
+    upper = np.triu(rng.random((p, p)) < prob, 1)
+    w = rng.uniform(0.1, 1.0, size=(p, p)) * rng.choice([-1.0, 1.0], size=(p, p))
+    W = torch.from_numpy(np.where(upper, w, 0.0)).to(device)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(seed))
+    E = torch.randn((n, p), generator=gen, dtype=torch.float64, device=device)
+    A = torch.eye(p, dtype=torch.float64, device=device) - W
+    Z = torch.linalg.solve_triangular(A, E, upper=True, left=False, unitriangular=True)
+    X = torch.empty_like(Z)
+    X[:, torch.from_numpy(order).to(device)] = Z
+    return X.contiguous()
+
+
+def batch_instance_sizes(count: int, base_seed: int = 1000, p_range=(50, 400), n_range=(500, 20000),
+                         deg_range=(2.0, 4.0)):
+    """Sizes of a batch of uneven Gaussian instances: instance k draws p ~ U{p_range},
+    n ~ U{n_range}, expected degree ~ U[deg_range] from default_rng(base_seed + k), and
+    its data use seed base_seed + k.  Returns a list of (p, n, deg, seed)."""
+    out = []
+    for k in range(count):
+        rng = np.random.default_rng(base_seed + k)
+        p = int(rng.integers(p_range[0], p_range[1] + 1))
+        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        deg = float(rng.uniform(deg_range[0], deg_range[1]))
+        out.append((p, n, deg, base_seed + k))
+    return out

@@ -52,6 +52,10 @@ typedef struct gcsl_stats {
 /* A sepset record in the int32 record pool: [lo, hi, level, S_0 .. S_{level-1}]. */
 
 int gcsl_version(void);
+/* Where and why the last failing CUDA call of the calling thread failed (the call that
+ * made an entry point return GCSL_ERR_DEVICE), e.g. "corr_ozaki_kernel launch:
+ * cudaErrorLaunchOutOfResources (...)"; "" when none failed. */
+const char *gcsl_last_error(void);
 const char *gcsl_status_string(int status);
 /* Number of kernels this library has launched in this process (instrumentation; no
  * reference counterpart). */
@@ -115,6 +119,72 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
 int gcsl_gauss_skeleton_noalloc(const double *C, int32_t p, int64_t n_obs, const double *thresholds,
                                 int32_t n_thresholds, int32_t max_level, uint16_t *G, int32_t *sepsets,
                                 int32_t *rec_pool, int64_t rec_cap, double *pmax, gcsl_stats *stats, void *stream);
+
+/* ---------------------------------------------------------------- batches
+ * Many independent Gaussian skeletons solved together (no counterpart in the reference,
+ * whose drivers solve one problem per call: discover_skeleton_gaussian.py:116-172).
+ * Every kernel of the level loop runs once for the whole batch; the run enqueues work
+ * only (no host reads), so it can be captured into a CUDA graph and replayed.
+ *
+ *   prepare  builds the device instance table inside `workspace` (synchronous; outside
+ *            any capture) and fills the opaque host plan;
+ *   run      enqueues the batch on `stream`: level 0, levels 1..max_level (each
+ *            instance stops by the reference's rule max degree - 1 < level), pmax;
+ *   collect  synchronises and writes status, levels_run, n_records, tests and retests
+ *            into the instance array.
+ * Precision GCSL_PREC_F64 gives results identical to gcsl_gauss_skeleton per instance.
+ * GCSL_PREC_SPLIT tests in FP32 on the instance's FP32 copy C32 and repeats in FP64 the
+ * tests whose p-value lies within 10 % of alpha (thresholds band_lo at 1.1 alpha and
+ * band_hi at 0.9 alpha) or whose elimination meets a pivot below 1e-3: skeleton and
+ * sepsets equal the FP64 ones, pmax carries the FP32 error of z*.
+ * max_level <= GCSL_BATCH_MAX_LEVEL; the instances of a plan must not overlap in time
+ * with another run of the same workspace. */
+#define GCSL_PREC_F64 0
+#define GCSL_PREC_SPLIT 1
+#define GCSL_BATCH_MAX_LEVEL 12
+
+typedef struct gcsl_gauss_instance {
+    const double *C;          /* device p x p FP64 correlation */
+    const float *C32;         /* device p x p FP32 copy (GCSL_PREC_SPLIT), else NULL */
+    int32_t p;
+    int64_t n_obs;
+    const double *thresholds; /* HOST Fisher-z thresholds at alpha (helpers.py:42-50) */
+    int32_t n_thresholds;
+    const double *band_lo;    /* HOST thresholds at 1.1 alpha (GCSL_PREC_SPLIT), else NULL */
+    const double *band_hi;    /* HOST thresholds at 0.9 alpha (GCSL_PREC_SPLIT), else NULL */
+    uint16_t *G;              /* device p x p skeleton out */
+    double *pmax;             /* device p x p pmax out */
+    int32_t *rec_pool;        /* device sepset record pool ([lo, hi, level, S...]), or NULL */
+    int64_t rec_cap;
+    int32_t status;           /* out (collect): device status of this instance */
+    int32_t levels_run;       /* out (collect) */
+    int64_t n_records;        /* out (collect): ints used in rec_pool (may exceed rec_cap) */
+    int64_t tests;            /* out (collect): canonical executed tests, level 0 included */
+    int64_t retests;          /* out (collect): FP64 re-tests of GCSL_PREC_SPLIT */
+} gcsl_gauss_instance;
+
+typedef struct gcsl_batch_plan {
+    int64_t w[48]; /* opaque */
+} gcsl_batch_plan;
+
+size_t gcsl_gauss_batch_workspace_bytes(const int32_t *p, int32_t count);
+int gcsl_gauss_batch_prepare(const gcsl_gauss_instance *inst, int32_t count, int32_t max_level, int32_t precision,
+                             void *workspace, size_t workspace_bytes, gcsl_batch_plan *plan, void *stream);
+int gcsl_gauss_batch_run(const gcsl_batch_plan *plan, void *stream);
+int gcsl_gauss_batch_collect(const gcsl_batch_plan *plan, gcsl_gauss_instance *inst, int32_t count, void *stream);
+/* Autotuner hook: lanes per edge (32 or 8; 8 only for levels <= 4) of a level's test
+ * kernel.  Results do not depend on it. */
+int gcsl_gauss_batch_set_lanes(gcsl_batch_plan *plan, int32_t level, int32_t lanes);
+
+/* Batched tensor-core correlation (the digit-product path of gcsl_corr_f64_tc for many
+ * sample matrices in one launch per stage).  X[k] is n[k] x p[k] (row stride ldx[k]),
+ * all of type dtype; C[k] receives the FP64 correlation and, when C32 is not NULL and
+ * C32[k] is not NULL, its FP32 copy.  prepare is synchronous; run only enqueues. */
+size_t gcsl_corr_tc_batch_workspace_bytes(const int64_t *n, const int32_t *p, int32_t count);
+int gcsl_corr_tc_batch_prepare(const void *const *X, int32_t dtype, const int64_t *n, const int32_t *p,
+                               const int64_t *ldx, double *const *C, float *const *C32, int32_t count,
+                               void *workspace, size_t workspace_bytes, gcsl_batch_plan *plan, void *stream);
+int gcsl_corr_tc_batch_run(const gcsl_batch_plan *plan, void *stream);
 
 /* ----------------------------------------------------- discrete skeleton (d,e) */
 /* Replaces the level loop of gpucsl/pc/discover_skeleton_discrete.py:80-112 with the

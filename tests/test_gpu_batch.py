@@ -1,0 +1,131 @@
+"""Batched Gaussian skeletons (many instances per launch) against the single-problem
+path and the FP64 oracle.
+
+Bar: the batched tensor-core correlation equals the single-problem one bit for bit
+(exact integer digit sums); precision "f64" gives each instance exactly the skeleton,
+sepsets and pmax of the single-problem path, and the oracle's within 1e-9; precision
+"split" (FP32 tests, FP64 re-test in the guard band) gives the same skeleton and
+sepsets; an instance gives the same results alone and in the mix, with or without
+CUDA-graph replay and after autotuning."""
+import numpy as np
+import pytest
+
+from gpucsl_gb300.synthetic import gaussian_dag_data
+from oracle import gaussian as og
+
+pytestmark = pytest.mark.gpu
+
+# (p, n, expected degree, seed): uneven sizes around the 128-row tile edge
+SIZES = [(20, 500, 2, 11), (57, 1200, 3, 12), (128, 3000, 2, 13), (129, 800, 4, 14), (200, 2500, 3, 15),
+         (64, 5000, 2, 16), (33, 700, 3, 17), (300, 1500, 2, 18), (7, 600, 2, 19), (1, 400, 2, 20)]
+ALPHA, MAXL = 0.01, 4
+
+
+@pytest.fixture(scope="module")
+def workloads():
+    return [gaussian_dag_data(p, n, d, s) for (p, n, d, s) in SIZES]
+
+
+def make_batch(torch, workloads, precision="f64", idx=None):
+    from gpucsl_gb300.batch import GaussianBatch
+
+    idx = list(range(len(workloads))) if idx is None else idx
+    ws = [workloads[k] for k in idx]
+    b = GaussianBatch([w.data.shape[1] for w in ws], [w.data.shape[0] for w in ws], ALPHA, MAXL, precision)
+    Xs = [torch.from_numpy(w.data).cuda() for w in ws]
+    b.bind_samples(Xs)
+    return b, Xs
+
+
+def test_batched_correlation_is_bit_identical(cuda, workloads):
+    from gpucsl_gb300 import engine
+
+    torch = cuda
+    b, Xs = make_batch(torch, workloads)
+    b.run(graph=False)
+    for k, X in enumerate(Xs):
+        C1 = engine.correlation(X)
+        assert torch.equal(b.C[k], C1), k
+
+
+def test_f64_batch_equals_single_path_and_oracle(cuda, workloads):
+    from gpucsl_gb300 import engine
+
+    torch = cuda
+    b, Xs = make_batch(torch, workloads)
+    res = b.run()
+    for k, w in enumerate(workloads):
+        n, p = w.data.shape
+        assert res[k].status == 0
+        G, sep, pmax = b.to_host(k)
+        s = engine.GaussianSolver(p, MAXL)
+        st = s.run(b.C[k], n, engine.gaussian_thresholds(n, ALPHA))
+        G1, sep1, pmax1 = s.to_host()
+        assert (G == G1).all() and (sep == sep1).all(), k
+        assert np.array_equal(pmax, pmax1), k
+        assert res[k].tests == st.tests, (k, res[k].tests, st.tests)
+        ref = og.skeleton(b.C[k].cpu().numpy(), n, ALPHA, MAXL)
+        assert (G == ref.skeleton).all() and (sep == ref.sepsets).all(), k
+        iu = np.triu_indices(p, 1)
+        rel = np.abs(pmax[iu] - ref.pmax[iu]) / np.maximum(np.abs(ref.pmax[iu]), 1e-300)
+        assert (rel <= 1e-9).all() | (p < 2), (k, float(rel.max()) if rel.size else 0.0)
+        assert res[k].tests == ref.tests_canonical, k
+
+
+def test_split_precision_keeps_every_decision(cuda, workloads):
+    torch = cuda
+    b64, _ = make_batch(torch, workloads, "f64")
+    r64 = b64.run()
+    b32, _ = make_batch(torch, workloads, "split")
+    r32 = b32.run()
+    worst = 0.0
+    for k in range(len(workloads)):
+        G, sep, pmax = b64.to_host(k)
+        G2, sep2, pmax2 = b32.to_host(k)
+        assert (G == G2).all() and (sep == sep2).all(), k
+        assert r32[k].tests == r64[k].tests, k
+        assert np.array_equal(b32.C[k].cpu().numpy(), b64.C[k].cpu().numpy())
+        worst = max(worst, float(np.abs(pmax - pmax2).max()))
+    assert worst < 1e-4, worst
+
+
+def test_instance_alone_equals_instance_in_the_mix(cuda, workloads):
+    torch = cuda
+    mix, _ = make_batch(torch, workloads)
+    mix.run()
+    for k in (0, 4, 7):
+        one, _ = make_batch(torch, workloads, idx=[k])
+        one.run()
+        a, b = mix.to_host(k), one.to_host(0)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y), k
+
+
+def test_graph_replay_and_autotune_keep_results(cuda, workloads):
+    torch = cuda
+    b, _ = make_batch(torch, workloads, "split")
+    b.run(graph=False)
+    first = [b.to_host(k) for k in range(len(workloads))]
+    b.autotune(reps=1)
+    for _ in range(2):
+        b.run(graph=True)
+        for k in range(len(workloads)):
+            for x, y in zip(first[k], b.to_host(k)):
+                assert np.array_equal(x, y), k
+
+
+def test_record_pool_growth(cuda, workloads):
+    from gpucsl_gb300.batch import GaussianBatch
+
+    torch = cuda
+    ws = workloads[:5]
+    b = GaussianBatch([w.data.shape[1] for w in ws], [w.data.shape[0] for w in ws], ALPHA, MAXL, "f64",
+                      record_cap=8)
+    b.bind_samples([torch.from_numpy(w.data).cuda() for w in ws])
+    res = b.run()
+    ref, _ = make_batch(torch, workloads, idx=list(range(5)))
+    ref.run()
+    for k in range(5):
+        assert res[k].n_records <= b.rec_caps[k]
+        for x, y in zip(b.to_host(k), ref.to_host(k)):
+            assert np.array_equal(x, y), k
