@@ -54,6 +54,7 @@ def parse_args():
     ap.add_argument("--impl", default="gpucsl_gb300", choices=["gpucsl_gb300", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip the discrete, batched and CPU-baseline legs")
     ap.add_argument("--batched-only", action="store_true", help="run only the batched-instances leg")
+    ap.add_argument("--serving-only", action="store_true", help="run only the serving leg")
     return ap.parse_args()
 
 
@@ -221,6 +222,8 @@ def batched_leg(reps: int = 10) -> dict:
     seeds 1000 + k, alpha 0.01, levels <= 4): batched tensor-core correlation + batched
     level loop replayed as one CUDA graph, split precision (FP32 tests, FP64 re-test in
     the guard band) and FP64; against the plain per-instance path on the same samples."""
+    import ctypes as ct
+
     import numpy as np
     import torch
 
@@ -257,6 +260,11 @@ def batched_leg(reps: int = 10) -> dict:
         for _ in range(2):
             b.graph.replay()
         ts = timed(b.graph.replay, reps)
+        L = engine._lib.lib()
+        t_corr = timed(lambda: engine._lib.check(L.gcsl_corr_tc_batch_run(ct.byref(b.corr_plan), engine._lib.stream_ptr()),
+                                                 "corr batch"), 3)
+        t_lv = timed(lambda: engine._lib.check(L.gcsl_gauss_batch_run(ct.byref(b.plan), engine._lib.stream_ptr()),
+                                               "gauss batch"), 3)
         res = b.collect()
         tests = sum(r.tests for r in res)
         results[prec] = [b.to_host(k) for k in range(BATCH_COUNT)]
@@ -264,6 +272,8 @@ def batched_leg(reps: int = 10) -> dict:
                      round(1e3 * statistics.median(ts), 3), "tests_per_batch": tests,
                      "tests_per_s": round(tests / statistics.median(ts), 1),
                      "retests": sum(r.retests for r in res), "lanes_per_level": lanes,
+                     "corr_ms": round(1e3 * statistics.median(t_corr), 3),
+                     "levels_ms": round(1e3 * statistics.median(t_lv), 3),
                      "status_nonzero": sum(1 for r in res if r.status != 0)}
         del b
         torch.cuda.empty_cache()
@@ -298,6 +308,36 @@ def batched_leg(reps: int = 10) -> dict:
                         "ms_per_batch": round(1e3 * statistics.median(tp), 3)}
     out["speedup_split_vs_plain"] = round(out["split"]["value"] / out["plain_f64"]["value"], 2)
     return out
+
+
+# ------------------------------------------------------------ serving leg
+SERVE_COUNT, SERVE_RATES = 64, (10.0, 40.0, 160.0, 320.0, 640.0, 1280.0)
+
+
+def serving_leg() -> dict:
+    """Poisson arrivals of a 70 % Gaussian (p log-uniform 20..2000, n 1000..50000, FP32
+    samples, alpha 0.01) / 30 % discrete (p 20..300, n 10000..100000, cardinality 2..6,
+    alpha 0.05) request mix, levels <= 3, 120 GB admission budget: latency from arrival
+    to results on the host through the continuous-batching server and through the plain
+    one-request-at-a-time path, on the same trace, rate swept until the server saturates."""
+    from gpucsl_gb300.serve import SkeletonServer, latency_summary, serve_plain
+    from gpucsl_gb300.synthetic import poisson_arrivals, serving_requests
+
+    reqs = serving_requests(SERVE_COUNT, seed=7)
+    warm = poisson_arrivals(reqs[:6], rate=1e9)
+    SkeletonServer(120e9).serve(warm)
+    serve_plain(warm)
+    rows = []
+    for rate in SERVE_RATES:
+        tr = poisson_arrivals(reqs, rate=rate, seed=11)
+        srv = latency_summary(SkeletonServer(120e9).serve(tr))
+        pln = latency_summary(serve_plain(tr))
+        rows.append({"rate_per_s": rate, "server": srv, "plain": pln})
+        if srv["skeletons_per_s"] is not None and srv["skeletons_per_s"] < 0.6 * rate:
+            break  # saturated
+    n_g = sum(1 for r in reqs if r.kind == "gaussian")
+    return {"workload": f"serving_{SERVE_COUNT}_requests_gauss{n_g}_disc{SERVE_COUNT - n_g}_L3_budget120GB",
+            "unit": "ms (latency), skeletons/s", "data": "synthetic (seeded per request)", "sweep": rows}
 
 
 # ------------------------------------------------------------------ our arm
@@ -484,6 +524,10 @@ def run_ours(args, world, rank, local):
     if not args.no_extras and rank == 0:
         out["batched"] = batched_leg()
 
+    # ---- serving: continuous batching under Poisson arrivals against the plain path
+    if not args.no_extras and rank == 0:
+        out["serving"] = serving_leg()
+
     # ---- CPU baseline: the oracle on the host cores (rank 0, N = 1 only)
     if not args.no_extras and rank == 0 and world == 1:
         t0 = time.perf_counter()
@@ -541,14 +585,15 @@ def main():
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
-    elif args.batched_only:
+    elif args.batched_only or args.serving_only:
         import torch
 
         from gpucsl_gb300 import build as gbuild
 
         gbuild.build()
         torch.cuda.set_device(local)
-        print(json.dumps({"batched": batched_leg()}), flush=True)
+        leg = batched_leg() if args.batched_only else serving_leg()
+        print(json.dumps({"batched" if args.batched_only else "serving": leg}), flush=True)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

@@ -130,18 +130,19 @@ struct LevelTimer {
     bool ok = false;
 };
 
+// The timers, the side stream and the pinned control words below exist once per host
+// thread and device: solves issued concurrently from several threads (on their own
+// streams) never share an event, a stream or a control word.
 LevelTimer *level_timer() {
     static const bool enabled = [] {
         const char *e = getenv("GCSL_LEVEL_TIMING");
         return e && e[0] == '1';
     }();
     if (!enabled) return nullptr;
-    static LevelTimer timers[64];
-    static std::mutex mu;
+    static thread_local LevelTimer timers[64];
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return nullptr;
-    std::lock_guard<std::mutex> lock(mu);
     LevelTimer &t = timers[dev];
     if (!t.ok) {
         for (auto &e : t.ev)
@@ -152,12 +153,10 @@ LevelTimer *level_timer() {
 }
 
 SideStream *side_stream() {
-    static SideStream streams[64];
-    static std::mutex mu;
+    static thread_local SideStream streams[64];
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return nullptr;
-    std::lock_guard<std::mutex> lock(mu);
     SideStream &s = streams[dev];
     if (!s.stream) {
         int lo = 0, hi = 0;  // numerically larger = lower priority
@@ -202,12 +201,10 @@ struct HostCtl {
 };
 
 HostCtl *host_ctl() {
-    static HostCtl ctl[64];
-    static std::mutex mu;
+    static thread_local HostCtl ctl[64];
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return nullptr;
-    std::lock_guard<std::mutex> lock(mu);
     HostCtl &c = ctl[dev];
     if (!c.words && cudaMallocHost(reinterpret_cast<void **>(&c.words), 2 * sizeof(int32_t)) != cudaSuccess)
         return nullptr;

@@ -536,7 +536,7 @@ static OzDims oz_dims(long long n, int p, int num_sms, int splits_req = 0) {
     D.p = p;
     D.p_pad = (p + OZ_TM - 1) / OZ_TM * OZ_TM;
     D.n_pad = (int)((n + OZ_KS - 1) / OZ_KS * OZ_KS);
-    D.n_tiles_j = D.p_pad / OZ_TN;
+    D.n_tiles_j = (p + OZ_TN - 1) / OZ_TN;  // 64-column tiles that hold a column < p
     const int n_tiles_i = D.p_pad / OZ_TM;
     int tiles = 0;
     for (int i = 0; i < n_tiles_i; ++i) tiles += D.n_tiles_j - 2 * i;

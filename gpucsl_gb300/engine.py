@@ -216,6 +216,15 @@ def ordinal_encode(data: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     n, p = data.shape
     codes = np.empty((p, n), np.uint8)
     dims = np.empty(p, np.uint8)
+    if data.dtype.kind in "ui" and n > 0 and data.min() >= 0 and data.max() <= 255:
+        # small non-negative integers: the observed values by a presence table per column
+        for v in range(p):
+            col = data[:, v].astype(np.intp)
+            present = np.bincount(col, minlength=256) > 0
+            rank = np.cumsum(present) - 1
+            codes[v] = rank[col].astype(np.uint8)
+            dims[v] = max(int(present.sum()), 1)
+        return codes, dims
     for v in range(p):
         uniq, inv = np.unique(data[:, v], return_inverse=True)
         if uniq.size > 255:

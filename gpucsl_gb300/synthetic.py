@@ -78,7 +78,7 @@ def discrete_bn_data(p: int, n: int, expected_degree: float, seed: int, max_in_d
     prob = 0.0 if p < 2 else min(1.0, expected_degree / (p - 1))
     upper = np.triu(rng.random((p, p)) < prob, 1)
     card = rng.integers(card_lo, card_hi + 1, size=p)
-    Z = np.zeros((n, p), np.int64)
+    Z = np.zeros((p, n), np.int64)  # one contiguous row per topological position
     kept = np.zeros((p, p), bool)
     card_pos = card[order]
     for b in range(p):
@@ -92,13 +92,13 @@ def discrete_bn_data(p: int, n: int, expected_degree: float, seed: int, max_in_d
         cfg = np.zeros(n, np.int64)
         mult = 1
         for u in parents:
-            cfg += Z[:, u] * mult
+            cfg += Z[u] * mult
             mult *= int(card_pos[u])
-        cdf = np.cumsum(cpt[cfg], axis=1)
+        cdf = np.cumsum(cpt, axis=1)[cfg]
         u01 = rng.random(n)[:, None]
-        Z[:, b] = np.minimum((u01 > cdf).sum(1), k - 1)
+        Z[b] = np.minimum((u01 > cdf).sum(1), k - 1)
     data = np.empty((n, p), np.uint8)
-    data[:, order] = Z.astype(np.uint8)
+    data[:, order] = Z.T.astype(np.uint8)
     dag = np.zeros((p, p), np.uint8)
     dag[np.ix_(order, order)] = kept.astype(np.uint8)
     return DiscreteWorkload(np.ascontiguousarray(data), dag, card, seed)
@@ -140,3 +140,45 @@ def batch_instance_sizes(count: int, base_seed: int = 1000, p_range=(50, 400), n
         deg = float(rng.uniform(deg_range[0], deg_range[1]))
         out.append((p, n, deg, base_seed + k))
     return out
+
+
+def serving_requests(count: int, seed: int = 7, gaussian_share: float = 0.7, max_level: int = 3,
+                     g_p=(20, 2000), g_n=(1000, 50000), d_p=(20, 300), d_n=(10000, 100000), d_card=(2, 6)):
+    """A mix of skeleton requests with their payloads in pinned host memory: Gaussian
+    (share `gaussian_share`): p log-uniform in g_p, n uniform in g_n, FP32 samples of a
+    degree-3 DAG, alpha 0.01; discrete: p uniform in d_p, n uniform in d_n, cardinality
+    uniform in d_card, degree 2, alpha 0.05, codes ordinal-encoded.  Each request draws
+    its sizes from default_rng(seed * 100003 + k) and its data from seed * 100003 + k.
+    Arrival times are left at 0 (see poisson_arrivals)."""
+    import torch
+
+    from .engine import ordinal_encode
+    from .serve import Request
+
+    out = []
+    for k in range(count):
+        s_k = seed * 100003 + k
+        rng = np.random.default_rng(s_k)
+        if rng.random() < gaussian_share:
+            p = int(round(np.exp(rng.uniform(np.log(g_p[0]), np.log(g_p[1])))))
+            n = int(rng.integers(g_n[0], g_n[1] + 1))
+            X = gaussian_dag_data_device(p, n, 3.0, s_k).float().cpu().pin_memory()
+            out.append(Request(k, "gaussian", p, n, 0.01, max_level, 0.0, samples=X))
+        else:
+            p = int(rng.integers(d_p[0], d_p[1] + 1))
+            n = int(rng.integers(d_n[0], d_n[1] + 1))
+            d = discrete_bn_data(p, n, 2, s_k, card_lo=d_card[0], card_hi=d_card[1])
+            codes, dims = ordinal_encode(d.data)
+            out.append(Request(k, "discrete", p, n, 0.05, max_level, 0.0,
+                               codes=torch.from_numpy(codes).pin_memory(), dims=dims))
+    return out
+
+
+def poisson_arrivals(requests, rate: float, seed: int = 11):
+    """Copies of `requests` with Poisson arrival times at `rate` per second (exponential
+    gaps from default_rng(seed)); the payloads are shared."""
+    from dataclasses import replace
+
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=len(requests)))
+    return [replace(r, arrival=float(a)) for r, a in zip(requests, t)]
