@@ -17,8 +17,8 @@
 
 namespace gcsl {
 namespace host {
-cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, int *kept, DevState *st,
-                          cudaStream_t s);
+cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, double *r2min, int *kept,
+                          DevState *st, cudaStream_t s);
 cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s);
 cudaError_t launch_scan_int(const int *cnt, int p, long long *prefix, DevState *st, cudaStream_t s);
 cudaError_t launch_recompact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s);
@@ -26,7 +26,8 @@ cudaError_t launch_scan_ll(const long long *cnt, int p, long long *prefix, DevSt
 cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, const int *up, const long long *prefix,
                                double tau, bool tau_valid, uint16_t *G, double *zmin, double *r2min, int *sep_dense,
                                int max_level, int *rec_pool, long long rec_cap, DevState *st, int num_sms,
-                               cudaStream_t s);
+                               const float *C32, int *qbuf, long long qcap, cudaStream_t s);
+cudaError_t launch_to_f32(const double *x, long long n, float *y, int num_sms, cudaStream_t s);
 cudaError_t launch_pmax(const int *kept, const DevState *st, const double *zmin, const double *r2min, int p,
                         long long n_obs, double *pmax, int num_sms,
                         cudaStream_t s);
@@ -256,8 +257,24 @@ struct GaussWs {
     long long *prefix;
     double *zmin, *r2min;
     int *kept;
+    float *c32;       // FP32 copy of C for the FP32-first tests
+    int *cand;        // FP64 z* candidate queue
+    long long cand_cap;
     size_t bytes;
 };
+
+// Ints of the z* candidate queue: entries hold 3 + level ints, about one or two per edge
+// and level; a full queue only moves evaluations back into the level kernel.
+long long cand_queue_ints(int p) { return std::max<long long>(1ll << 20, 4ll * p * p); }
+
+// FP32-first level tests (default) or FP64 throughout (GCSL_F64_TESTS=1, for comparisons).
+bool mixed_tests() {
+    static const bool mixed = [] {
+        const char *e = getenv("GCSL_F64_TESTS");
+        return !(e && e[0] == '1');
+    }();
+    return mixed;
+}
 
 GaussWs carve_gauss(void *ws, size_t cap, int p) {
     Carver c(ws, cap);
@@ -269,6 +286,9 @@ GaussWs carve_gauss(void *ws, size_t cap, int p) {
     w.zmin = c.take<double>((size_t)p * p);
     w.r2min = c.take<double>((size_t)p * p);
     w.kept = c.take<int>((size_t)p * (p - 1) / 2 + 1);
+    w.c32 = c.take<float>((size_t)p * p);
+    w.cand_cap = cand_queue_ints(p);
+    w.cand = c.take<int>((size_t)w.cand_cap);
     w.bytes = c.off;
     return w;
 }
@@ -382,7 +402,10 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
     LevelTimer *lt = stats ? level_timer() : nullptr;
     int n_timed = 0;  // events recorded: ev[0 .. n_timed]
     if (lt) cudaEventRecord(lt->ev[0], s);
-    if (host::launch_level0(C, p, thresholds[0], G, w.zmin, w.kept, w.st, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    const bool mixed = mixed_tests() && max_level >= 1;
+    if (mixed && host::launch_to_f32(C, (long long)p * p, w.c32, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    if (host::launch_level0(C, p, thresholds[0], G, w.zmin, w.r2min, w.kept, w.st, s) != cudaSuccess)
+        return GCSL_ERR_DEVICE;
     if (lt) {
         cudaEventRecord(lt->ev[1], s);
         n_timed = 1;
@@ -403,7 +426,8 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
         const double tau = tau_valid ? thresholds[level] : 0.0;
         if (e == cudaSuccess)
             e = host::launch_gauss_level(level, C, p, w.adj, w.up, w.prefix, tau, tau_valid, G, w.zmin, w.r2min,
-                                         sepsets, max_level, rec_pool, rec_cap, w.st, sms, s);
+                                         sepsets, max_level, rec_pool, rec_cap, w.st, sms, mixed ? w.c32 : nullptr,
+                                         mixed ? w.cand : nullptr, w.cand_cap, s);
         if (lt && level + 1 < GCSL_MAX_LEVELS + 2) {
             cudaEventRecord(lt->ev[level + 1], s);
             n_timed = level + 1;

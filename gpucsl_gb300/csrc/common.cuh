@@ -38,6 +38,7 @@ struct DevState {
     unsigned long long removed[GCSL_MAX_LEVELS];
     unsigned long long n_rec_ints;           // ints used in the record pool
     unsigned long long retests;              // FP64 re-tests of the split-precision path
+    unsigned long long cand_ints[GCSL_MAX_LEVELS];  // ints queued for the FP64 z* candidate kernel
 };
 
 // Arguments of one discrete test-kernel launch.

@@ -61,7 +61,7 @@ struct OzJob {
 
 // Kernel stages of a job; each has its own count of blocks per job.
 enum OzStage { OZ_INIT = 0, OZ_STATS, OZ_MEAN, OZ_DIGITS, OZ_PRODUCT, OZ_DIAG, OZ_FINISH, OZ_NSTAGES };
-constexpr int OZ_FINISH_ENTRIES = 4096;  // entries of C per finish block
+constexpr int OZ_FINISH_ENTRIES = 1024;  // entries of C per finish block (4 per thread)
 
 // Where a kernel finds its job: one job passed by value (block b of the stage is block b
 // of the job), or a device table of jobs with each stage's exclusive block offsets
@@ -359,6 +359,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
     if (warp == OZ_DRAIN_WARPS) {
         // ---------------- producer
         if (lane == 0) {
+            // a register copy: the copies' memory clobbers would reload a shared-memory field
+            const uint8_t *__restrict__ dig = s_job.dig;
             for (long long st = 0; st < nst; ++st) {
                 const int b = (int)(st % OZ_NST);
                 if (st >= OZ_NST && !mbar_wait_fast(&empty_bar[b], (uint32_t)(((st / OZ_NST) - 1) & 1))) {
@@ -371,11 +373,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
                 mbar_expect_tx(&full_bar[b], (uint32_t)OZ_STAGE_BYTES);
                 const long long q = q0 + st;
                 for (int k = 0; k < OZ_S; ++k) {
-                    bulk_g2s(sA + k * 4096, s_job.dig + (((size_t)k * nI + I) * nq + q) * 4096, 4096u,
-                             &full_bar[b]);
+                    bulk_g2s(sA + k * 4096, dig + (((size_t)k * nI + I) * nq + q) * 4096, 4096u, &full_bar[b]);
                     bulk_g2s(sB + k * 2048,
-                             s_job.dig + (((size_t)k * nI + (J >> 1)) * nq + q) * 4096 + (size_t)(J & 1) * 2048,
-                             2048u, &full_bar[b]);
+                             dig + (((size_t)k * nI + (J >> 1)) * nq + q) * 4096 + (size_t)(J & 1) * 2048, 2048u,
+                             &full_bar[b]);
                 }
             }
         }
@@ -460,9 +461,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
         if (ok) {
             const int row = qd * 32 + lane;
             const size_t base = ((size_t)split * D.p_pad + (size_t)(I * OZ_TM + row)) * D.p_pad + J * OZ_TN + cq * 16;
-#pragma unroll
             long long *__restrict__ part_hi = s_job.phi;
             long long *__restrict__ part_lo = s_job.plo;
+#pragma unroll
             for (int e = 0; e < 16; ++e) {
                 part_hi[base + e] = acc_hi[e];
                 part_lo[base + e] = acc_lo[e];

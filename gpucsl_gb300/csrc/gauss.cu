@@ -21,9 +21,9 @@ namespace gcsl {
 
 // ----------------------------------------------------------------- level 0
 __global__ void gauss_level0_kernel(const double *__restrict__ C, int p, double tau0, double t0sq,
-                                    uint16_t *__restrict__ G, double *__restrict__ zmin, int *__restrict__ kept,
-                                    DevState *st) {
-    level0_tile(C, p, tau0, t0sq, G, zmin, kept, st, (int)blockIdx.x);
+                                    uint16_t *__restrict__ G, double *__restrict__ zmin, double *__restrict__ r2min,
+                                    int *__restrict__ kept, DevState *st) {
+    level0_tile(C, p, tau0, t0sq, G, zmin, r2min, kept, st, (int)blockIdx.x);
 }
 
 // ------------------------------------------------------------- compaction
@@ -60,14 +60,22 @@ __global__ void row_scan_kernel(const T *__restrict__ cnt, int p, long long *__r
 // Level kernel: groups of G lanes each own one edge (32 / G edges per warp) and walk its
 // merged key sequence G keys at a time.  Small groups keep the FP64 pipe busy at the
 // upper levels, where an edge has only a handful of candidate sets, and stop at most
-// G - 1 tests past the first remover.
-template <int L, int G>
+// G - 1 tests past the first remover.  MIXED: the tests run FP32-first (MixedTest) and
+// queue their FP64 z* candidates for gauss_cand_kernel.
+struct MixArgs {
+    const float *C32;  // FP32 copy of C
+    float t2lo, t2hi;  // FP32 bounds of the knife edge around tanh(tau)^2
+    CandQueue q;
+};
+
+template <int L, int G, bool MIXED>
 __global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__restrict__ C, int p,
                                                              const int *__restrict__ adj, const int *__restrict__ up,
                                                              const long long *__restrict__ prefix, double tau,
                                                              double t2, bool tau_valid, uint16_t *G_, double *zmin,
                                                              double *r2min_pair, int *sep_dense, int max_level,
-                                                             int *rec_pool, long long rec_cap, DevState *st) {
+                                                             int *rec_pool, long long rec_cap, DevState *st,
+                                                             MixArgs mix) {
     if (!level_active(st, L, tau_valid)) return;
     constexpr int GPW = 32 / G;  // groups per warp
     const int lane = threadIdx.x & 31, gl = lane & (G - 1), gw = lane / G;
@@ -90,11 +98,17 @@ __global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__re
         if (has && gl == 0) n_full += J.T;
         double r2min = inf, zmin_exact = inf;
         bool removed = false;
-        walk_edge<L, G>(J, has, adj, p, gl, gshift, gbits, F64Test<L>{C, p, tau, t2}, G_, sep_dense, max_level,
-                        rec_pool, rec_cap, st, r2min, zmin_exact, removed, n_tests);
+        if constexpr (MIXED) {
+            walk_edge<L, G>(J, has, adj, p, gl, gshift, gbits,
+                            MixedTest<L>{C, mix.C32, p, tau, t2, mix.t2lo, mix.t2hi}, G_, sep_dense, max_level,
+                            rec_pool, rec_cap, st, r2min, zmin_exact, removed, n_tests, &mix.q);
+        } else {
+            walk_edge<L, G>(J, has, adj, p, gl, gshift, gbits, F64Test<L>{C, p, tau, t2}, G_, sep_dense, max_level,
+                            rec_pool, rec_cap, st, r2min, zmin_exact, removed, n_tests);
+        }
         if (has && gl == 0 && J.T > 0) {
             // z* candidates: exact Z into zmin, the monotone branch's min rho^2 into r2min
-            // (converted to Z once per pair by pmax_kernel)
+            // (converted to Z once per pair by the pmax kernel)
             const size_t ix = (size_t)J.lo * p + J.hi;
             if (zmin_exact < inf) zmin[ix] = fmin(zmin[ix], zmin_exact);
             if (r2min < inf) r2min_pair[ix] = fmin(r2min_pair[ix], r2min);
@@ -107,6 +121,20 @@ __global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__re
         if (n_removed) atomicAdd(&st->removed[L], n_removed);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) st->edges[L] = (unsigned long long)n_edges;
+}
+
+// FP64 evaluation of the z* candidates queued by the mixed level-L kernel (one thread
+// per entry; entries beyond the queue's capacity were evaluated in the level kernel).
+template <int L>
+__global__ void __launch_bounds__(256) gauss_cand_kernel(const double *__restrict__ C, int p, double tau, double t2,
+                                                        const int *__restrict__ q, long long cap,
+                                                        const unsigned long long *__restrict__ count,
+                                                        double *zmin, double *r2min) {
+    constexpr int W = 3 + L;
+    const long long used = (long long)*count;
+    const long long n = (used < cap ? used : cap) / W;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        eval_candidate<L>(C, p, q + t * W, tau, t2, zmin, r2min);
 }
 
 // ---------------------------------------------------------- level l, any L
@@ -261,11 +289,11 @@ __global__ void unrank_kernel(int K, int L, long long count, int *out) {
 // ------------------------------------------------------------- host launchers
 namespace host {
 
-cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, int *kept, DevState *st,
-                          cudaStream_t s) {
+cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, double *r2min, int *kept,
+                          DevState *st, cudaStream_t s) {
     const int nb = (p + 31) / 32;
     const double t0 = tanh(tau0);
-    gauss_level0_kernel<<<nb * (nb + 1) / 2, 256, 0, s>>>(C, p, tau0, t0 * t0, G, zmin, kept, st);
+    gauss_level0_kernel<<<nb * (nb + 1) / 2, 256, 0, s>>>(C, p, tau0, t0 * t0, G, zmin, r2min, kept, st);
     note_launch(1);
     return cudaGetLastError();
 }
@@ -300,16 +328,34 @@ cudaError_t launch_scan_ll(const long long *cnt, int p, long long *prefix, DevSt
 cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, const int *up, const long long *prefix,
                                double tau, bool tau_valid, uint16_t *G, double *zmin, double *r2min, int *sep_dense,
                                int max_level, int *rec_pool, long long rec_cap, DevState *st, int num_sms,
-                               cudaStream_t s) {
+                               const float *C32, int *qbuf, long long qcap, cudaStream_t s) {
     // register-heavy upper levels run 128-thread blocks so a full wave of warps is resident
     const int threads = L >= 4 ? 128 : 256;
     const int blocks = num_sms * (L >= 4 ? 12 : 8);
     const double th = tanh(tau);
     const double t2 = th * th;  // Z < tau  <=>  rho^2 < tanh(tau)^2 for |rho| < 1
-#define GCSL_LVL(K)                                                                                               \
-    case K:                                                                                                       \
-        gauss_level_reg_kernel<K, 32><<<blocks, threads, 0, s>>>(C, p, adj, up, prefix, tau, t2, tau_valid, G, zmin, \
-                                                                 r2min, sep_dense, max_level, rec_pool, rec_cap, st);\
+    MixArgs mix;
+    mix.C32 = C32;
+    // FP32 bounds of the FP64 knife edge [t2 (1 - 1e-12), t2 (1 + 1e-12)], rounded outward
+    mix.t2lo = nextafterf((float)(t2 * (1.0 - 2e-12)), 0.0f);
+    mix.t2hi = nextafterf((float)(t2 * (1.0 + 2e-12)), 2.0f);
+    mix.q.buf = qbuf;
+    mix.q.cap = qcap;
+    mix.q.count = &st->cand_ints[L < GCSL_MAX_LEVELS ? L : 0];
+    const bool mixed = C32 != nullptr && qbuf != nullptr;
+#define GCSL_LVL(K)                                                                                           \
+    case K:                                                                                                   \
+        if (mixed) {                                                                                          \
+            gauss_level_reg_kernel<K, 32, true><<<blocks, threads, 0, s>>>(C, p, adj, up, prefix, tau, t2,     \
+                                                                           tau_valid, G, zmin, r2min, sep_dense, \
+                                                                           max_level, rec_pool, rec_cap, st, mix); \
+            gauss_cand_kernel<K><<<num_sms * 4, 256, 0, s>>>(C, p, tau, t2, qbuf, qcap, mix.q.count, zmin, r2min); \
+            note_launch(1);                                                                                   \
+        } else {                                                                                              \
+            gauss_level_reg_kernel<K, 32, false><<<blocks, threads, 0, s>>>(C, p, adj, up, prefix, tau, t2,    \
+                                                                            tau_valid, G, zmin, r2min, sep_dense, \
+                                                                            max_level, rec_pool, rec_cap, st, mix); \
+        }                                                                                                     \
         break;
     switch (L) {
         GCSL_LVL(1)
@@ -336,6 +382,19 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
     }
     }
 #undef GCSL_LVL
+    note_launch(1);
+    return cudaGetLastError();
+}
+
+// FP32 copy of an FP64 array (round to nearest).
+__global__ void to_f32_kernel(const double *__restrict__ x, long long n, float *__restrict__ y) {
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        y[k] = (float)x[k];
+}
+
+cudaError_t launch_to_f32(const double *x, long long n, float *y, int num_sms, cudaStream_t s) {
+    const long long want = (n + 255) / 256;
+    to_f32_kernel<<<(int)(want < (long long)num_sms * 8 ? want : (long long)num_sms * 8), 256, 0, s>>>(x, n, y);
     note_launch(1);
     return cudaGetLastError();
 }

@@ -101,6 +101,7 @@ __device__ __forceinline__ bool gauss_test_f32(const float *__restrict__ C32, in
 
 template <int L>
 struct SplitTest {
+    static constexpr bool kMixed = false;
     const double *__restrict__ C;
     const float *__restrict__ C32;
     int p;
@@ -149,7 +150,7 @@ __global__ void batch_level0_kernel(const BInst *__restrict__ inst, const long l
                                     int count) {
     long long lb;
     const BInst &I = inst[inst_of(off_tiles, count, blockIdx.x, lb)];
-    level0_tile(I.C, I.p, I.tau[0], I.t2[0], I.G, I.zmin, I.kept, I.st, (int)lb);
+    level0_tile(I.C, I.p, I.tau[0], I.t2[0], I.G, I.zmin, I.r2min, I.kept, I.st, (int)lb);
 }
 
 // Warp per (instance, row); level 1 compacts G, later levels refilter the lists.

@@ -9,16 +9,18 @@ namespace gcsl {
 
 // ----------------------------------------------------------------- level 0
 // 32 x 32 tiles of the upper triangle (tile row bi <= tile column bj): for i < j,
-// Z = |0.5 log|(1+r)/(1-r)||, r = C[i*p + j]; remove iff Z < tau0.  Kept pairs store
-// z* = Z (NaN ignored) and append i * p + j to `kept`; removed pairs store the marker
-// -1: their z* is final and their pmax is computed from C by pmax_level0_kernel,
-// concurrently with the later levels.
+// Z = |0.5 log|(1+r)/(1-r)||, r = C[i*p + j]; remove iff Z < tau0, decided as
+// r^2 < tanh(tau0)^2 away from the knife edge.  Kept pairs store r^2 in r2min (zmin =
+// +inf; the exact Z only where the reference formula decided) and append i * p + j to
+// `kept`; removed pairs store the marker zmin = -1: their z* is final and their pmax is
+// computed from C by pmax_level0_kernel, concurrently with the later levels.
 // The mirrored skeleton entries are written through a shared-memory transpose so both
 // triangles are stored row-contiguously; zero diagonal.
 // One block of 256 threads per tile; `tile` enumerates the upper-triangle tiles row by row.
 __device__ __forceinline__ void level0_tile(const double *__restrict__ C, int p, double tau0, double t0sq,
                                             uint16_t *__restrict__ G, double *__restrict__ zmin,
-                                            int *__restrict__ kept, DevState *st, int tile) {
+                                            double *__restrict__ r2min, int *__restrict__ kept, DevState *st,
+                                            int tile) {
     __shared__ uint16_t tg[32][33];
     const int nb = (p + 31) / 32;
     int rem = tile, bi = 0;
@@ -41,7 +43,12 @@ __device__ __forceinline__ void level0_tile(const double *__restrict__ C, int p,
             double z = -1.0;  // marker: z* of a level-0 removal is finished on the side stream
             if (r2 < 1.0 && fabs(r2 - t0sq) > 1e-12 * t0sq) {
                 rem0 = r2 < t0sq;
-                if (!rem0) z = fabs(0.5 * log(fabs((1.0 + c) / (1.0 - c))));
+                if (!rem0) {
+                    // kept: r^2 joins the pair's rho^2 minimum; the logarithm is taken once,
+                    // in the pmax kernel, instead of in this (divergent) warp
+                    z = __longlong_as_double(0x7ff0000000000000ll);
+                    r2min[(size_t)i * p + j] = r2;
+                }
             } else {
                 z = fabs(0.5 * log(fabs((1.0 + c) / (1.0 - c))));
                 rem0 = z < tau0;
@@ -184,6 +191,8 @@ struct TestOut {
     double rho2;   // rho^2 when the monotone branch decided, +inf otherwise
     double zexact; // Z from the reference formula when evaluated, +inf otherwise (NaN kept)
     bool remove;
+    bool exact;    // rho2 / zexact hold the FP64 result; else r32 +- e32 encloses FP64 rho^2
+    float r32, e32;
 };
 
 __device__ __forceinline__ double z_of_rho(double rho) {
@@ -206,6 +215,7 @@ __device__ __forceinline__ TestOut gauss_test_reg(const double *__restrict__ C, 
         const double n01 = fma(r, m, -(a * b));
         const double num = n01 * n01, den = fabs(d00) * fabs(d11);
         TestOut o;
+        o.exact = true;
         const double tden = t2 * den;
         if (num < den && fabs(num - tden) > 1e-12 * tden) {
             o.rho2 = num / den;
@@ -247,6 +257,7 @@ __device__ __forceinline__ TestOut gauss_test_reg(const double *__restrict__ C, 
     const double h11 = A[(L + 1) * (L + 2) / 2 + L + 1];
     const double rho2 = (h01 * h01) / (fabs(h00) * fabs(h11));
     TestOut o;
+    o.exact = true;
     if (rho2 < 1.0 && fabs(rho2 - t2) > 1e-12 * t2) {
         o.rho2 = rho2;
         o.zexact = inf;
@@ -350,9 +361,147 @@ __device__ __forceinline__ double group_min(double v) {
     return v;
 }
 
+// The FP64 test out of line: the mixed kernels call it rarely (guard band, unusable
+// bounds, full queue), and keeping it out of their main path keeps its registers out of
+// their register budget.
+template <int L>
+__device__ __noinline__ TestOut gauss_test_reg_call(const double *__restrict__ C, int p, int vi, int vj,
+                                                    const int *S, double tau, double t2) {
+    return gauss_test_reg<L>(C, p, vi, vj, S, tau, t2);
+}
+
+// ------------------------------------------------------- FP32 test with a bound
+// The same elimination in FP32 on the FP32 copy of C, carrying for every entry a
+// first-order bound of its distance to the exact value for the FP64 matrix C:
+// inputs |fl32(c) - c| <= u|c|; a reciprocal, a product and an fma each add u times
+// their result plus the propagated bounds of their operands (u = 2^-24, round to
+// nearest).  rho^2 = H01^2 / (H00 H11) gets the first-order bound of the quotient with
+// the denominators at their lower ends, doubled for the neglected higher-order terms;
+// FP64 rounding of the reference path (~1e-15 relative) is far inside that margin.
+// Returns false (bound unusable) when a pivot or H00 / H11 is not clearly positive,
+// when a relative bound exceeds 1/4, or when rho^2 + bound reaches 0.98.
+constexpr float F32_U = 5.9604645e-08f;  // 2^-24
+
+__device__ __forceinline__ bool f32_rho2_bound(float h00, float e00, float h01, float e01, float h11, float e11,
+                                               float &rho2, float &err) {
+    const float lo00 = h00 - e00, lo11 = h11 - e11;
+    rho2 = (h01 * h01) / (h00 * h11);
+    const float ah = fabsf(h01);
+    err = 2.f * ((2.f * ah * e01 + e01 * e01) / (lo00 * lo11) + rho2 * (e00 / lo00 + e11 / lo11) +
+                 4.f * F32_U * rho2);
+    return e00 < 0.25f * h00 && e11 < 0.25f * h11 && rho2 + err < 0.98f;  // NaN fails
+}
+
+template <int L>
+__device__ __forceinline__ bool gauss_test_f32b(const float *__restrict__ C32, int p, int vi, int vj, const int *S,
+                                                float &rho2, float &err) {
+    const float u = F32_U;
+    if constexpr (L == 1) {
+        const float m = __ldg(C32 + (size_t)S[0] * p + S[0]);
+        const float a = __ldg(C32 + (size_t)vi * p + S[0]);
+        const float b = __ldg(C32 + (size_t)vj * p + S[0]);
+        const float r = __ldg(C32 + (size_t)vi * p + vj);
+        const float em = u * fabsf(m), ea = u * fabsf(a), eb = u * fabsf(b), er = u * fabsf(r);
+        const float d00 = fmaf(-a, a, m), d11 = fmaf(-b, b, m);
+        const float e00 = em + 2.f * fabsf(a) * ea + u * fabsf(d00);
+        const float e11 = em + 2.f * fabsf(b) * eb + u * fabsf(d11);
+        const float ab = a * b;
+        const float eab = fabsf(a) * eb + fabsf(b) * ea + u * fabsf(ab);
+        const float n01 = fmaf(r, m, -ab);
+        const float e01 = fabsf(m) * er + fabsf(r) * em + eab + u * fabsf(n01);
+        return f32_rho2_bound(d00, e00, n01, e01, d11, e11, rho2, err);
+    }
+    constexpr int D = L + 2;
+    float A[D * (D + 1) / 2], E[D * (D + 1) / 2];
+#pragma unroll
+    for (int r = 0; r < L; ++r) {
+        const float *Cr = C32 + (size_t)S[r] * p;
+#pragma unroll
+        for (int c = 0; c <= r; ++c) A[r * (r + 1) / 2 + c] = __ldg(Cr + S[c]);
+        A[L * (L + 1) / 2 + r] = __ldg(C32 + (size_t)vi * p + S[r]);
+        A[(L + 1) * (L + 2) / 2 + r] = __ldg(C32 + (size_t)vj * p + S[r]);
+    }
+    A[L * (L + 1) / 2 + L] = 1.0f;
+    A[(L + 1) * (L + 2) / 2 + L] = __ldg(C32 + (size_t)vi * p + vj);
+    A[(L + 1) * (L + 2) / 2 + L + 1] = 1.0f;
+#pragma unroll
+    for (int k = 0; k < D * (D + 1) / 2; ++k) E[k] = u * fabsf(A[k]);
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+        const float piv = A[j * (j + 1) / 2 + j], ep = E[j * (j + 1) / 2 + j];
+        ok = ok && ep < 0.25f * piv;
+        const float inv = 1.0f / piv;
+        const float einv = ep * inv * inv * 1.5f + u * fabsf(inv);  // 1/(p - e) <= (1 + 1.5 e/p)/p for e < p/4
+#pragma unroll
+        for (int i = j + 1; i < D; ++i) {
+            const float aij = A[i * (i + 1) / 2 + j];
+            const float t = aij * inv;
+            const float et = fabsf(aij) * einv + fabsf(inv) * E[i * (i + 1) / 2 + j] + u * fabsf(t);
+#pragma unroll
+            for (int k = j + 1; k <= i; ++k) {
+                const float akj = A[k * (k + 1) / 2 + j];
+                const float v = fmaf(-t, akj, A[i * (i + 1) / 2 + k]);
+                E[i * (i + 1) / 2 + k] += fabsf(t) * E[k * (k + 1) / 2 + j] + fabsf(akj) * et + u * fabsf(v);
+                A[i * (i + 1) / 2 + k] = v;
+            }
+        }
+    }
+    const int i00 = L * (L + 1) / 2 + L, i01 = (L + 1) * (L + 2) / 2 + L, i11 = (L + 1) * (L + 2) / 2 + L + 1;
+    return f32_rho2_bound(A[i00], E[i00], A[i01], E[i01], A[i11], E[i11], rho2, err) && ok;
+}
+
+// FP32 first: the decision is taken there when the bound puts rho^2 clearly on one side
+// of the FP64 path's knife edge [t2 (1 - 1e-12), t2 (1 + 1e-12)] (t2lo / t2hi are FP32
+// bounds of it, rounded outward); otherwise, or when the bound is unusable, the FP64
+// test runs here and its result is exact.
+template <int L>
+struct MixedTest {
+    static constexpr bool kMixed = true;
+    const double *__restrict__ C;
+    const float *__restrict__ C32;
+    int p;
+    double tau, t2;
+    float t2lo, t2hi;
+    __device__ __forceinline__ TestOut operator()(int vi, int vj, const int *S) const {
+        float r, e;
+        if (gauss_test_f32b<L>(C32, p, vi, vj, S, r, e) && (r + e < t2lo || r - e > t2hi)) {
+            TestOut o;
+            o.rho2 = __longlong_as_double(0x7ff0000000000000ll);
+            o.zexact = o.rho2;
+            o.remove = r + e < t2lo;
+            o.exact = false;
+            o.r32 = r;
+            o.e32 = e;
+            return o;
+        }
+        return gauss_test_reg_call<L>(C, p, vi, vj, S, tau, t2);
+    }
+};
+
+// Deferred FP64 evaluations of level L: entries [pair index lo * p + hi, vi, vj, S...]
+// appended by the level kernel, evaluated densely by the candidate kernel.
+struct CandQueue {
+    int *buf;
+    long long cap;                 // ints
+    unsigned long long *count;     // ints used (may exceed cap: those entries were evaluated inline)
+};
+
+__device__ __forceinline__ void atomic_min_nonneg_f64(double *addr, double v) {
+    atomicMin(reinterpret_cast<unsigned long long *>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
+template <int G>
+__device__ __forceinline__ float group_min_f(float v) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(GCSL_FULL_MASK, v, o));
+    return v;
+}
+
 // The FP64 test of the plain path as a functor for walk_edge.
 template <int L>
 struct F64Test {
+    static constexpr bool kMixed = false;
     const double *__restrict__ C;
     int p;
     double tau, t2;
@@ -366,12 +515,17 @@ struct F64Test {
 // and the keys up to it fold into the group's minima of rho^2 (r2min) and of the exactly
 // evaluated Z (zmin_exact).  Every lane of the warp must call this (warp-wide votes); a
 // lane with has == false takes part without testing.
+//
+// With a mixed (FP32-first) test, keys decided in FP32 carry an interval r32 +- e32
+// around their FP64 rho^2: every such key of the fold whose interval reaches below the
+// smallest upper end in its step could hold the minimum and is queued for the FP64
+// candidate kernel (or evaluated here when the queue is full); exact keys fold directly.
 template <int L, int G, class Test>
 __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int *__restrict__ adj, int p, int gl,
                                           unsigned gshift, unsigned gbits, const Test &test, uint16_t *G_,
                                           int *sep_dense, int max_level, int *rec_pool, long long rec_cap,
                                           DevState *st, double &r2min, double &zmin_exact, bool &removed,
-                                          unsigned long long &n_tests) {
+                                          unsigned long long &n_tests, const CandQueue *q = nullptr) {
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
     bool done = !has || J.T == 0;
     long long base = 0;
@@ -382,12 +536,15 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
         o.rho2 = inf;
         o.zexact = inf;
         o.remove = false;
+        o.exact = true;
         int S[L];
+        int vi = 0, vj = 0;
         if (valid) {
             long long rank;
             int dir;
             key_of(J, m, rank, dir);
-            const int vi = dir ? J.hi : J.lo, vj = dir ? J.lo : J.hi;
+            vi = dir ? J.hi : J.lo;
+            vj = dir ? J.lo : J.hi;
             const int K = (dir ? J.deg_hi : J.deg_lo) - 1;
             int pos[L];
             unrank_positions<L>(K, rank, pos);
@@ -399,11 +556,53 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
         const unsigned bal = (__ballot_sync(GCSL_FULL_MASK, o.remove) >> gshift) & gbits;
         const int first = bal ? (__ffs(bal) - 1) : G;
         const bool fold = valid && gl <= first;
-        const double r2 = group_min<G>(fold ? o.rho2 : inf);
-        const double ze = group_min<G>((fold && !isnan(o.zexact)) ? o.zexact : inf);
+        if constexpr (Test::kMixed) {
+            const float hi = group_min_f<G>((fold && !o.exact) ? o.r32 + o.e32 : __int_as_float(0x7f800000));
+            bool cand = fold && !o.exact && o.r32 - o.e32 <= hi;
+            const unsigned cm = __ballot_sync(GCSL_FULL_MASK, cand);
+            if (cm) {
+                constexpr int W = 3 + L;
+                unsigned long long b0 = 0;
+                const int leader = __ffs(cm) - 1;
+                if ((threadIdx.x & 31) == leader) b0 = atomicAdd(q->count, (unsigned long long)(W * __popc(cm)));
+                b0 = __shfl_sync(GCSL_FULL_MASK, b0, leader);
+                if (cand) {
+                    const unsigned long long at = b0 + (unsigned long long)W * __popc(cm & ((1u << (threadIdx.x & 31)) - 1u));
+                    if ((long long)(at + W) <= q->cap) {
+                        int *e = q->buf + at;
+                        e[0] = J.lo * p + J.hi;
+                        e[1] = vi;
+                        e[2] = vj;
+#pragma unroll
+                        for (int c = 0; c < L; ++c) e[3 + c] = S[c];
+                        cand = false;
+                    }
+                }
+                if (__any_sync(GCSL_FULL_MASK, cand)) {  // queue full: evaluate here
+                    if (cand) {
+                        o = gauss_test_reg_call<L>(test.C, p, vi, vj, S, test.tau, test.t2);
+                        o.remove = false;  // decided already; only the statistic is folded
+                    }
+                }
+            }
+            const bool ex = fold && (o.exact || cand);
+            if (__any_sync(GCSL_FULL_MASK, ex)) {
+                const double r2 = group_min<G>(ex ? o.rho2 : inf);
+                const double ze = group_min<G>((ex && !isnan(o.zexact)) ? o.zexact : inf);
+                if (!done) {
+                    r2min = fmin(r2min, r2);
+                    zmin_exact = fmin(zmin_exact, ze);
+                }
+            }
+        } else {
+            const double r2 = group_min<G>(fold ? o.rho2 : inf);
+            const double ze = group_min<G>((fold && !isnan(o.zexact)) ? o.zexact : inf);
+            if (!done) {
+                r2min = fmin(r2min, r2);
+                zmin_exact = fmin(zmin_exact, ze);
+            }
+        }
         if (!done) {
-            r2min = fmin(r2min, r2);
-            zmin_exact = fmin(zmin_exact, ze);
             const long long left = J.T - base;
             if (gl == 0) n_tests += (unsigned long long)(bal ? first + 1 : (left < G ? left : G));
             if (bal) {
@@ -416,6 +615,19 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
             }
         }
     }
+}
+
+// Candidate kernel body: the FP64 test of queued entry e, folded into the pair's minima.
+template <int L>
+__device__ __forceinline__ void eval_candidate(const double *__restrict__ C, int p, const int *e, double tau,
+                                               double t2, double *zmin, double *r2min) {
+    int S[L];
+#pragma unroll
+    for (int c = 0; c < L; ++c) S[c] = e[3 + c];
+    const TestOut o = gauss_test_reg<L>(C, p, e[1], e[2], S, tau, t2);
+    const size_t ix = (size_t)e[0];
+    if (o.rho2 < __longlong_as_double(0x7ff0000000000000ll)) atomic_min_nonneg_f64(r2min + ix, o.rho2);
+    if (o.zexact < __longlong_as_double(0x7ff0000000000000ll)) atomic_min_nonneg_f64(zmin + ix, o.zexact);
 }
 
 // ------------------------------------------------------------------ p-values

@@ -45,8 +45,7 @@ def main(argv=None):
 
     if args.workload in GAUSS:
         p, n, deg, seed, alpha, maxl = GAUSS[args.workload]
-        X = (torch.from_numpy(gaussian_dag_data(p, n, deg, seed).data).cuda() if p <= 1000
-             else gaussian_dag_data_device(p, n, deg, seed))
+        X = torch.from_numpy(gaussian_dag_data(p, n, deg, seed).data).cuda()
         thr = engine.gaussian_thresholds(n, alpha)
         solver = engine.GaussianSolver(p, min(maxl, p - 2) if p > 2 else 0)
         C = torch.empty((p, p), dtype=torch.float64, device="cuda")
