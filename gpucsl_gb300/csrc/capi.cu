@@ -19,15 +19,24 @@ namespace gcsl {
 namespace host {
 cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, double *r2min, int *kept,
                           DevState *st, cudaStream_t s);
-cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s);
+cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, int2 *elist,
+                           cudaStream_t s);
 cudaError_t launch_scan_int(const int *cnt, int p, long long *prefix, DevState *st, cudaStream_t s);
-cudaError_t launch_recompact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s);
+cudaError_t launch_recompact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, int2 *elist,
+                             cudaStream_t s);
 cudaError_t launch_scan_ll(const long long *cnt, int p, long long *prefix, DevState *st, cudaStream_t s);
-cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, const int *up, const long long *prefix,
-                               double tau, bool tau_valid, uint16_t *G, double *zmin, double *r2min, int *sep_dense,
-                               int max_level, int *rec_pool, long long rec_cap, DevState *st, int num_sms,
-                               const float *C32, int *qbuf, long long qcap, cudaStream_t s);
+cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, const int *up, const int2 *elist,
+                               const long long *prefix, double tau, bool tau_valid, uint16_t *G, double *zmin,
+                               double *r2min, int *sep_dense, int max_level, int *rec_pool, long long rec_cap,
+                               DevState *st, int num_sms, const float *C32, int *qbuf, long long qcap,
+                               cudaStream_t s);
+
 cudaError_t launch_to_f32(const double *x, long long n, float *y, int num_sms, cudaStream_t s);
+cudaError_t launch_cand(int L, const double *C, int p, double tau, double *zmin, double *r2min, const int *qbuf,
+                        long long qcap, DevState *st, int num_sms, cudaStream_t s);
+cudaError_t launch_recompact_cand(int L, const uint16_t *G, int p, int *adj, int *up, DevState *st, int2 *elist,
+                                  const double *C, double tau_prev, double *zmin, double *r2min, const int *qbuf,
+                                  long long qcap, int num_sms, cudaStream_t s);
 cudaError_t launch_pmax(const int *kept, const DevState *st, const double *zmin, const double *r2min, int p,
                         long long n_obs, double *pmax, int num_sms,
                         cudaStream_t s);
@@ -212,11 +221,11 @@ HostCtl *host_ctl() {
     return &c;
 }
 
-// Run levels 1..max_level with the given per-level enqueue function.  Levels are
-// enqueued in batches; between batches the host reads the done flag and the last
-// level's maximum degree d, and since degrees only shrink, level l can only run while
-// d - 1 >= l: the next batch ends at min(d - 1, last + 8), so no level is launched
-// past the termination point once the degrees have settled.
+// Run levels 1..max_level with the given per-level enqueue function.  Every level
+// kernel reads the termination state on the device, so levels are enqueued in batches:
+// level 1 alone, then up to 8 levels per host read of two pinned words (done flag, the
+// last level's maximum degree d).  Degrees only shrink, so level l can only run while
+// d - 1 >= l: a batch never extends past min(d - 1, ...) of the last read.
 template <typename EnqueueLevel>
 int run_levels(int max_level, DevState *d_st, cudaStream_t s, EnqueueLevel enqueue) {
     HostCtl *hc = host_ctl();
@@ -238,8 +247,9 @@ int run_levels(int max_level, DevState *d_st, cudaStream_t s, EnqueueLevel enque
         if (e != cudaSuccess) return GCSL_ERR_DEVICE;
         if (hc->words[0]) break;
         bound = std::min(bound, hc->words[1] - 1);
-        batch = std::min(batch * 2, 8);
-        if (bound - level + 1 <= 8) batch = bound - level + 1;  // finish in one batch when it fits
+        // after the first level, up to 8 levels per host read (a level enqueued past the end
+        // costs four early-exit launches, about as much as a host read)
+        batch = 8;
     }
     if (max_level >= GCSL_MAX_LEVELS && bound >= GCSL_MAX_LEVELS - 1) {
         // levels beyond the state arrays: only an error if the loop had not finished
@@ -257,6 +267,7 @@ struct GaussWs {
     long long *prefix;
     double *zmin, *r2min;
     int *kept;
+    int2 *elist;      // the level's edges (lo, hi)
     float *c32;       // FP32 copy of C for the FP32-first tests
     int *cand;        // FP64 z* candidate queue
     long long cand_cap;
@@ -286,6 +297,7 @@ GaussWs carve_gauss(void *ws, size_t cap, int p) {
     w.zmin = c.take<double>((size_t)p * p);
     w.r2min = c.take<double>((size_t)p * p);
     w.kept = c.take<int>((size_t)p * (p - 1) / 2 + 1);
+    w.elist = c.take<int2>((size_t)p * (p - 1) / 2 + 1);
     w.c32 = c.take<float>((size_t)p * p);
     w.cand_cap = cand_queue_ints(p);
     w.cand = c.take<int>((size_t)w.cand_cap);
@@ -417,23 +429,43 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
         return GCSL_ERR_DEVICE;
     if (host::launch_pmax_level0(C, w.zmin, p, n_obs, pmax, sms, ss->stream) != cudaSuccess) return GCSL_ERR_DEVICE;
     if (cudaEventRecord(ss->join, ss->stream) != cudaSuccess) return GCSL_ERR_DEVICE;
+    int last_enqueued = 0;
     int rc = run_levels(max_level, w.st, s, [&](int level) -> cudaError_t {
         // level 1 compacts the full matrix; later levels only shrink the previous lists
-        cudaError_t e = (level == 1) ? host::launch_compact(G, p, w.adj, w.up, w.st, level, s)
-                                     : host::launch_recompact(G, p, w.adj, w.up, w.st, level, s);
-        if (e == cudaSuccess) e = host::launch_scan_int(w.up, p, w.prefix, w.st, s);
+        // (re)compaction writes the level's edge list (fused with the previous mixed level's
+        // z* candidates); the row prefix is only needed by the shared-memory kernel of
+        // levels above GCSL_GAUSS_REG_LEVELS
+        cudaError_t e;
+        if (level == 1) {
+            e = host::launch_compact(G, p, w.adj, w.up, w.st, level, w.elist, s);
+        } else if (mixed && level - 1 <= GCSL_GAUSS_REG_LEVELS) {
+            const double tau_prev = level - 1 < n_thresholds ? thresholds[level - 1] : 0.0;
+            e = host::launch_recompact_cand(level, G, p, w.adj, w.up, w.st, w.elist, C, tau_prev, w.zmin, w.r2min,
+                                            w.cand, w.cand_cap, sms, s);
+        } else {
+            e = host::launch_recompact(G, p, w.adj, w.up, w.st, level, w.elist, s);
+        }
+        last_enqueued = level;
+        if (e == cudaSuccess && level > GCSL_GAUSS_REG_LEVELS) e = host::launch_scan_int(w.up, p, w.prefix, w.st, s);
         const bool tau_valid = level < n_thresholds;
         const double tau = tau_valid ? thresholds[level] : 0.0;
         if (e == cudaSuccess)
-            e = host::launch_gauss_level(level, C, p, w.adj, w.up, w.prefix, tau, tau_valid, G, w.zmin, w.r2min,
-                                         sepsets, max_level, rec_pool, rec_cap, w.st, sms, mixed ? w.c32 : nullptr,
-                                         mixed ? w.cand : nullptr, w.cand_cap, s);
+            e = host::launch_gauss_level(level, C, p, w.adj, w.up, w.elist, w.prefix, tau, tau_valid, G, w.zmin,
+                                         w.r2min, sepsets, max_level, rec_pool, rec_cap, w.st, sms,
+                                         mixed ? w.c32 : nullptr, mixed ? w.cand : nullptr, w.cand_cap, s);
         if (lt && level + 1 < GCSL_MAX_LEVELS + 2) {
             cudaEventRecord(lt->ev[level + 1], s);
             n_timed = level + 1;
         }
         return e;
     });
+    // the z* candidates of the last enqueued level have no following recompaction
+    if (rc == GCSL_OK && mixed && last_enqueued >= 1 && last_enqueued <= GCSL_GAUSS_REG_LEVELS) {
+        const double tau_last = last_enqueued < n_thresholds ? thresholds[last_enqueued] : 0.0;
+        if (host::launch_cand(last_enqueued, C, p, tau_last, w.zmin, w.r2min, w.cand, w.cand_cap, w.st, sms, s) !=
+            cudaSuccess)
+            return GCSL_ERR_DEVICE;
+    }
     if (cudaStreamWaitEvent(s, ss->join, 0) != cudaSuccess) return GCSL_ERR_DEVICE;
     if (rc != GCSL_OK) return rc;
     if (host::launch_pmax(w.kept, w.st, w.zmin, w.r2min, p, n_obs, pmax, sms, s) != cudaSuccess)
@@ -481,8 +513,9 @@ int gcsl_disc_skeleton(const uint8_t *data, int64_t ld, int64_t n, int32_t p, co
     if (e != cudaSuccess) return GCSL_ERR_DEVICE;
     DiscLevelArgs A{data, ld, n, p, dims, alpha, 0, w.adj, w.prefix, G, pmax, w.win, cap, w.st};
     if (host::launch_disc_tests(A, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    int last_enqueued = 0;
     int rc = run_levels(max_level, w.st, s, [&](int level) -> cudaError_t {
-        cudaError_t e2 = host::launch_compact(G, p, w.adj, nullptr, w.st, level, s);
+        cudaError_t e2 = host::launch_compact(G, p, w.adj, nullptr, w.st, level, nullptr, s);
         if (e2 == cudaSuccess) e2 = host::launch_disc_weights(w.adj, p, level, w.weights, w.st, s);
         if (e2 == cudaSuccess) e2 = host::launch_scan_ll(w.weights, p, w.prefix, w.st, s);
         if (e2 == cudaSuccess) e2 = host::launch_disc_level_stats(w.prefix, w.adj, p, level, w.st, s);
@@ -501,7 +534,7 @@ int gcsl_disc_skeleton(const uint8_t *data, int64_t ld, int64_t n, int32_t p, co
 
 int gcsl_compact(const uint16_t *G, int32_t p, int32_t *adj, void *stream) {
     if (!G || !adj || p < 1) return GCSL_ERR_INVALID_ARG;
-    return map_cuda(host::launch_compact(G, p, adj, nullptr, nullptr, 0, static_cast<cudaStream_t>(stream)));
+    return map_cuda(host::launch_compact(G, p, adj, nullptr, nullptr, 0, nullptr, static_cast<cudaStream_t>(stream)));
 }
 
 int gcsl_unrank(int32_t K, int32_t level, int64_t count, int32_t *out, void *stream) {

@@ -82,12 +82,58 @@ __device__ __forceinline__ long long binom_rt(long long n, int k) {
     return (long long)r;
 }
 
+// Pascal's triangle C(n, k) for n < GCSL_BT_N, k < GCSL_BT_K (saturated at 2^62; ranks
+// at or beyond GCSL_RANK_LIMIT are rejected anyway), built at compile time.  A lookup
+// replaces the multiplicative recurrence in the unranking's binary searches, whose
+// dependent 64-bit multiply / divide chains set the latency of a test step.
+constexpr int GCSL_BT_N = 1024, GCSL_BT_K = 13;
+struct BinomTable {
+    long long v[GCSL_BT_N][GCSL_BT_K];
+};
+constexpr BinomTable make_binom_table() {
+    BinomTable t{};
+    for (int n = 0; n < GCSL_BT_N; ++n) {
+        t.v[n][0] = 1;
+        for (int k = 1; k < GCSL_BT_K; ++k) {
+            const long long a = n > 0 ? t.v[n - 1][k - 1] : 0, b = n > 0 ? t.v[n - 1][k] : 0;
+            const long long cap = 1ll << 62;
+            t.v[n][k] = (a >= cap - b) ? cap : a + b;
+        }
+    }
+    return t;
+}
+static __device__ const BinomTable g_binom = make_binom_table();
+
+template <int KMAX>
+__device__ __forceinline__ long long binom_fast(long long n, int k) {
+    if (k < 0 || n < k) return 0;
+    if (n < GCSL_BT_N && k < GCSL_BT_K) return __ldg(&g_binom.v[n][k]);
+    return KMAX > 0 ? binom_small<KMAX>(n, k) : binom_rt(n, k);
+}
+
+// Rows n < GCSL_SB_N of the table, copied into shared memory by a block that unranks
+// (a binary-search probe then costs a shared-memory load instead of an L2 round trip).
+constexpr int GCSL_SB_N = 128;
+struct BinomRows {
+    long long v[GCSL_SB_N][GCSL_BT_K];
+};
+__device__ __forceinline__ void binom_rows_load(BinomRows &sb) {
+    const long long *src = &g_binom.v[0][0];
+    long long *dst = &sb.v[0][0];
+    for (int k = threadIdx.x; k < GCSL_SB_N * GCSL_BT_K; k += blockDim.x) dst[k] = __ldg(src + k);
+}
+template <int KMAX>
+__device__ __forceinline__ long long binom_rows(const BinomRows *sb, long long n, int k) {
+    if (sb != nullptr && n >= 0 && n < GCSL_SB_N && k >= 0 && k < GCSL_BT_K) return n < k ? 0 : sb->v[n][k];
+    return binom_fast<KMAX>(n, k);
+}
+
 // Lexicographic unranking of `rank` among the L-subsets of {1..K} into 1-based
 // positions (the order of set_helpers.cu:25-49).  Each position is found by a binary
 // search on the hockey-stick identity sum_{u=1..t} C(N-u, r) = C(N, r+1) - C(N-t, r+1),
 // so the cost is O(L^2 log K) instead of the O(L K) walk.
 template <int L>
-__device__ __forceinline__ void unrank_positions(int K, long long rank, int *pos) {
+__device__ __forceinline__ void unrank_positions(int K, long long rank, int *pos, const BinomRows *sb = nullptr) {
     int xprev = 0;
 #pragma unroll
     for (int c = 0; c < L; ++c) {
@@ -96,15 +142,15 @@ __device__ __forceinline__ void unrank_positions(int K, long long rank, int *pos
         if (r == 0) {
             pos[c] = xprev + (int)rank + 1;
         } else {
-            const long long total = binom_small<L>(N, r + 1);
+            const long long total = binom_rows<L>(sb, N, r + 1);
             const long long target = total - rank;  // want smallest t: C(N-t, r+1) < target
             int lo = 1, hi = N - r;                  // t in [1, N-r]
             while (lo < hi) {
                 int mid = (lo + hi) >> 1;
-                if (binom_small<L>(N - mid, r + 1) < target) hi = mid;
+                if (binom_rows<L>(sb, N - mid, r + 1) < target) hi = mid;
                 else lo = mid + 1;
             }
-            rank -= total - binom_small<L>(N - lo + 1, r + 1);
+            rank -= total - binom_rows<L>(sb, N - lo + 1, r + 1);
             xprev += lo;
             pos[c] = xprev;
         }
@@ -120,15 +166,15 @@ __device__ __forceinline__ void unrank_positions_rt(int L, int K, long long rank
         if (r == 0) {
             pos[c] = xprev + (int)rank + 1;
         } else {
-            const long long total = binom_rt(N, r + 1);
+            const long long total = binom_fast<0>(N, r + 1);
             const long long target = total - rank;
             int lo = 1, hi = N - r;
             while (lo < hi) {
                 int mid = (lo + hi) >> 1;
-                if (binom_rt(N - mid, r + 1) < target) hi = mid;
+                if (binom_fast<0>(N - mid, r + 1) < target) hi = mid;
                 else lo = mid + 1;
             }
-            rank -= total - binom_rt(N - lo + 1, r + 1);
+            rank -= total - binom_fast<0>(N - lo + 1, r + 1);
             xprev += lo;
             pos[c] = xprev;
         }

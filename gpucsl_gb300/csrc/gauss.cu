@@ -30,25 +30,40 @@ __global__ void gauss_level0_kernel(const double *__restrict__ C, int p, double 
 // Warp per row (level 1: from G; later levels: refiltering the previous list).  Return at
 // once when the level loop is already finished.
 __global__ void compact_kernel(const uint16_t *__restrict__ G, int p, int *__restrict__ adj, int *__restrict__ up,
-                               DevState *st, int level) {
+                               DevState *st, int level, int2 *elist) {
     if (st != nullptr && st->done) return;
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     int maxdeg = 0;
+    unsigned long long *ecount = (st != nullptr && elist != nullptr) ? &st->edges[level] : nullptr;
     for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p; r += warps)
-        maxdeg = max(maxdeg, compact_row(G, p, adj, up, r, lane));
+        maxdeg = max(maxdeg, compact_row(G, p, adj, up, r, lane, elist, ecount));
     if (lane == 0 && st != nullptr) atomicMax(&st->max_degree[level], maxdeg);
 }
 
-__global__ void recompact_kernel(const uint16_t *__restrict__ G, int p, int *__restrict__ adj, int *__restrict__ up,
-                                 DevState *st, int level) {
+// Recompaction by `nblocks` blocks (block index b) for one level.
+__device__ __forceinline__ void recompact_blocks(const uint16_t *__restrict__ G, int p, int *__restrict__ adj,
+                                                 int *__restrict__ up, DevState *st, int level, int2 *elist, int b,
+                                                 int nblocks) {
     if (st->done) return;
+    if (st->removed[level - 1] == 0) {  // nothing removed: the lists, degrees and edges stand
+        if (b == 0 && threadIdx.x == 0) {
+            st->max_degree[level] = st->max_degree[level - 1];
+            st->edges[level] = st->edges[level - 1];
+        }
+        return;
+    }
     const int lane = threadIdx.x & 31;
-    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int warps = (nblocks * blockDim.x) >> 5;
     int maxdeg = 0;
-    for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p; r += warps)
-        maxdeg = max(maxdeg, recompact_row(G, p, adj, up, r, lane));
+    for (int r = (b * blockDim.x + threadIdx.x) >> 5; r < p; r += warps)
+        maxdeg = max(maxdeg, recompact_row(G, p, adj, up, r, lane, elist, &st->edges[level]));
     if (lane == 0) atomicMax(&st->max_degree[level], maxdeg);
+}
+
+__global__ void recompact_kernel(const uint16_t *__restrict__ G, int p, int *__restrict__ adj, int *__restrict__ up,
+                                 DevState *st, int level, int2 *elist) {
+    recompact_blocks(G, p, adj, up, st, level, elist, (int)blockIdx.x, (int)gridDim.x);
 }
 
 template <typename T>
@@ -70,18 +85,24 @@ struct MixArgs {
 
 template <int L, int G, bool MIXED>
 __global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__restrict__ C, int p,
-                                                             const int *__restrict__ adj, const int *__restrict__ up,
+                                                             const int *__restrict__ adj, const int2 *__restrict__ elist,
                                                              const long long *__restrict__ prefix, double tau,
                                                              double t2, bool tau_valid, uint16_t *G_, double *zmin,
                                                              double *r2min_pair, int *sep_dense, int max_level,
                                                              int *rec_pool, long long rec_cap, DevState *st,
                                                              MixArgs mix) {
+    __shared__ BinomRows sb;
     if (!level_active(st, L, tau_valid)) return;
+    const long long n_edges = (long long)st->edges[L];  // filled by the (re)compaction
+    if ((long long)blockIdx.x * (blockDim.x >> 5) * (32 / G) >= n_edges) return;  // no edge for this block
+    if (L >= 2) {
+        binom_rows_load(sb);
+        __syncthreads();
+    }
     constexpr int GPW = 32 / G;  // groups per warp
     const int lane = threadIdx.x & 31, gl = lane & (G - 1), gw = lane / G;
     const unsigned gshift = (unsigned)(gw * G);
     const unsigned gbits = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
-    const long long n_edges = prefix[p];
     const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
     unsigned long long n_tests = 0, n_full = 0, n_removed = 0;
@@ -91,7 +112,7 @@ __global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__re
         EdgeJob J;
         J.T = 0;
         bool has = e < n_edges;
-        if (has && !load_edge<L>(adj, up, prefix, p, e, L, J)) {
+        if (has && !load_edge_list<L>(adj, elist, p, e, L, J)) {
             if (gl == 0) set_status(st, GCSL_ERR_UNSUPPORTED);
             J.T = 0;
         }
@@ -99,12 +120,16 @@ __global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__re
         double r2min = inf, zmin_exact = inf;
         bool removed = false;
         if constexpr (MIXED) {
+            // the pair's exact rho^2 minimum from earlier levels (level 0 stored r^2)
+            const double floor = (has && J.T > 0) ? r2min_pair[(size_t)J.lo * p + J.hi] : 0.0;
             walk_edge<L, G>(J, has, adj, p, gl, gshift, gbits,
                             MixedTest<L>{C, mix.C32, p, tau, t2, mix.t2lo, mix.t2hi}, G_, sep_dense, max_level,
-                            rec_pool, rec_cap, st, r2min, zmin_exact, removed, n_tests, &mix.q);
+                            rec_pool, rec_cap, st, r2min, zmin_exact, removed, n_tests, &mix.q,
+                            L >= 2 ? &sb : nullptr, floor);
         } else {
             walk_edge<L, G>(J, has, adj, p, gl, gshift, gbits, F64Test<L>{C, p, tau, t2}, G_, sep_dense, max_level,
-                            rec_pool, rec_cap, st, r2min, zmin_exact, removed, n_tests);
+                            rec_pool, rec_cap, st, r2min, zmin_exact, removed, n_tests, nullptr,
+                            L >= 2 ? &sb : nullptr);
         }
         if (has && gl == 0 && J.T > 0) {
             // z* candidates: exact Z into zmin, the monotone branch's min rho^2 into r2min
@@ -120,21 +145,48 @@ __global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__re
         if (n_full) atomicAdd(&st->tests_full[L], n_full);
         if (n_removed) atomicAdd(&st->removed[L], n_removed);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) st->edges[L] = (unsigned long long)n_edges;
 }
 
 // FP64 evaluation of the z* candidates queued by the mixed level-L kernel (one thread
 // per entry; entries beyond the queue's capacity were evaluated in the level kernel).
+// One warp per block: the few thousand entries of a level spread over every SM's FP64
+// pipe instead of filling a handful of SMs.
+struct CandArgs {
+    const double *C;
+    int p;
+    double tau, t2;
+    const int *q;
+    long long cap;
+    const unsigned long long *count;
+    double *zmin, *r2min;
+};
+
 template <int L>
-__global__ void __launch_bounds__(256) gauss_cand_kernel(const double *__restrict__ C, int p, double tau, double t2,
-                                                        const int *__restrict__ q, long long cap,
-                                                        const unsigned long long *__restrict__ count,
-                                                        double *zmin, double *r2min) {
+__device__ __forceinline__ void cand_threads(const CandArgs &a, long long t0, long long stride) {
     constexpr int W = 3 + L;
-    const long long used = (long long)*count;
-    const long long n = (used < cap ? used : cap) / W;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-        eval_candidate<L>(C, p, q + t * W, tau, t2, zmin, r2min);
+    const long long used = (long long)*a.count;
+    const long long n = (used < a.cap ? used : a.cap) / W;
+    for (long long t = t0; t < n; t += stride) eval_candidate<L>(a.C, a.p, a.q + t * W, a.tau, a.t2, a.zmin, a.r2min);
+}
+
+template <int L>
+__global__ void __launch_bounds__(32) gauss_cand_kernel(CandArgs a) {
+    cand_threads<L>(a, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+}
+
+// The candidates of level L and the recompaction of level L + 1 in one launch: blocks
+// [0, rblocks) recompact, the others evaluate candidates; the two touch disjoint data
+// (z* minima versus adjacency), so their latencies overlap.
+template <int L>
+__global__ void __launch_bounds__(256) recompact_cand_kernel(const uint16_t *__restrict__ G, int p,
+                                                            int *__restrict__ adj, int *__restrict__ up, DevState *st,
+                                                            int2 *elist, int rblocks, CandArgs a) {
+    if ((int)blockIdx.x < rblocks) {
+        recompact_blocks(G, p, adj, up, st, L + 1, elist, (int)blockIdx.x, rblocks);
+    } else {
+        const long long cb = (long long)blockIdx.x - rblocks, ncb = (long long)gridDim.x - rblocks;
+        cand_threads<L>(a, cb * blockDim.x + threadIdx.x, ncb * blockDim.x);
+    }
 }
 
 // ---------------------------------------------------------- level l, any L
@@ -298,17 +350,19 @@ cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, doub
     return cudaGetLastError();
 }
 
-cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s) {
+cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, int2 *elist,
+                           cudaStream_t s) {
     const int threads = 256, wpb = threads / 32;
     int blocks = (p + wpb - 1) / wpb;
-    compact_kernel<<<blocks, threads, 0, s>>>(G, p, adj, up, st, level);
+    compact_kernel<<<blocks, threads, 0, s>>>(G, p, adj, up, st, level, elist);
     note_launch(1);
     return cudaGetLastError();
 }
 
-cudaError_t launch_recompact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, cudaStream_t s) {
+cudaError_t launch_recompact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, int2 *elist,
+                             cudaStream_t s) {
     const int threads = 256, wpb = threads / 32;
-    recompact_kernel<<<(p + wpb - 1) / wpb, threads, 0, s>>>(G, p, adj, up, st, level);
+    recompact_kernel<<<(p + wpb - 1) / wpb, threads, 0, s>>>(G, p, adj, up, st, level, elist);
     note_launch(1);
     return cudaGetLastError();
 }
@@ -325,10 +379,11 @@ cudaError_t launch_scan_ll(const long long *cnt, int p, long long *prefix, DevSt
     return cudaGetLastError();
 }
 
-cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, const int *up, const long long *prefix,
-                               double tau, bool tau_valid, uint16_t *G, double *zmin, double *r2min, int *sep_dense,
-                               int max_level, int *rec_pool, long long rec_cap, DevState *st, int num_sms,
-                               const float *C32, int *qbuf, long long qcap, cudaStream_t s) {
+cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, const int *up, const int2 *elist,
+                               const long long *prefix, double tau, bool tau_valid, uint16_t *G, double *zmin,
+                               double *r2min, int *sep_dense, int max_level, int *rec_pool, long long rec_cap,
+                               DevState *st, int num_sms, const float *C32, int *qbuf, long long qcap,
+                               cudaStream_t s) {
     // register-heavy upper levels run 128-thread blocks so a full wave of warps is resident
     const int threads = L >= 4 ? 128 : 256;
     const int blocks = num_sms * (L >= 4 ? 12 : 8);
@@ -346,13 +401,11 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
 #define GCSL_LVL(K)                                                                                           \
     case K:                                                                                                   \
         if (mixed) {                                                                                          \
-            gauss_level_reg_kernel<K, 32, true><<<blocks, threads, 0, s>>>(C, p, adj, up, prefix, tau, t2,     \
+            gauss_level_reg_kernel<K, 32, true><<<blocks, threads, 0, s>>>(C, p, adj, elist, prefix, tau, t2,  \
                                                                            tau_valid, G, zmin, r2min, sep_dense, \
                                                                            max_level, rec_pool, rec_cap, st, mix); \
-            gauss_cand_kernel<K><<<num_sms * 4, 256, 0, s>>>(C, p, tau, t2, qbuf, qcap, mix.q.count, zmin, r2min); \
-            note_launch(1);                                                                                   \
         } else {                                                                                              \
-            gauss_level_reg_kernel<K, 32, false><<<blocks, threads, 0, s>>>(C, p, adj, up, prefix, tau, t2,    \
+            gauss_level_reg_kernel<K, 32, false><<<blocks, threads, 0, s>>>(C, p, adj, elist, prefix, tau, t2, \
                                                                             tau_valid, G, zmin, r2min, sep_dense, \
                                                                             max_level, rec_pool, rec_cap, st, mix); \
         }                                                                                                     \
@@ -382,6 +435,57 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
     }
     }
 #undef GCSL_LVL
+    note_launch(1);
+    return cudaGetLastError();
+}
+
+static CandArgs cand_args(int L, const double *C, int p, double tau, double *zmin, double *r2min, const int *qbuf,
+                          long long qcap, DevState *st) {
+    const double th = tanh(tau);
+    CandArgs a;
+    a.C = C;
+    a.p = p;
+    a.tau = tau;
+    a.t2 = th * th;
+    a.q = qbuf;
+    a.cap = qcap;
+    a.count = &st->cand_ints[L];
+    a.zmin = zmin;
+    a.r2min = r2min;
+    return a;
+}
+
+// FP64 z* candidates of mixed level L (1 <= L <= GCSL_GAUSS_REG_LEVELS) on their own.
+cudaError_t launch_cand(int L, const double *C, int p, double tau, double *zmin, double *r2min, const int *qbuf,
+                        long long qcap, DevState *st, int num_sms, cudaStream_t s) {
+    const CandArgs a = cand_args(L, C, p, tau, zmin, r2min, qbuf, qcap, st);
+    switch (L) {
+#define GCSL_CAND(K) \
+    case K: gauss_cand_kernel<K><<<num_sms * 16, 32, 0, s>>>(a); break;
+        GCSL_CAND(1) GCSL_CAND(2) GCSL_CAND(3) GCSL_CAND(4) GCSL_CAND(5) GCSL_CAND(6)
+        GCSL_CAND(7) GCSL_CAND(8) GCSL_CAND(9) GCSL_CAND(10) GCSL_CAND(11) GCSL_CAND(12)
+#undef GCSL_CAND
+    default: return cudaSuccess;
+    }
+    note_launch(1);
+    return cudaGetLastError();
+}
+
+// Candidates of level L - 1 fused with the recompaction of level L (2 <= L <= 13).
+cudaError_t launch_recompact_cand(int L, const uint16_t *G, int p, int *adj, int *up, DevState *st, int2 *elist,
+                                  const double *C, double tau_prev, double *zmin, double *r2min, const int *qbuf,
+                                  long long qcap, int num_sms, cudaStream_t s) {
+    const int wpb = 256 / 32, rblocks = (p + wpb - 1) / wpb;
+    const int grid = rblocks + num_sms * 2;
+    const CandArgs a = cand_args(L - 1, C, p, tau_prev, zmin, r2min, qbuf, qcap, st);
+    switch (L - 1) {
+#define GCSL_RC(K) \
+    case K: recompact_cand_kernel<K><<<grid, 256, 0, s>>>(G, p, adj, up, st, elist, rblocks, a); break;
+        GCSL_RC(1) GCSL_RC(2) GCSL_RC(3) GCSL_RC(4) GCSL_RC(5) GCSL_RC(6)
+        GCSL_RC(7) GCSL_RC(8) GCSL_RC(9) GCSL_RC(10) GCSL_RC(11) GCSL_RC(12)
+#undef GCSL_RC
+    default: return cudaErrorInvalidValue;
+    }
     note_launch(1);
     return cudaGetLastError();
 }

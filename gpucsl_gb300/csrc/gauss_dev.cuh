@@ -90,8 +90,22 @@ __device__ __forceinline__ void level0_tile(const double *__restrict__ C, int p,
 // One warp compacts row r: adj[r*p] = degree, adj[r*p + 1 ..] = ascending neighbour ids
 // (entries past the degree keep stale values, as in the reference); also writes
 // up[r] = #neighbours > r.  Returns the degree.
+// The row's edges to larger ids, (r, j) for its last `ups` neighbours, appended to the
+// level's edge list at slots reserved with one atomic per row (the list order does not
+// matter: a test warp owns its edge).
+__device__ __forceinline__ void emit_row_edges(const int *row, int cnt, int ups, int r, int lane,
+                                               int2 *__restrict__ elist, unsigned long long *ecount) {
+    if (elist == nullptr || ups == 0) return;
+    __syncwarp();  // the row's entries are written
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(ecount, (unsigned long long)ups);
+    base = __shfl_sync(GCSL_FULL_MASK, base, 0);
+    for (int k = lane; k < ups; k += 32) elist[base + k] = make_int2(r, row[1 + cnt - ups + k]);
+}
+
 __device__ __forceinline__ int compact_row(const uint16_t *__restrict__ G, int p, int *__restrict__ adj,
-                                           int *__restrict__ up, int r, int lane) {
+                                           int *__restrict__ up, int r, int lane, int2 *elist = nullptr,
+                                           unsigned long long *ecount = nullptr) {
     {
         const uint16_t *Gr = G + (size_t)r * p;
         int *row = adj + (size_t)r * p;
@@ -108,15 +122,17 @@ __device__ __forceinline__ int compact_row(const uint16_t *__restrict__ G, int p
             row[0] = cnt;
             if (up != nullptr) up[r] = ups;
         }
+        emit_row_edges(row, cnt, ups, r, lane, elist, ecount);
         return cnt;
     }
 }
 
 // Levels >= 2: one warp refilters row r's previous neighbour list against G (rows only
-// shrink, so this touches deg entries instead of p) and writes up[r]; the row scan then
-// rebuilds the edge prefix.  Returns the degree.
+// shrink, so this touches deg entries instead of p), writes up[r] and, when given, the
+// row's edges.  Returns the degree.
 __device__ __forceinline__ int recompact_row(const uint16_t *__restrict__ G, int p, int *__restrict__ adj,
-                                             int *__restrict__ up, int r, int lane) {
+                                             int *__restrict__ up, int r, int lane, int2 *elist = nullptr,
+                                             unsigned long long *ecount = nullptr) {
     {
         int *row = adj + (size_t)r * p;
         const int deg = row[0];
@@ -135,6 +151,7 @@ __device__ __forceinline__ int recompact_row(const uint16_t *__restrict__ G, int
             row[0] = cnt;
             up[r] = ups;
         }
+        emit_row_edges(row, cnt, ups, r, lane, elist, ecount);
         return cnt;
     }
 }
@@ -291,8 +308,26 @@ __device__ __forceinline__ bool load_edge(const int *__restrict__ adj, const int
     J.deg_lo = deg;
     J.deg_hi = adj[(size_t)j * p];
     const int K0 = J.deg_lo - 1, K1 = J.deg_hi - 1;
-    J.R0 = (K0 >= L) ? (KMAX > 0 ? binom_small<KMAX>(K0, L) : binom_rt(K0, L)) : 0;
-    J.R1 = (K1 >= L) ? (KMAX > 0 ? binom_small<KMAX>(K1, L) : binom_rt(K1, L)) : 0;
+    J.R0 = (K0 >= L) ? binom_fast<KMAX>(K0, L) : 0;
+    J.R1 = (K1 >= L) ? binom_fast<KMAX>(K1, L) : 0;
+    J.T = J.R0 + J.R1;
+    J.Rmin = J.R0 < J.R1 ? J.R0 : J.R1;
+    J.longer = J.R0 > J.R1 ? 0 : 1;
+    return J.R0 < GCSL_RANK_LIMIT && J.R1 < GCSL_RANK_LIMIT;
+}
+
+// Edge e of the level from the explicit edge list (lo < hi) written by the edge scan.
+template <int KMAX>
+__device__ __forceinline__ bool load_edge_list(const int *__restrict__ adj, const int2 *__restrict__ elist, int p,
+                                               long long e, int L, EdgeJob &J) {
+    const int2 ed = elist[e];
+    J.lo = ed.x;
+    J.hi = ed.y;
+    J.deg_lo = adj[(size_t)ed.x * p];
+    J.deg_hi = adj[(size_t)ed.y * p];
+    const int K0 = J.deg_lo - 1, K1 = J.deg_hi - 1;
+    J.R0 = (K0 >= L) ? binom_fast<KMAX>(K0, L) : 0;
+    J.R1 = (K1 >= L) ? binom_fast<KMAX>(K1, L) : 0;
     J.T = J.R0 + J.R1;
     J.Rmin = J.R0 < J.R1 ? J.R0 : J.R1;
     J.longer = J.R0 > J.R1 ? 0 : 1;
@@ -465,11 +500,11 @@ struct MixedTest {
     float t2lo, t2hi;
     __device__ __forceinline__ TestOut operator()(int vi, int vj, const int *S) const {
         float r, e;
-        if (gauss_test_f32b<L>(C32, p, vi, vj, S, r, e) && (r + e < t2lo || r - e > t2hi)) {
+        if (gauss_test_f32b<L>(C32, p, vi, vj, S, r, e) && (__fadd_ru(r, e) < t2lo || __fsub_rd(r, e) > t2hi)) {
             TestOut o;
             o.rho2 = __longlong_as_double(0x7ff0000000000000ll);
             o.zexact = o.rho2;
-            o.remove = r + e < t2lo;
+            o.remove = __fadd_ru(r, e) < t2lo;
             o.exact = false;
             o.r32 = r;
             o.e32 = e;
@@ -517,15 +552,17 @@ struct F64Test {
 // lane with has == false takes part without testing.
 //
 // With a mixed (FP32-first) test, keys decided in FP32 carry an interval r32 +- e32
-// around their FP64 rho^2: every such key of the fold whose interval reaches below the
-// smallest upper end in its step could hold the minimum and is queued for the FP64
-// candidate kernel (or evaluated here when the queue is full); exact keys fold directly.
+// around their FP64 rho^2: every such key of the fold whose interval reaches below both
+// the smallest upper end in its step and the pair's minimum from earlier levels could
+// hold the minimum and is queued for the FP64 candidate kernel (or evaluated here when
+// the queue is full); exact keys fold directly.
 template <int L, int G, class Test>
 __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int *__restrict__ adj, int p, int gl,
                                           unsigned gshift, unsigned gbits, const Test &test, uint16_t *G_,
                                           int *sep_dense, int max_level, int *rec_pool, long long rec_cap,
                                           DevState *st, double &r2min, double &zmin_exact, bool &removed,
-                                          unsigned long long &n_tests, const CandQueue *q = nullptr) {
+                                          unsigned long long &n_tests, const CandQueue *q = nullptr,
+                                          const BinomRows *sb = nullptr, double r2_floor = 0.0) {
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
     bool done = !has || J.T == 0;
     long long base = 0;
@@ -547,7 +584,7 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
             vj = dir ? J.lo : J.hi;
             const int K = (dir ? J.deg_hi : J.deg_lo) - 1;
             int pos[L];
-            unrank_positions<L>(K, rank, pos);
+            unrank_positions<L>(K, rank, pos, sb);
             const int *nbrs = adj + (size_t)vi * p + 1;
 #pragma unroll
             for (int c = 0; c < L; ++c) S[c] = resolve_position(nbrs, vj, pos[c]);
@@ -557,8 +594,11 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
         const int first = bal ? (__ffs(bal) - 1) : G;
         const bool fold = valid && gl <= first;
         if constexpr (Test::kMixed) {
-            const float hi = group_min_f<G>((fold && !o.exact) ? o.r32 + o.e32 : __int_as_float(0x7f800000));
-            bool cand = fold && !o.exact && o.r32 - o.e32 <= hi;
+            // interval ends rounded outward; a key whose interval starts above the pair's
+            // exact minimum so far (r2_floor, from earlier levels) cannot lower z*
+            const float lo32 = __fsub_rd(o.r32, o.e32);
+            const float hi = group_min_f<G>((fold && !o.exact) ? __fadd_ru(o.r32, o.e32) : __int_as_float(0x7f800000));
+            bool cand = fold && !o.exact && lo32 <= hi && (double)lo32 <= r2_floor;
             const unsigned cm = __ballot_sync(GCSL_FULL_MASK, cand);
             if (cm) {
                 constexpr int W = 3 + L;
