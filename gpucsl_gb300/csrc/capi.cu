@@ -18,7 +18,8 @@
 namespace gcsl {
 namespace host {
 cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, double *r2min, int *kept,
-                          DevState *st, cudaStream_t s);
+                          DevState *st, float *C32, cudaStream_t s);
+cudaError_t launch_sf_table(double *out, cudaStream_t s);
 cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, int2 *elist,
                            cudaStream_t s);
 cudaError_t launch_scan_int(const int *cnt, int p, long long *prefix, DevState *st, cudaStream_t s);
@@ -38,9 +39,10 @@ cudaError_t launch_recompact_cand(int L, const uint16_t *G, int p, int *adj, int
                                   const double *C, double tau_prev, double *zmin, double *r2min, const int *qbuf,
                                   long long qcap, int num_sms, cudaStream_t s);
 cudaError_t launch_pmax(const int *kept, const DevState *st, const double *zmin, const double *r2min, int p,
-                        long long n_obs, double *pmax, int num_sms,
+                        long long n_obs, const double *sftab, double *pmax, int num_sms,
                         cudaStream_t s);
-cudaError_t launch_pmax_level0(const double *C, const double *zmin, int p, long long n_obs, double *pmax,
+cudaError_t launch_pmax_level0(const double *C, const double *zmin, int p, long long n_obs, const double *sftab,
+                               double *pmax,
                                int num_sms, cudaStream_t s);
 size_t corr_workspace_bytes(long long n, int p);
 cudaError_t corr_f64(const void *X, int dtype, long long n, int p, long long ldx, double *C, void *ws,
@@ -269,6 +271,7 @@ struct GaussWs {
     int *kept;
     int2 *elist;      // the level's edges (lo, hi)
     float *c32;       // FP32 copy of C for the FP32-first tests
+    double *sftab;    // erfc Taylor table of the pmax kernels
     int *cand;        // FP64 z* candidate queue
     long long cand_cap;
     size_t bytes;
@@ -299,6 +302,7 @@ GaussWs carve_gauss(void *ws, size_t cap, int p) {
     w.kept = c.take<int>((size_t)p * (p - 1) / 2 + 1);
     w.elist = c.take<int2>((size_t)p * (p - 1) / 2 + 1);
     w.c32 = c.take<float>((size_t)p * p);
+    w.sftab = c.take<double>(32 * 13);
     w.cand_cap = cand_queue_ints(p);
     w.cand = c.take<int>((size_t)w.cand_cap);
     w.bytes = c.off;
@@ -415,8 +419,8 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
     int n_timed = 0;  // events recorded: ev[0 .. n_timed]
     if (lt) cudaEventRecord(lt->ev[0], s);
     const bool mixed = mixed_tests() && max_level >= 1;
-    if (mixed && host::launch_to_f32(C, (long long)p * p, w.c32, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
-    if (host::launch_level0(C, p, thresholds[0], G, w.zmin, w.r2min, w.kept, w.st, s) != cudaSuccess)
+    if (host::launch_level0(C, p, thresholds[0], G, w.zmin, w.r2min, w.kept, w.st, mixed ? w.c32 : nullptr, s) !=
+        cudaSuccess)
         return GCSL_ERR_DEVICE;
     if (lt) {
         cudaEventRecord(lt->ev[1], s);
@@ -427,7 +431,9 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
     if (!ss) return GCSL_ERR_DEVICE;
     if (cudaEventRecord(ss->fork, s) != cudaSuccess || cudaStreamWaitEvent(ss->stream, ss->fork, 0) != cudaSuccess)
         return GCSL_ERR_DEVICE;
-    if (host::launch_pmax_level0(C, w.zmin, p, n_obs, pmax, sms, ss->stream) != cudaSuccess) return GCSL_ERR_DEVICE;
+    if (host::launch_sf_table(w.sftab, ss->stream) != cudaSuccess ||
+        host::launch_pmax_level0(C, w.zmin, p, n_obs, w.sftab, pmax, sms, ss->stream) != cudaSuccess)
+        return GCSL_ERR_DEVICE;
     if (cudaEventRecord(ss->join, ss->stream) != cudaSuccess) return GCSL_ERR_DEVICE;
     int last_enqueued = 0;
     int rc = run_levels(max_level, w.st, s, [&](int level) -> cudaError_t {
@@ -468,7 +474,7 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
     }
     if (cudaStreamWaitEvent(s, ss->join, 0) != cudaSuccess) return GCSL_ERR_DEVICE;
     if (rc != GCSL_OK) return rc;
-    if (host::launch_pmax(w.kept, w.st, w.zmin, w.r2min, p, n_obs, pmax, sms, s) != cudaSuccess)
+    if (host::launch_pmax(w.kept, w.st, w.zmin, w.r2min, p, n_obs, w.sftab, pmax, sms, s) != cudaSuccess)
         return GCSL_ERR_DEVICE;
     const int frc = finish_stats(w.st, stats, s, false, p);
     if (lt) {

@@ -22,8 +22,8 @@ namespace gcsl {
 // ----------------------------------------------------------------- level 0
 __global__ void gauss_level0_kernel(const double *__restrict__ C, int p, double tau0, double t0sq,
                                     uint16_t *__restrict__ G, double *__restrict__ zmin, double *__restrict__ r2min,
-                                    int *__restrict__ kept, DevState *st) {
-    level0_tile(C, p, tau0, t0sq, G, zmin, r2min, kept, st, (int)blockIdx.x);
+                                    int *__restrict__ kept, DevState *st, float *C32) {
+    level0_tile(C, p, tau0, t0sq, G, zmin, r2min, kept, st, (int)blockIdx.x, C32);
 }
 
 // ------------------------------------------------------------- compaction
@@ -292,14 +292,22 @@ __global__ void __launch_bounds__(128) gauss_level_smem_kernel(const double *__r
 // pmax_ij = 2 * sf(sqrt(n - 3) * z*_ij) for i < j (0 when z* = +inf), -1 elsewhere.
 // 2 sf(x) = erfc(x / sqrt 2), written as scipy's ndtr does it (erf below 1/sqrt 2).
 // Grid: (column blocks of 256, rows); no index division.
+// The erfc Taylor table of the pmax kernels, built once per solve by one warp.
+__global__ void sf_table_kernel(double *__restrict__ out) {
+    __shared__ double tab[SF_CENTRES][SF_TERMS];
+    sf_table_build(tab);
+    __syncthreads();
+    for (int k = threadIdx.x; k < SF_CENTRES * SF_TERMS; k += blockDim.x) out[k] = (&tab[0][0])[k];
+}
+
 // Pairs kept at level 0 (the list the level-0 kernel appended): z* = min(zmin, Z of the
 // smallest rho^2 any later level stored), pmax = 2 sf(sqrt(n - 3) z*)
 // (helpers.py:62-82 with the FP64 z*).
 __global__ void pmax_kept_kernel(const int *__restrict__ kept, const DevState *__restrict__ st,
                                  const double *__restrict__ zmin, const double *__restrict__ r2min, double sqrt_nm3,
-                                 double *__restrict__ pmax) {
+                                 const double *__restrict__ sftab, double *__restrict__ pmax) {
     __shared__ double tab[SF_CENTRES][SF_TERMS];
-    sf_table_build(tab);
+    sf_table_load(tab, sftab);
     __syncthreads();
     const int count = st->n_kept;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
@@ -316,9 +324,9 @@ __global__ void pmax_kept_kernel(const int *__restrict__ kept, const DevState *_
 // a second stream right after level 0; the later levels never touch these entries, so it
 // runs concurrently with them.
 __global__ void pmax_level0_kernel(const double *__restrict__ C, const double *__restrict__ zmin, int p,
-                                   double sqrt_nm3, double *__restrict__ pmax) {
+                                   double sqrt_nm3, const double *__restrict__ sftab, double *__restrict__ pmax) {
     __shared__ double tab[SF_CENTRES][SF_TERMS];
-    sf_table_build(tab);
+    sf_table_load(tab, sftab);
     __syncthreads();
     const unsigned total = (unsigned)p * (unsigned)p;  // p <= 46340: fits in 31 bits
     for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
@@ -342,10 +350,10 @@ __global__ void unrank_kernel(int K, int L, long long count, int *out) {
 namespace host {
 
 cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, double *zmin, double *r2min, int *kept,
-                          DevState *st, cudaStream_t s) {
+                          DevState *st, float *C32, cudaStream_t s) {
     const int nb = (p + 31) / 32;
     const double t0 = tanh(tau0);
-    gauss_level0_kernel<<<nb * (nb + 1) / 2, 256, 0, s>>>(C, p, tau0, t0 * t0, G, zmin, r2min, kept, st);
+    gauss_level0_kernel<<<nb * (nb + 1) / 2, 256, 0, s>>>(C, p, tau0, t0 * t0, G, zmin, r2min, kept, st, C32);
     note_launch(1);
     return cudaGetLastError();
 }
@@ -510,22 +518,29 @@ cudaError_t launch_unrank(int K, int L, long long count, int *out, cudaStream_t 
     return cudaGetLastError();
 }
 
-cudaError_t launch_pmax_level0(const double *C, const double *zmin, int p, long long n_obs, double *pmax,
-                               int num_sms, cudaStream_t s) {
+cudaError_t launch_sf_table(double *out, cudaStream_t s) {
+    sf_table_kernel<<<1, 32, 0, s>>>(out);
+    note_launch(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pmax_level0(const double *C, const double *zmin, int p, long long n_obs, const double *sftab,
+                               double *pmax, int num_sms, cudaStream_t s) {
     const long long total = (long long)p * p;
     const long long want = (total + 255) / 256;
     const int blocks = (int)(want < (long long)num_sms * 4 ? want : (long long)num_sms * 4);
-    pmax_level0_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(C, zmin, p, sqrt((double)(n_obs - 3)), pmax);
+    pmax_level0_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(C, zmin, p, sqrt((double)(n_obs - 3)), sftab, pmax);
     note_launch(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pmax(const int *kept, const DevState *st, const double *zmin, const double *r2min, int p,
-                        long long n_obs, double *pmax, int num_sms, cudaStream_t s) {
+                        long long n_obs, const double *sftab, double *pmax, int num_sms, cudaStream_t s) {
     const long long pairs = (long long)p * (p - 1) / 2;
     const long long want = (pairs + 255) / 256;
     const int blocks = (int)(want < (long long)num_sms * 2 ? want : (long long)num_sms * 2);
-    pmax_kept_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(kept, st, zmin, r2min, sqrt((double)(n_obs - 3)), pmax);
+    pmax_kept_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(kept, st, zmin, r2min, sqrt((double)(n_obs - 3)), sftab,
+                                                             pmax);
     note_launch(1);
     return cudaGetLastError();
 }

@@ -132,8 +132,10 @@ __device__ __forceinline__ int inst_of(const long long *__restrict__ off, int co
 }
 
 // Per p^2 chunk: r2min = 1.4e306 (above every stored rho^2); chunk 0 also clears the
-// instance's DevState.
-__global__ void batch_init_kernel(const BInst *__restrict__ inst, const long long *__restrict__ off_p2, int count) {
+// instance's DevState; block 0 builds the erfc table of the pmax kernels.
+__global__ void batch_init_kernel(const BInst *__restrict__ inst, const long long *__restrict__ off_p2, int count,
+                                  double *__restrict__ sftab) {
+    if (blockIdx.x == 0) sf_table_build(reinterpret_cast<double (*)[SF_TERMS]>(sftab));  // erfc table for pmax
     long long lb;
     const BInst &I = inst[inst_of(off_p2, count, blockIdx.x, lb)];
     const long long total = (long long)I.p * I.p;
@@ -255,9 +257,9 @@ __global__ void __launch_bounds__(256) batch_level_kernel(const BInst *__restric
 
 // pmax of the pairs removed at level 0 and the -1 fill, per p^2 chunk.
 __global__ void batch_pmax_removed_kernel(const BInst *__restrict__ inst, const long long *__restrict__ off_p2,
-                                          int count) {
+                                          int count, const double *__restrict__ sftab) {
     __shared__ double tab[SF_CENTRES][SF_TERMS];
-    sf_table_build(tab);
+    sf_table_load(tab, sftab);
     __syncthreads();
     long long lb;
     const BInst &I = inst[inst_of(off_p2, count, blockIdx.x, lb)];
@@ -272,9 +274,9 @@ __global__ void batch_pmax_removed_kernel(const BInst *__restrict__ inst, const 
 }
 
 // pmax of the pairs kept at level 0, block per instance.
-__global__ void batch_pmax_kept_kernel(const BInst *__restrict__ inst) {
+__global__ void batch_pmax_kept_kernel(const BInst *__restrict__ inst, const double *__restrict__ sftab) {
     __shared__ double tab[SF_CENTRES][SF_TERMS];
-    sf_table_build(tab);
+    sf_table_load(tab, sftab);
     __syncthreads();
     const BInst &I = inst[blockIdx.x];
     const int n = I.st->n_kept;
@@ -293,7 +295,7 @@ namespace host {
 namespace {
 
 struct BatchLayout {
-    size_t table, off_tiles, off_rows, off_p2, edges, edge_off, slices, total;
+    size_t table, off_tiles, off_rows, off_p2, edges, edge_off, sftab, slices, total;
 };
 
 size_t al(size_t x) { return (x + 255) / 256 * 256; }
@@ -320,6 +322,8 @@ BatchLayout layout(const int *p, int count) {
     off += al((size_t)count * sizeof(long long));
     L.edge_off = off;
     off += al(((size_t)count + 1) * sizeof(long long));
+    L.sftab = off;
+    off += al((size_t)SF_CENTRES * SF_TERMS * sizeof(double));
     L.slices = off;
     for (int k = 0; k < count; ++k) off += slice_bytes(p[k]);
     L.total = off;
@@ -472,14 +476,16 @@ int gauss_batch_run(const long long *plan, cudaStream_t s) {
     Ly.off_p2 = Ly.off_rows + al(((size_t)count + 1) * sizeof(long long));
     Ly.edges = Ly.off_p2 + al(((size_t)count + 1) * sizeof(long long));
     Ly.edge_off = Ly.edges + al((size_t)count * sizeof(long long));
+    Ly.sftab = Ly.edge_off + al(((size_t)count + 1) * sizeof(long long));
     const BInst *inst = reinterpret_cast<const BInst *>(base + Ly.table);
     const long long *ot = reinterpret_cast<const long long *>(base + Ly.off_tiles);
     const long long *orow = reinterpret_cast<const long long *>(base + Ly.off_rows);
     const long long *op2 = reinterpret_cast<const long long *>(base + Ly.off_p2);
     long long *edges = reinterpret_cast<long long *>(base + Ly.edges);
     long long *eoff = reinterpret_cast<long long *>(base + Ly.edge_off);
+    double *sftab = reinterpret_cast<double *>(base + Ly.sftab);
 
-    batch_init_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count);
+    batch_init_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count, sftab);
     batch_level0_kernel<<<(unsigned)plan[PW_TILES], 256, 0, s>>>(inst, ot, count);
     note_launch(2);
     const long long rows = plan[PW_ROWS];
@@ -494,8 +500,8 @@ int gauss_batch_run(const long long *plan, cudaStream_t s) {
                                     : launch_level<false>(level, lanes, inst, eoff, count, sms, s);
         if (e != cudaSuccess) return GCSL_ERR_DEVICE;
     }
-    batch_pmax_removed_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count);
-    batch_pmax_kept_kernel<<<count, 256, 0, s>>>(inst);
+    batch_pmax_removed_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count, sftab);
+    batch_pmax_kept_kernel<<<count, 256, 0, s>>>(inst, sftab);
     note_launch(2);
     return cudaGetLastError() == cudaSuccess ? GCSL_OK : GCSL_ERR_DEVICE;
 }

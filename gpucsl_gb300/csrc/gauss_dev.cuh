@@ -20,8 +20,9 @@ namespace gcsl {
 __device__ __forceinline__ void level0_tile(const double *__restrict__ C, int p, double tau0, double t0sq,
                                             uint16_t *__restrict__ G, double *__restrict__ zmin,
                                             double *__restrict__ r2min, int *__restrict__ kept, DevState *st,
-                                            int tile) {
+                                            int tile, float *__restrict__ C32 = nullptr) {
     __shared__ uint16_t tg[32][33];
+    __shared__ float tc[32][33];
     const int nb = (p + 31) / 32;
     int rem = tile, bi = 0;
     while (rem >= nb - bi) {
@@ -34,8 +35,13 @@ __device__ __forceinline__ void level0_tile(const double *__restrict__ C, int p,
     for (int r = ty; r < 32; r += 8) {
         const int i = bi * 32 + r, j = bj * 32 + tx;
         uint16_t g = 0;
+        if (C32 != nullptr && i == j && i < p) C32[(size_t)i * p + i] = (float)__ldg(C + (size_t)i * p + i);
         if (i < p && j < p && i < j) {
             const double c = __ldg(C + (size_t)i * p + j);
+            if (C32 != nullptr) {  // the FP32 copy of C for the FP32-first levels, both triangles
+                C32[(size_t)i * p + j] = (float)c;
+                tc[r][tx] = (float)c;
+            }
             // Z0 = atanh-like in |r| on [0, 1): Z0 < tau0 <=> r^2 < tanh(tau0)^2; the knife
             // edge, |r| >= 1 and NaN take the reference formula
             const double r2 = c * c;
@@ -73,12 +79,18 @@ __device__ __forceinline__ void level0_tile(const double *__restrict__ C, int p,
     if (bi != bj) {
         for (int r = ty; r < 32; r += 8) {
             const int j = bj * 32 + r, i = bi * 32 + tx;  // lower triangle (j, i), j > i
-            if (i < p && j < p) G[(size_t)j * p + i] = tg[tx][r];
+            if (i < p && j < p) {
+                G[(size_t)j * p + i] = tg[tx][r];
+                if (C32 != nullptr) C32[(size_t)j * p + i] = tc[tx][r];
+            }
         }
     } else {
         for (int r = ty; r < 32; r += 8) {
             const int j = bj * 32 + r, i = bi * 32 + tx;
-            if (i < p && j < p && j > i) G[(size_t)j * p + i] = tg[tx][r];
+            if (i < p && j < p && j > i) {
+                G[(size_t)j * p + i] = tg[tx][r];
+                if (C32 != nullptr) C32[(size_t)j * p + i] = tc[tx][r];
+            }
         }
     }
 #pragma unroll
@@ -110,13 +122,35 @@ __device__ __forceinline__ int compact_row(const uint16_t *__restrict__ G, int p
         const uint16_t *Gr = G + (size_t)r * p;
         int *row = adj + (size_t)r * p;
         int cnt = 0, ups = 0;
-        for (int c0 = 0; c0 < p; c0 += 32) {
-            const int c = c0 + lane;
-            const bool e = (c < p) && (c != r) && (Gr[c] != 0);
-            const unsigned b = __ballot_sync(GCSL_FULL_MASK, e);
-            if (e) row[1 + cnt + __popc(b & ((1u << lane) - 1))] = c;
-            cnt += __popc(b);
-            ups += __popc(__ballot_sync(GCSL_FULL_MASK, e && c > r));
+        // 256 columns per pass, 8 consecutive ones per lane (independent loads), positions
+        // from a warp prefix sum of the lanes' counts
+        for (int c0 = 0; c0 < p; c0 += 256) {
+            const int cb = c0 + lane * 8;
+            unsigned m = 0;
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int c = cb + t;
+                if (c < p && c != r && Gr[c] != 0) m |= 1u << t;
+            }
+            const int nb = __popc(m);
+            int x = nb;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(GCSL_FULL_MASK, x, o);
+                if (lane >= o) x += y;
+            }
+            int pos = cnt + x - nb;
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+                if ((m >> t) & 1u) row[1 + pos++] = cb + t;
+            cnt += __shfl_sync(GCSL_FULL_MASK, x, 31);
+            // neighbours above r: the bits of columns > r
+            const int above = r - cb;  // bits t > above count
+            const unsigned mu = above >= 7 ? 0u : (above < 0 ? m : (m & ~((2u << above) - 1u)));
+            int u = __popc(mu);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) u += __shfl_xor_sync(GCSL_FULL_MASK, u, o);
+            ups += u;
         }
         if (lane == 0) {
             row[0] = cnt;
@@ -694,6 +728,12 @@ __device__ __forceinline__ void sf_table_build(double (*a)[SF_TERMS]) {
             b = bn;
         }
     }
+}
+
+// The table built once per solve (sf_table_kernel) copied into a block's shared memory.
+__device__ __forceinline__ void sf_table_load(double (*a)[SF_TERMS], const double *__restrict__ g) {
+    double *dst = &a[0][0];
+    for (int k = threadIdx.x; k < SF_CENTRES * SF_TERMS; k += blockDim.x) dst[k] = __ldg(g + k);
 }
 
 __device__ __forceinline__ double two_sf_tab(double z, const double (*a)[SF_TERMS]) {
