@@ -36,6 +36,7 @@ EXPORTED = [
     "gcsl_gauss_batch_workspace_bytes", "gcsl_gauss_batch_prepare", "gcsl_gauss_batch_run",
     "gcsl_gauss_batch_collect", "gcsl_gauss_batch_set_lanes",
     "gcsl_corr_tc_batch_workspace_bytes", "gcsl_corr_tc_batch_prepare", "gcsl_corr_tc_batch_run",
+    "gcsl_orient_workspace_bytes", "gcsl_orient_edges",
 ]
 
 GCSL_PREC_F64 = 0
@@ -186,6 +187,10 @@ def lib() -> ct.CDLL:
                                              ct.POINTER(BatchPlan), _vp]
     L.gcsl_corr_tc_batch_run.restype = ct.c_int
     L.gcsl_corr_tc_batch_run.argtypes = [ct.POINTER(BatchPlan), _vp]
+    L.gcsl_orient_workspace_bytes.restype = _sz
+    L.gcsl_orient_workspace_bytes.argtypes = [_i32]
+    L.gcsl_orient_edges.restype = ct.c_int
+    L.gcsl_orient_edges.argtypes = [_vp, _i32, _vp, _i32, _vp, ct.POINTER(_i32), _vp, _sz, _vp]
     if L.gcsl_version() != 1:
         raise RuntimeError("libgpucsl_gb300.so ABI version mismatch")
     return L

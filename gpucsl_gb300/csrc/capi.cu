@@ -33,6 +33,9 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
                                cudaStream_t s);
 
 cudaError_t launch_to_f32(const double *x, long long n, float *y, int num_sms, cudaStream_t s);
+size_t orient_workspace_bytes(int p);
+cudaError_t orient_edges(const uint16_t *S, int p, const int *sep, int L, uint8_t *D, void *ws, int num_sms,
+                         int *host_word, int *passes, cudaStream_t s);
 cudaError_t launch_cand(int L, const double *C, int p, double tau, double *zmin, double *r2min, const int *qbuf,
                         long long qcap, DevState *st, int num_sms, cudaStream_t s);
 cudaError_t launch_recompact_cand(int L, const uint16_t *G, int p, int *adj, int *up, DevState *st, int2 *elist,
@@ -668,6 +671,27 @@ int gcsl_corr_tc_batch_run(const gcsl_batch_plan *plan, void *stream) {
     if (w[0] != kCorrPlanMagic) return GCSL_ERR_INVALID_ARG;
     return map_cuda(host::corr_tc_batch_run(reinterpret_cast<void *>(static_cast<uintptr_t>(w[1])), (int)w[2], w + 4,
                                             (int)w[3], static_cast<cudaStream_t>(stream)));
+}
+
+
+// ---------------------------------------------------------------- orientation
+size_t gcsl_orient_workspace_bytes(int32_t p) {
+    if (p < 1 || p > GCSL_GAUSS_MAX_P) return 0;
+    return host::orient_workspace_bytes(p);
+}
+
+int gcsl_orient_edges(const uint16_t *G, int32_t p, const int32_t *sepsets, int32_t sep_len, uint8_t *dag,
+                      int32_t *passes, void *workspace, size_t workspace_bytes, void *stream) {
+    if (!G || !dag || p < 1 || sep_len < 0 || (sep_len > 0 && !sepsets)) return GCSL_ERR_INVALID_ARG;
+    if (p > GCSL_GAUSS_MAX_P) return GCSL_ERR_UNSUPPORTED;
+    if (!workspace || workspace_bytes < host::orient_workspace_bytes(p)) return GCSL_ERR_WORKSPACE;
+    HostCtl *hc = host_ctl();
+    if (!hc) return GCSL_ERR_DEVICE;
+    int n = 0;
+    const cudaError_t e = host::orient_edges(G, p, sepsets, sep_len, dag, workspace, device_sms(), &hc->words[0], &n,
+                                             static_cast<cudaStream_t>(stream));
+    if (passes) *passes = n;
+    return map_cuda(e);
 }
 
 }  // extern "C"

@@ -36,14 +36,12 @@ class PC(ABC):
 
     @timed
     def execute(self):
-        """Skeleton on the GPU, then edge orientation (pc.py:50-68)."""
-        import networkx as nx
-
-        from .edge_orientation.edge_orientation import orient_edges
+        """Skeleton on the GPU, then edge orientation, also on the GPU (pc.py:50-68)."""
+        from .edge_orientation.edge_orientation import orient_edges_gpu
 
         ((skeleton, separation_sets, pmax, discover_skeleton_kernel_time), discover_skeleton_time) = \
             self.discover_skeleton()
-        (directed_graph, edge_orientation_time) = orient_edges(nx.DiGraph(skeleton), separation_sets)
+        (directed_graph, edge_orientation_time) = orient_edges_gpu(skeleton, separation_sets)
         return PCResult(directed_graph, separation_sets, pmax, discover_skeleton_time, edge_orientation_time,
                         discover_skeleton_kernel_time)
 

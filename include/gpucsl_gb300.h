@@ -120,6 +120,21 @@ int gcsl_gauss_skeleton_noalloc(const double *C, int32_t p, int64_t n_obs, const
                                 int32_t n_thresholds, int32_t max_level, uint16_t *G, int32_t *sepsets,
                                 int32_t *rec_pool, int64_t rec_cap, double *pmax, gcsl_stats *stats, void *stream);
 
+/* Edge orientation of a skeleton (replaces orient_edges, gpucsl/pc/edge_orientation/
+ * edge_orientation.py:25-36: v-structures (v_structures.py:8-35), then Meek's rules
+ * R1-R3 to a fixed point (orientation_rules.py:7-89)), with the result of the reference's
+ * sequential visiting order.
+ *   G        device p x p uint16 skeleton (symmetric, zero diagonal)
+ *   sepsets  device p x p x sep_len int32 separating sets, -1 padded (the reference's
+ *            dense layout), or NULL with sep_len = 0
+ *   dag      device p x p uint8 out: dag[a * p + b] = 1 for the edge a -> b (an undirected
+ *            edge has both directions)
+ *   passes   optional host out: rule passes run (the last one changed nothing)
+ * Synchronises `stream` once per rule pass. */
+size_t gcsl_orient_workspace_bytes(int32_t p);
+int gcsl_orient_edges(const uint16_t *G, int32_t p, const int32_t *sepsets, int32_t sep_len, uint8_t *dag,
+                      int32_t *passes, void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---------------------------------------------------------------- batches
  * Many independent Gaussian skeletons solved together (no counterpart in the reference,
  * whose drivers solve one problem per call: discover_skeleton_gaussian.py:116-172).
