@@ -24,6 +24,9 @@ GCSL_ERR_UNSUPPORTED = 7
 GCSL_MAX_LEVELS = 64
 GCSL_DTYPE_F64 = 0
 GCSL_DTYPE_F32 = 1
+GCSL_DTYPE_I32 = 2
+GCSL_DTYPE_I64 = 3
+GCSL_DTYPE_U8 = 4
 
 # every symbol the header declares (checked by the CPU test-suite)
 EXPORTED = [
@@ -36,7 +39,7 @@ EXPORTED = [
     "gcsl_gauss_batch_workspace_bytes", "gcsl_gauss_batch_prepare", "gcsl_gauss_batch_run",
     "gcsl_gauss_batch_collect", "gcsl_gauss_batch_set_lanes",
     "gcsl_corr_tc_batch_workspace_bytes", "gcsl_corr_tc_batch_prepare", "gcsl_corr_tc_batch_run",
-    "gcsl_orient_workspace_bytes", "gcsl_orient_edges",
+    "gcsl_orient_workspace_bytes", "gcsl_orient_edges", "gcsl_encode_workspace_bytes", "gcsl_ordinal_encode",
 ]
 
 GCSL_PREC_F64 = 0
@@ -187,6 +190,10 @@ def lib() -> ct.CDLL:
                                              ct.POINTER(BatchPlan), _vp]
     L.gcsl_corr_tc_batch_run.restype = ct.c_int
     L.gcsl_corr_tc_batch_run.argtypes = [ct.POINTER(BatchPlan), _vp]
+    L.gcsl_encode_workspace_bytes.restype = _sz
+    L.gcsl_encode_workspace_bytes.argtypes = []
+    L.gcsl_ordinal_encode.restype = ct.c_int
+    L.gcsl_ordinal_encode.argtypes = [_vp, _i32, _i64, _i32, _i64, _vp, _i64, _vp, _vp, _sz, _vp]
     L.gcsl_orient_workspace_bytes.restype = _sz
     L.gcsl_orient_workspace_bytes.argtypes = [_i32]
     L.gcsl_orient_edges.restype = ct.c_int

@@ -208,6 +208,31 @@ class DiscreteSolver:
         return G, sep, pmax
 
 
+def ordinal_encode_device(X, ld: int | None = None):
+    """Device ordinal encoding (gcsl_ordinal_encode) of an (n, p) integer-valued device
+    tensor (int32, int64, uint8, or float64 holding integers): returns (codes (p, ld)
+    uint8 column-major device tensor, ld = n rounded up to 16 by default, dims (p,) uint8
+    device tensor).  Raises GcslError (unsupported) for a column with more than 255
+    distinct values or a value range of 4096 or more."""
+    torch = _torch()
+    if X.dim() != 2:
+        raise ValueError("X must be 2-D (samples x variables)")
+    dt = {torch.int32: _lib.GCSL_DTYPE_I32, torch.int64: _lib.GCSL_DTYPE_I64, torch.uint8: _lib.GCSL_DTYPE_U8,
+          torch.float64: _lib.GCSL_DTYPE_F64}.get(X.dtype)
+    if dt is None:
+        raise ValueError(f"unsupported dtype {X.dtype}")
+    X = X.contiguous()
+    n, p = X.shape
+    ld = (n + 15) // 16 * 16 if ld is None else int(ld)
+    codes = torch.zeros((p, ld), dtype=torch.uint8, device=X.device)
+    dims = torch.empty(p, dtype=torch.uint8, device=X.device)
+    L = _lib.lib()
+    ws = torch.empty(int(L.gcsl_encode_workspace_bytes()), dtype=torch.uint8, device=X.device)
+    _lib.check(L.gcsl_ordinal_encode(X.data_ptr(), dt, n, p, p, codes.data_ptr(), ld, dims.data_ptr(), ws.data_ptr(),
+                                     ws.numel(), _lib.stream_ptr()), "gcsl_ordinal_encode")
+    return codes, dims
+
+
 def ordinal_encode(data: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     """Per-column codes 0..k-1 over the observed values in sorted order, and k per column
     (the OrdinalEncoder + max+1 of discover_skeleton_discrete.py:38-39, 49).

@@ -35,6 +35,9 @@ extern "C" {
 #define GCSL_MAX_LEVELS 64
 #define GCSL_DTYPE_F64 0
 #define GCSL_DTYPE_F32 1
+#define GCSL_DTYPE_I32 2
+#define GCSL_DTYPE_I64 3
+#define GCSL_DTYPE_U8 4
 
 /* Per-level counters returned to the host. */
 typedef struct gcsl_stats {
@@ -119,6 +122,19 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
 int gcsl_gauss_skeleton_noalloc(const double *C, int32_t p, int64_t n_obs, const double *thresholds,
                                 int32_t n_thresholds, int32_t max_level, uint16_t *G, int32_t *sepsets,
                                 int32_t *rec_pool, int64_t rec_cap, double *pmax, gcsl_stats *stats, void *stream);
+
+/* Ordinal encoding of discrete samples on the device (replaces the host OrdinalEncoder
+ * and dims of gpucsl/pc/discover_skeleton_discrete.py:38-49): per column the observed
+ * values, ascending, get codes 0..k-1 and dims[j] = k.
+ *   X      device n x p samples, row stride ld elements, dtype GCSL_DTYPE_I32 / I64 / U8,
+ *          or F64 holding integers
+ *   codes  device out, column j at codes + j * ldc (the layout gcsl_disc_skeleton reads)
+ *   dims   device p uint8 out
+ * A column with more than 255 distinct values, a value range of 4096 or more, or a
+ * non-integer value returns GCSL_ERR_UNSUPPORTED.  Synchronises `stream`. */
+size_t gcsl_encode_workspace_bytes(void);
+int gcsl_ordinal_encode(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ld, uint8_t *codes, int64_t ldc,
+                        uint8_t *dims, void *workspace, size_t workspace_bytes, void *stream);
 
 /* Edge orientation of a skeleton (replaces orient_edges, gpucsl/pc/edge_orientation/
  * edge_orientation.py:25-36: v-structures (v_structures.py:8-35), then Meek's rules
