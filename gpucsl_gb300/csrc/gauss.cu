@@ -393,8 +393,11 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
                                DevState *st, int num_sms, const float *C32, int *qbuf, long long qcap,
                                cudaStream_t s) {
     // register-heavy upper levels run 128-thread blocks so a full wave of warps is resident
+    // level 1 (tens of thousands of edges) strides over the edges with many blocks; the
+    // upper levels have a few thousand edges, one warp each: one resident wave of blocks,
+    // so no empty blocks queue behind the working ones
     const int threads = L >= 4 ? 128 : 256;
-    const int blocks = num_sms * (L >= 4 ? 12 : 8);
+    const int blocks = L == 1 ? num_sms * 8 : num_sms * (L >= 4 ? 4 : 2);
     const double th = tanh(tau);
     const double t2 = th * th;  // Z < tau  <=>  rho^2 < tanh(tau)^2 for |rho| < 1
     MixArgs mix;
@@ -484,7 +487,7 @@ cudaError_t launch_recompact_cand(int L, const uint16_t *G, int p, int *adj, int
                                   const double *C, double tau_prev, double *zmin, double *r2min, const int *qbuf,
                                   long long qcap, int num_sms, cudaStream_t s) {
     const int wpb = 256 / 32, rblocks = (p + wpb - 1) / wpb;
-    const int grid = rblocks + num_sms * 2;
+    const int grid = rblocks + num_sms / 2;
     const CandArgs a = cand_args(L - 1, C, p, tau_prev, zmin, r2min, qbuf, qcap, st);
     switch (L - 1) {
 #define GCSL_RC(K) \
