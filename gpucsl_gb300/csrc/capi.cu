@@ -40,9 +40,6 @@ cudaError_t orient_edges(const uint16_t *S, int p, const int *sep, int L, uint8_
                          int *host_word, int *passes, cudaStream_t s);
 cudaError_t launch_cand(int L, const double *C, int p, double tau, double *zmin, double *r2min, const int *qbuf,
                         long long qcap, DevState *st, int num_sms, cudaStream_t s);
-cudaError_t launch_recompact_cand(int L, const uint16_t *G, int p, int *adj, int *up, DevState *st, int2 *elist,
-                                  const double *C, double tau_prev, double *zmin, double *r2min, const int *qbuf,
-                                  long long qcap, int num_sms, cudaStream_t s);
 cudaError_t launch_pmax(const int *kept, const DevState *st, const double *zmin, const double *r2min, int p,
                         long long n_obs, const double *sftab, double *pmax, int num_sms,
                         cudaStream_t s);
@@ -53,6 +50,7 @@ size_t corr_workspace_bytes(long long n, int p);
 cudaError_t corr_f64(const void *X, int dtype, long long n, int p, long long ldx, double *C, void *ws,
                      size_t ws_bytes, int num_sms, cudaStream_t s);
 int disc_table_cap(int device);
+void disc_level_caps(int cap_full, int max_dim, int L, int &table_cap, int &part_cap);
 cudaError_t launch_disc_tests(const DiscLevelArgs &A, int num_sms, cudaStream_t s);
 cudaError_t launch_disc_weights(const int *adj, int p, int L, long long *w, DevState *st, cudaStream_t s);
 cudaError_t launch_disc_finalize(const int *adj, int p, int L, uint16_t *G, unsigned long long *win, int *sep,
@@ -138,6 +136,7 @@ int map_cuda(cudaError_t e) {
 struct SideStream {
     cudaStream_t stream = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEvent_t level[GCSL_GAUSS_REG_LEVELS + 1] = {};  // level l's tests done (candidate hand-off)
 };
 
 // Per-level device timing (gcsl_stats.level_ms) when GCSL_LEVEL_TIMING=1: one event per
@@ -181,6 +180,8 @@ SideStream *side_stream() {
         if (cudaStreamCreateWithPriority(&s.stream, cudaStreamNonBlocking, lo) != cudaSuccess) return nullptr;
         if (cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming) != cudaSuccess) return nullptr;
         if (cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+        for (cudaEvent_t &e : s.level)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
     }
     return &s;
 }
@@ -285,6 +286,10 @@ struct GaussWs {
 // Ints of the z* candidate queue: entries hold 3 + level ints, about one or two per edge
 // and level; a full queue only moves evaluations back into the level kernel.
 long long cand_queue_ints(int p) { return std::max<long long>(1ll << 20, 4ll * p * p); }
+
+// The queue holds one region per register level (1 .. GCSL_GAUSS_REG_LEVELS), so a
+// level's candidates can still be waiting on the side stream while the next levels append.
+long long cand_region_ints(long long cap) { return cap / GCSL_GAUSS_REG_LEVELS; }
 
 // FP32-first level tests (default) or FP64 throughout (GCSL_F64_TESTS=1, for comparisons).
 bool mixed_tests() {
@@ -439,45 +444,38 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
     if (host::launch_sf_table(w.sftab, ss->stream) != cudaSuccess ||
         host::launch_pmax_level0(C, w.zmin, p, n_obs, w.sftab, pmax, sms, ss->stream) != cudaSuccess)
         return GCSL_ERR_DEVICE;
-    if (cudaEventRecord(ss->join, ss->stream) != cudaSuccess) return GCSL_ERR_DEVICE;
-    int last_enqueued = 0;
+    const long long region = cand_region_ints(w.cand_cap);
     int rc = run_levels(max_level, w.st, s, [&](int level) -> cudaError_t {
-        // level 1 compacts the full matrix; later levels only shrink the previous lists
-        // (re)compaction writes the level's edge list (fused with the previous mixed level's
-        // z* candidates); the row prefix is only needed by the shared-memory kernel of
-        // levels above GCSL_GAUSS_REG_LEVELS
-        cudaError_t e;
-        if (level == 1) {
-            e = host::launch_compact(G, p, w.adj, w.up, w.st, level, w.elist, s);
-        } else if (mixed && level - 1 <= GCSL_GAUSS_REG_LEVELS) {
-            const double tau_prev = level - 1 < n_thresholds ? thresholds[level - 1] : 0.0;
-            e = host::launch_recompact_cand(level, G, p, w.adj, w.up, w.st, w.elist, C, tau_prev, w.zmin, w.r2min,
-                                            w.cand, w.cand_cap, sms, s);
-        } else {
-            e = host::launch_recompact(G, p, w.adj, w.up, w.st, level, w.elist, s);
-        }
-        last_enqueued = level;
+        // level 1 compacts the full matrix; later levels only shrink the previous lists;
+        // (re)compaction writes the level's edge list; the row prefix is only needed by
+        // the shared-memory kernel of levels above GCSL_GAUSS_REG_LEVELS
+        cudaError_t e = level == 1 ? host::launch_compact(G, p, w.adj, w.up, w.st, level, w.elist, s)
+                                   : host::launch_recompact(G, p, w.adj, w.up, w.st, level, w.elist, s);
         if (e == cudaSuccess && level > GCSL_GAUSS_REG_LEVELS) e = host::launch_scan_int(w.up, p, w.prefix, w.st, s);
         const bool tau_valid = level < n_thresholds;
         const double tau = tau_valid ? thresholds[level] : 0.0;
+        const bool cand = mixed && level <= GCSL_GAUSS_REG_LEVELS;
+        int *qbuf = cand ? w.cand + (size_t)(level - 1) * region : nullptr;
         if (e == cudaSuccess)
             e = host::launch_gauss_level(level, C, p, w.adj, w.up, w.elist, w.prefix, tau, tau_valid, G, w.zmin,
                                          w.r2min, sepsets, max_level, rec_pool, rec_cap, w.st, sms,
-                                         mixed ? w.c32 : nullptr, mixed ? w.cand : nullptr, w.cand_cap, s);
+                                         mixed ? w.c32 : nullptr, qbuf, region, s);
+        // the level's FP64 z* candidates only feed pmax: they run on the low-priority side
+        // stream while the next levels proceed
+        if (e == cudaSuccess && cand) {
+            e = cudaEventRecord(ss->level[level], s);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(ss->stream, ss->level[level], 0);
+            if (e == cudaSuccess)
+                e = host::launch_cand(level, C, p, tau, w.zmin, w.r2min, qbuf, region, w.st, sms, ss->stream);
+        }
         if (lt && level + 1 < GCSL_MAX_LEVELS + 2) {
             cudaEventRecord(lt->ev[level + 1], s);
             n_timed = level + 1;
         }
         return e;
     });
-    // the z* candidates of the last enqueued level have no following recompaction
-    if (rc == GCSL_OK && mixed && last_enqueued >= 1 && last_enqueued <= GCSL_GAUSS_REG_LEVELS) {
-        const double tau_last = last_enqueued < n_thresholds ? thresholds[last_enqueued] : 0.0;
-        if (host::launch_cand(last_enqueued, C, p, tau_last, w.zmin, w.r2min, w.cand, w.cand_cap, w.st, sms, s) !=
-            cudaSuccess)
-            return GCSL_ERR_DEVICE;
-    }
-    if (cudaStreamWaitEvent(s, ss->join, 0) != cudaSuccess) return GCSL_ERR_DEVICE;
+    if (cudaEventRecord(ss->join, ss->stream) != cudaSuccess || cudaStreamWaitEvent(s, ss->join, 0) != cudaSuccess)
+        return GCSL_ERR_DEVICE;
     if (rc != GCSL_OK) return rc;
     if (host::launch_pmax(w.kept, w.st, w.zmin, w.r2min, p, n_obs, w.sftab, pmax, sms, s) != cudaSuccess)
         return GCSL_ERR_DEVICE;
@@ -522,7 +520,8 @@ int gcsl_disc_skeleton(const uint8_t *data, int64_t ld, int64_t n, int32_t p, co
     if (e == cudaSuccess) e = cudaMemsetAsync(pmax, 0, sizeof(double) * (size_t)p * p, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(G, 0, sizeof(uint16_t) * (size_t)p * p, s);
     if (e != cudaSuccess) return GCSL_ERR_DEVICE;
-    DiscLevelArgs A{data, ld, n, p, dims, alpha, 0, w.adj, w.prefix, G, pmax, w.win, cap, w.st};
+    DiscLevelArgs A{data, ld, n, p, dims, alpha, 0, w.adj, w.prefix, G, pmax, w.win, cap, 1024, w.st};
+    host::disc_level_caps(cap, max_dim, 0, A.table_cap, A.part_cap);
     if (host::launch_disc_tests(A, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
     int last_enqueued = 0;
     int rc = run_levels(max_level, w.st, s, [&](int level) -> cudaError_t {
@@ -532,6 +531,7 @@ int gcsl_disc_skeleton(const uint8_t *data, int64_t ld, int64_t n, int32_t p, co
         if (e2 == cudaSuccess) e2 = host::launch_disc_level_stats(w.prefix, w.adj, p, level, w.st, s);
         DiscLevelArgs B = A;
         B.level = level;
+        host::disc_level_caps(cap, max_dim, level, B.table_cap, B.part_cap);
         if (e2 == cudaSuccess) e2 = host::launch_disc_tests(B, sms, s);
         if (e2 == cudaSuccess)
             e2 = host::launch_disc_finalize(w.adj, p, level, G, w.win, sepsets, max_level, rec_pool, rec_cap, w.st,

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <cmath>
 #include <stdint.h>
 
 #include "../../include/gpucsl_gb300.h"
@@ -23,6 +24,36 @@ void note_launch(int kernels);
 // for gcsl_last_error) and returns e.
 cudaError_t note_error(const char *where, cudaError_t e);
 }  // namespace host
+
+// Level-0 decision bounds on the bit pattern of |r| (non-negative doubles order like
+// their bit patterns): |r| < lo removes and hi <= |r| < one keeps without any FP64
+// arithmetic; everything else (the knife edge around tanh(tau0), |r| >= 1, NaN) takes
+// the reference's logarithm.  lo and hi leave a band of 2e-12 relative in r^2 around
+// tanh(tau0)^2, wider than the band inside which r^2 < tanh(tau0)^2 and the logarithm
+// can disagree.
+struct L0Bounds {
+    unsigned long long lo, hi, one;
+};
+
+__host__ inline L0Bounds level0_bounds(double t0sq) {
+    // first b in [0, bits of 1.0] with fl(x(b)^2) > target (monotone in b)
+    auto first_above = [](double target) {
+        unsigned long long a = 0, b = 0x3ff0000000000000ull;
+        while (a < b) {
+            const unsigned long long m = a + (b - a) / 2;
+            double x;
+            __builtin_memcpy(&x, &m, 8);
+            if (x * x > target) b = m;
+            else a = m + 1;
+        }
+        return a;
+    };
+    L0Bounds B;
+    B.lo = t0sq > 0.0 ? first_above(t0sq * (1.0 - 2e-12)) : 0ull;  // t0sq = 0 removes nothing
+    B.hi = first_above(t0sq * (1.0 + 2e-12));
+    B.one = first_above(std::nextafter(1.0, 0.0));  // fl(x^2) < 1 below it
+    return B;
+}
 
 // Device-side state of one skeleton solve.  Per-level slots are written once per
 // level, so no counter has to be reset between levels.
@@ -54,7 +85,8 @@ struct DiscLevelArgs {
     uint16_t *G;
     double *pmax;
     unsigned long long *win;  // canonical remover key per (lo, hi)
-    int table_cap;            // max counters of one table copy in shared memory
+    int table_cap;            // counters of shared memory for the table and its replicas
+    int part_cap;             // strata of the per-stratum statistic buffer (after the table)
     DevState *st;
 };
 

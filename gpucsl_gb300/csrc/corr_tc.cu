@@ -61,7 +61,6 @@ struct OzJob {
 
 // Kernel stages of a job; each has its own count of blocks per job.
 enum OzStage { OZ_INIT = 0, OZ_STATS, OZ_MEAN, OZ_DIGITS, OZ_PRODUCT, OZ_DIAG, OZ_FINISH, OZ_NSTAGES };
-constexpr int OZ_FINISH_ENTRIES = 1024;  // entries of C per finish block (4 per thread)
 
 // Where a kernel finds its job: one job passed by value (block b of the stage is block b
 // of the job), or a device table of jobs with each stage's exclusive block offsets
@@ -500,31 +499,44 @@ __global__ void ozaki_diag_kernel(Src src) {
     if (i < J.p) J.inv_sd[i] = 1.0 / sqrt(oz_cov(J.phi, J.plo, J.D, J.expo, scale, i, i));
 }
 
-// C_ij = clip(cov_ij / s_i / s_j, -1, 1) for i <= j, written to both triangles (the
-// normalisation of numpy's corrcoef, with reciprocals of the standard deviations).
-// C_ij = clip(cov_ij / s_i / s_j, -1, 1) for i <= j, written to both triangles (the
-// normalisation of numpy's corrcoef, with reciprocals of the standard deviations), and
-// to the FP32 copy when the job has one.  A block covers OZ_FINISH_ENTRIES entries.
+// C_ij = clip(cov_ij / s_i / s_j, -1, 1) (the normalisation of numpy's corrcoef, with
+// reciprocals of the standard deviations), for one 32 x 32 tile of the upper triangle
+// per block; the mirrored tile is written through shared memory so both triangles are
+// stored row-contiguously, and the FP32 copy the same way when the job has one.
 template <class Src>
 __global__ void ozaki_finish_kernel(Src src) {
+    __shared__ double tv[32][33];
     long long lb;
     const OzJob &J = src.get(blockIdx.x, lb);
     const int p = J.p;
-    const long long total = (long long)p * p;
+    const int nb = (p + 31) / 32;
+    int rem = (int)lb, bi = 0;
+    while (rem >= nb - bi) {
+        rem -= nb - bi;
+        ++bi;
+    }
+    const int bj = bi + rem;
     const double scale = 1.0 / (double)(J.n - 1);
     const bool failed = *J.err != 0;  // a tensor-core wait timed out: poison the output
-    const long long k0 = lb * OZ_FINISH_ENTRIES, k1 = min(total, k0 + OZ_FINISH_ENTRIES);
-    for (long long k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-        const int i = (int)(k / p), j = (int)(k - (long long)i * p);
-        if (i > j) continue;
-        double v = oz_cov(J.phi, J.plo, J.D, J.expo, scale, i, j) * J.inv_sd[i] * J.inv_sd[j];
-        v = fmin(fmax(v, -1.0), 1.0);
-        if (failed) v = __longlong_as_double(0x7ff8000000000000ll);
-        J.C[(size_t)i * p + j] = v;
-        J.C[(size_t)j * p + i] = v;
-        if (J.C32 != nullptr) {
-            J.C32[(size_t)i * p + j] = (float)v;
-            J.C32[(size_t)j * p + i] = (float)v;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int r = ty; r < 32; r += 8) {
+        const int i = bi * 32 + r, j = bj * 32 + tx;
+        double v = 0.0;
+        if (i < p && j < p && (bi != bj || i <= j)) {
+            v = oz_cov(J.phi, J.plo, J.D, J.expo, scale, i, j) * J.inv_sd[i] * J.inv_sd[j];
+            v = fmin(fmax(v, -1.0), 1.0);
+            if (failed) v = __longlong_as_double(0x7ff8000000000000ll);
+            J.C[(size_t)i * p + j] = v;
+            if (J.C32 != nullptr) J.C32[(size_t)i * p + j] = (float)v;
+        }
+        tv[r][tx] = v;
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        const int j = bj * 32 + r, i = bi * 32 + tx;  // lower triangle (j, i)
+        if (i < p && j < p && (bi != bj || j > i)) {
+            J.C[(size_t)j * p + i] = tv[tx][r];
+            if (J.C32 != nullptr) J.C32[(size_t)j * p + i] = (float)tv[tx][r];
         }
     }
 }
@@ -598,7 +610,8 @@ static void oz_stage_blocks(const OzJob &J, long long *nb) {
     nb[OZ_DIGITS] = (long long)(J.D.n_pad / 32) * (J.D.p_pad / 32);
     nb[OZ_PRODUCT] = (long long)J.tiles * J.D.splits;
     nb[OZ_DIAG] = (J.p + 255) / 256;
-    nb[OZ_FINISH] = ((long long)J.p * J.p + OZ_FINISH_ENTRIES - 1) / OZ_FINISH_ENTRIES;
+    const long long tb = (J.p + 31) / 32;
+    nb[OZ_FINISH] = tb * (tb + 1) / 2;  // 32 x 32 upper-triangle tiles
 }
 
 size_t corr_tc_workspace_bytes(long long n, int p, int num_sms) {

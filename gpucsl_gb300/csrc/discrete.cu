@@ -219,7 +219,8 @@ __device__ double table_chi2(const uint32_t *sm_tab, int dim_s, int di, int dj, 
 
 // Per-test header prepared by thread 0: table geometry and replica count.
 __device__ __forceinline__ bool table_geometry(const uint8_t *dims, const int *S, int *mult, int L, int vi, int vj,
-                                               int table_cap, int &dim_s, int &di, int &dj, int &copies) {
+                                               int table_cap, int part_cap, int &dim_s, int &di, int &dj,
+                                               int &copies) {
     long long ds = 1;
     for (int k = 0; k < L; ++k) {
         mult[k] = (int)ds;
@@ -229,7 +230,7 @@ __device__ __forceinline__ bool table_geometry(const uint8_t *dims, const int *S
     di = dims[vi];
     dj = dims[vj];
     const long long T = ds * di * dj;
-    if (T > table_cap || ds > 1024) return false;
+    if (T > table_cap || ds > part_cap) return false;
     dim_s = (int)ds;
     copies = 1;
     if (T <= table_cap / 8) copies = 8;
@@ -244,8 +245,9 @@ __global__ void __launch_bounds__(256) disc_test_kernel(DiscLevelArgs A) {
     __shared__ int s_mult[GCSL_MAX_LEVELS + 2];
     __shared__ int s_hdr[7];  // vi, vj, di, dj, dim_s, copies, ok
     __shared__ long long s_rank;
-    __shared__ double s_part[1024];
     __shared__ int s_bad;
+    // per-stratum statistics follow the counters (8-byte aligned)
+    double *s_part = reinterpret_cast<double *>(sm_tab + ((A.table_cap + 1) & ~1));
     DevState *st = A.st;
     if (threadIdx.x == 0) s_bad = 0;
     const int L = A.level;
@@ -279,7 +281,8 @@ __global__ void __launch_bounds__(256) disc_test_kernel(DiscLevelArgs A) {
                 for (int c = 0; c < L; ++c) s_S[c] = resolve_position(nbrs, vj, s_S[c]);
             }
             int dim_s = 0, di = 0, dj = 0, copies = 1;
-            const bool ok = table_geometry(A.dims, s_S, s_mult, L, vi, vj, A.table_cap, dim_s, di, dj, copies);
+            const bool ok =
+                table_geometry(A.dims, s_S, s_mult, L, vi, vj, A.table_cap, A.part_cap, dim_s, di, dj, copies);
             s_hdr[0] = vi;
             s_hdr[1] = vj;
             s_hdr[2] = di;
@@ -340,7 +343,7 @@ __global__ void __launch_bounds__(256) disc_table_kernel(const uint8_t *data, lo
     if (threadIdx.x == 0) {
         for (int k = 0; k < L; ++k) s_S[k] = us.S[k];
         int dim_s = 0, di = 0, dj = 0, copies = 1;
-        bool ok = table_geometry(dims, s_S, s_mult, L, vi, vj, table_cap, dim_s, di, dj, copies);
+        bool ok = table_geometry(dims, s_S, s_mult, L, vi, vj, table_cap, 1024, dim_s, di, dj, copies);
         if (ok && (long long)dim_s * di * dj > counts_cap) ok = false;  // never write past the caller's buffer
         s_hdr[0] = ok ? dim_s : -1;
         s_hdr[1] = di;
@@ -457,19 +460,44 @@ namespace host {
 int disc_table_cap(int device) {
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
-    // leave room for the static shared arrays of the kernel
+    // leave room for the static shared arrays of the kernels and 1024 strata statistics
     const int dyn = optin - 16 * 1024;
     return dyn / (int)sizeof(uint32_t);
 }
 
-cudaError_t launch_disc_tests(const DiscLevelArgs &A, int num_sms, cudaStream_t s) {
-    const size_t smem = (size_t)A.table_cap * sizeof(uint32_t);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(disc_test_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr_set = true;
+// Shared memory of one level's tables: the largest table of the level has at most
+// max_dim^(L+2) counters; small tables get replicas (fewer atomic collisions) while the
+// footprint stays small enough for several CTAs per SM.  Levels whose largest table
+// would not fit take the whole budget.
+void disc_level_caps(int cap_full, int max_dim, int L, int &table_cap, int &part_cap) {
+    long long need = 1, ds = 1;
+    for (int k = 0; k < L + 2 && need <= cap_full; ++k) {
+        need *= max_dim;
+        if (k < L) ds *= max_dim;
     }
-    disc_test_kernel<<<num_sms * 4, 256, smem, s>>>(A);
+    if (need > cap_full || ds > 1024) {
+        table_cap = cap_full;
+        part_cap = 1024;
+        return;
+    }
+    const long long reps = need <= 512 ? 8 : need <= 2048 ? 4 : need <= 8192 ? 2 : 1;
+    table_cap = (int)(need * reps < cap_full ? need * reps : cap_full);
+    part_cap = (int)ds;
+}
+
+cudaError_t launch_disc_tests(const DiscLevelArgs &A, int num_sms, cudaStream_t s) {
+    const size_t smem = (size_t)((A.table_cap + 1) & ~1) * sizeof(uint32_t) + (size_t)A.part_cap * sizeof(double);
+    static thread_local int attr_bytes = 0;
+    if ((int)smem > attr_bytes) {
+        cudaError_t e = cudaFuncSetAttribute(disc_test_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return note_error("disc_test_kernel shared memory", e);
+        attr_bytes = (int)smem;
+    }
+    int per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, disc_test_kernel, 256, smem) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    disc_test_kernel<<<num_sms * per_sm, 256, smem, s>>>(A);
     note_launch(1);
     return cudaGetLastError();
 }

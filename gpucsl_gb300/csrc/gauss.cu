@@ -20,10 +20,10 @@
 namespace gcsl {
 
 // ----------------------------------------------------------------- level 0
-__global__ void gauss_level0_kernel(const double *__restrict__ C, int p, double tau0, double t0sq,
+__global__ void gauss_level0_kernel(const double *__restrict__ C, int p, double tau0, L0Bounds B,
                                     uint16_t *__restrict__ G, double *__restrict__ zmin, double *__restrict__ r2min,
                                     int *__restrict__ kept, DevState *st, float *C32) {
-    level0_tile(C, p, tau0, t0sq, G, zmin, r2min, kept, st, (int)blockIdx.x, C32);
+    level0_tile(C, p, tau0, B, G, zmin, r2min, kept, st, (int)blockIdx.x, C32);
 }
 
 // ------------------------------------------------------------- compaction
@@ -134,9 +134,11 @@ __global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__re
         if (has && gl == 0 && J.T > 0) {
             // z* candidates: exact Z into zmin, the monotone branch's min rho^2 into r2min
             // (converted to Z once per pair by the pmax kernel)
+            // atomic minima: the candidate kernel of an earlier level may update the same
+            // pair concurrently from the side stream
             const size_t ix = (size_t)J.lo * p + J.hi;
-            if (zmin_exact < inf) zmin[ix] = fmin(zmin[ix], zmin_exact);
-            if (r2min < inf) r2min_pair[ix] = fmin(r2min_pair[ix], r2min);
+            if (zmin_exact < inf) atomic_min_nonneg_f64(zmin + ix, zmin_exact);
+            if (r2min < inf) atomic_min_nonneg_f64(r2min_pair + ix, r2min);
             n_removed += removed;
         }
     }
@@ -174,20 +176,6 @@ __global__ void __launch_bounds__(32) gauss_cand_kernel(CandArgs a) {
     cand_threads<L>(a, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
 }
 
-// The candidates of level L and the recompaction of level L + 1 in one launch: blocks
-// [0, rblocks) recompact, the others evaluate candidates; the two touch disjoint data
-// (z* minima versus adjacency), so their latencies overlap.
-template <int L>
-__global__ void __launch_bounds__(256) recompact_cand_kernel(const uint16_t *__restrict__ G, int p,
-                                                            int *__restrict__ adj, int *__restrict__ up, DevState *st,
-                                                            int2 *elist, int rblocks, CandArgs a) {
-    if ((int)blockIdx.x < rblocks) {
-        recompact_blocks(G, p, adj, up, st, L + 1, elist, (int)blockIdx.x, rblocks);
-    } else {
-        const long long cb = (long long)blockIdx.x - rblocks, ncb = (long long)gridDim.x - rblocks;
-        cand_threads<L>(a, cb * blockDim.x + threadIdx.x, ncb * blockDim.x);
-    }
-}
 
 // ---------------------------------------------------------- level l, any L
 // One warp per edge, one test at a time in key order; the (L+2)-dimensional lower
@@ -353,7 +341,8 @@ cudaError_t launch_level0(const double *C, int p, double tau0, uint16_t *G, doub
                           DevState *st, float *C32, cudaStream_t s) {
     const int nb = (p + 31) / 32;
     const double t0 = tanh(tau0);
-    gauss_level0_kernel<<<nb * (nb + 1) / 2, 256, 0, s>>>(C, p, tau0, t0 * t0, G, zmin, r2min, kept, st, C32);
+    gauss_level0_kernel<<<nb * (nb + 1) / 2, 256, 0, s>>>(C, p, tau0, level0_bounds(t0 * t0), G, zmin, r2min, kept,
+                                                         st, C32);
     note_launch(1);
     return cudaGetLastError();
 }
@@ -412,7 +401,7 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
 #define GCSL_LVL(K)                                                                                           \
     case K:                                                                                                   \
         if (mixed) {                                                                                          \
-            gauss_level_reg_kernel<K, 32, true><<<blocks, threads, 0, s>>>(C, p, adj, elist, prefix, tau, t2,  \
+            gauss_level_reg_kernel<K, 32, true><<<blocks, threads, 0, s>>>(C, p, adj, elist, prefix, tau, t2, \
                                                                            tau_valid, G, zmin, r2min, sep_dense, \
                                                                            max_level, rec_pool, rec_cap, st, mix); \
         } else {                                                                                              \
@@ -482,24 +471,6 @@ cudaError_t launch_cand(int L, const double *C, int p, double tau, double *zmin,
     return cudaGetLastError();
 }
 
-// Candidates of level L - 1 fused with the recompaction of level L (2 <= L <= 13).
-cudaError_t launch_recompact_cand(int L, const uint16_t *G, int p, int *adj, int *up, DevState *st, int2 *elist,
-                                  const double *C, double tau_prev, double *zmin, double *r2min, const int *qbuf,
-                                  long long qcap, int num_sms, cudaStream_t s) {
-    const int wpb = 256 / 32, rblocks = (p + wpb - 1) / wpb;
-    const int grid = rblocks + num_sms / 2;
-    const CandArgs a = cand_args(L - 1, C, p, tau_prev, zmin, r2min, qbuf, qcap, st);
-    switch (L - 1) {
-#define GCSL_RC(K) \
-    case K: recompact_cand_kernel<K><<<grid, 256, 0, s>>>(G, p, adj, up, st, elist, rblocks, a); break;
-        GCSL_RC(1) GCSL_RC(2) GCSL_RC(3) GCSL_RC(4) GCSL_RC(5) GCSL_RC(6)
-        GCSL_RC(7) GCSL_RC(8) GCSL_RC(9) GCSL_RC(10) GCSL_RC(11) GCSL_RC(12)
-#undef GCSL_RC
-    default: return cudaErrorInvalidValue;
-    }
-    note_launch(1);
-    return cudaGetLastError();
-}
 
 // FP32 copy of an FP64 array (round to nearest).
 __global__ void to_f32_kernel(const double *__restrict__ x, long long n, float *__restrict__ y) {

@@ -45,6 +45,7 @@ struct BInst {
     double sqrt_nm3;
     double tau[BATCH_MAX_LEVEL + 1], t2[BATCH_MAX_LEVEL + 1];
     float t2lo[BATCH_MAX_LEVEL + 1], t2hi[BATCH_MAX_LEVEL + 1];
+    L0Bounds l0;
 };
 
 // ------------------------------------------------------------- FP32 test
@@ -152,7 +153,7 @@ __global__ void batch_level0_kernel(const BInst *__restrict__ inst, const long l
                                     int count) {
     long long lb;
     const BInst &I = inst[inst_of(off_tiles, count, blockIdx.x, lb)];
-    level0_tile(I.C, I.p, I.tau[0], I.t2[0], I.G, I.zmin, I.r2min, I.kept, I.st, (int)lb);
+    level0_tile(I.C, I.p, I.tau[0], I.l0, I.G, I.zmin, I.r2min, I.kept, I.st, (int)lb);
 }
 
 // Warp per (instance, row); level 1 compacts G, later levels refilter the lists.
@@ -415,6 +416,7 @@ int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level,
             const double t = std::tanh(tau);
             I.tau[l] = tau;
             I.t2[l] = t * t;
+            if (l == 0) I.l0 = level0_bounds(t * t);
             if (precision == GCSL_PREC_SPLIT) {
                 const double lo = std::tanh(l < X.n_thresholds ? X.band_lo[l] : 0.0);
                 const double hi = std::tanh(l < X.n_thresholds ? X.band_hi[l] : 0.0);

@@ -17,7 +17,7 @@ namespace gcsl {
 // The mirrored skeleton entries are written through a shared-memory transpose so both
 // triangles are stored row-contiguously; zero diagonal.
 // One block of 256 threads per tile; `tile` enumerates the upper-triangle tiles row by row.
-__device__ __forceinline__ void level0_tile(const double *__restrict__ C, int p, double tau0, double t0sq,
+__device__ __forceinline__ void level0_tile(const double *__restrict__ C, int p, double tau0, L0Bounds B,
                                             uint16_t *__restrict__ G, double *__restrict__ zmin,
                                             double *__restrict__ r2min, int *__restrict__ kept, DevState *st,
                                             int tile, float *__restrict__ C32 = nullptr) {
@@ -42,19 +42,20 @@ __device__ __forceinline__ void level0_tile(const double *__restrict__ C, int p,
                 C32[(size_t)i * p + j] = (float)c;
                 tc[r][tx] = (float)c;
             }
-            // Z0 = atanh-like in |r| on [0, 1): Z0 < tau0 <=> r^2 < tanh(tau0)^2; the knife
-            // edge, |r| >= 1 and NaN take the reference formula
-            const double r2 = c * c;
+            // Z0 = atanh-like in |r| on [0, 1): Z0 < tau0 <=> r^2 < tanh(tau0)^2, decided
+            // on the bits of |r| outside the knife edge; the knife edge, |r| >= 1 and NaN
+            // take the reference formula
+            const unsigned long long a = (unsigned long long)__double_as_longlong(c) & 0x7fffffffffffffffull;
             bool rem0;
             double z = -1.0;  // marker: z* of a level-0 removal is finished on the side stream
-            if (r2 < 1.0 && fabs(r2 - t0sq) > 1e-12 * t0sq) {
-                rem0 = r2 < t0sq;
-                if (!rem0) {
-                    // kept: r^2 joins the pair's rho^2 minimum; the logarithm is taken once,
-                    // in the pmax kernel, instead of in this (divergent) warp
-                    z = __longlong_as_double(0x7ff0000000000000ll);
-                    r2min[(size_t)i * p + j] = r2;
-                }
+            if (a < B.lo) {
+                rem0 = true;
+            } else if (a >= B.hi && a < B.one) {
+                // kept: r^2 joins the pair's rho^2 minimum; the logarithm is taken once,
+                // in the pmax kernel, instead of in this (divergent) warp
+                rem0 = false;
+                z = __longlong_as_double(0x7ff0000000000000ll);
+                r2min[(size_t)i * p + j] = c * c;
             } else {
                 z = fabs(0.5 * log(fabs((1.0 + c) / (1.0 - c))));
                 rem0 = z < tau0;
@@ -461,15 +462,24 @@ __device__ __forceinline__ bool f32_rho2_bound(float h00, float e00, float h01, 
     return e00 < 0.25f * h00 && e11 < 0.25f * h11 && rho2 + err < 0.98f;  // NaN fails
 }
 
-template <int L>
-__device__ __forceinline__ bool gauss_test_f32b(const float *__restrict__ C32, int p, int vi, int vj, const int *S,
-                                                float &rho2, float &err) {
+// Entries of the FP32 correlation copy by variable id (row-major, row stride p).
+struct GlobalC32 {
+    const float *__restrict__ C32;
+    int p;
+    __device__ __forceinline__ float operator()(int a, int b) const { return __ldg(C32 + (size_t)a * p + b); }
+};
+
+// The FP32 elimination with its running error bound on the entries at(.,.) of the
+// (xi, xj, X) submatrix; the diagonal entries of xi and xj are 1 (as in C).
+template <int L, class Acc>
+__device__ __forceinline__ bool gauss_test_f32_at(const Acc &at, int xi, int xj, const int *X, float &rho2,
+                                                  float &err) {
     const float u = F32_U;
     if constexpr (L == 1) {
-        const float m = __ldg(C32 + (size_t)S[0] * p + S[0]);
-        const float a = __ldg(C32 + (size_t)vi * p + S[0]);
-        const float b = __ldg(C32 + (size_t)vj * p + S[0]);
-        const float r = __ldg(C32 + (size_t)vi * p + vj);
+        const float m = at(X[0], X[0]);
+        const float a = at(xi, X[0]);
+        const float b = at(xj, X[0]);
+        const float r = at(xi, xj);
         const float em = u * fabsf(m), ea = u * fabsf(a), eb = u * fabsf(b), er = u * fabsf(r);
         const float d00 = fmaf(-a, a, m), d11 = fmaf(-b, b, m);
         const float e00 = em + 2.f * fabsf(a) * ea + u * fabsf(d00);
@@ -484,14 +494,13 @@ __device__ __forceinline__ bool gauss_test_f32b(const float *__restrict__ C32, i
     float A[D * (D + 1) / 2], E[D * (D + 1) / 2];
 #pragma unroll
     for (int r = 0; r < L; ++r) {
-        const float *Cr = C32 + (size_t)S[r] * p;
 #pragma unroll
-        for (int c = 0; c <= r; ++c) A[r * (r + 1) / 2 + c] = __ldg(Cr + S[c]);
-        A[L * (L + 1) / 2 + r] = __ldg(C32 + (size_t)vi * p + S[r]);
-        A[(L + 1) * (L + 2) / 2 + r] = __ldg(C32 + (size_t)vj * p + S[r]);
+        for (int c = 0; c <= r; ++c) A[r * (r + 1) / 2 + c] = at(X[r], X[c]);
+        A[L * (L + 1) / 2 + r] = at(xi, X[r]);
+        A[(L + 1) * (L + 2) / 2 + r] = at(xj, X[r]);
     }
     A[L * (L + 1) / 2 + L] = 1.0f;
-    A[(L + 1) * (L + 2) / 2 + L] = __ldg(C32 + (size_t)vi * p + vj);
+    A[(L + 1) * (L + 2) / 2 + L] = at(xi, xj);
     A[(L + 1) * (L + 2) / 2 + L + 1] = 1.0f;
 #pragma unroll
     for (int k = 0; k < D * (D + 1) / 2; ++k) E[k] = u * fabsf(A[k]);
@@ -518,6 +527,12 @@ __device__ __forceinline__ bool gauss_test_f32b(const float *__restrict__ C32, i
     }
     const int i00 = L * (L + 1) / 2 + L, i01 = (L + 1) * (L + 2) / 2 + L, i11 = (L + 1) * (L + 2) / 2 + L + 1;
     return f32_rho2_bound(A[i00], E[i00], A[i01], E[i01], A[i11], E[i11], rho2, err) && ok;
+}
+
+template <int L>
+__device__ __forceinline__ bool gauss_test_f32b(const float *__restrict__ C32, int p, int vi, int vj, const int *S,
+                                                float &rho2, float &err) {
+    return gauss_test_f32_at<L>(GlobalC32{C32, p}, vi, vj, S, rho2, err);
 }
 
 // FP32 first: the decision is taken there when the bound puts rho^2 clearly on one side

@@ -223,6 +223,8 @@ int gcsl_corr_tc_batch_run(const gcsl_batch_plan *plan, void *stream);
  *   data         p columns of ordinal codes, column-major, column stride ld >= n
  *                (ld a multiple of 16; bytes in [n, ld) are ignored)
  *   dims         p uint8 observed cardinalities (discover_skeleton_discrete.py:49)
+ *   max_dim      the largest entry of dims; it sizes each level's shared-memory tables
+ *                (a larger cardinality in dims sets GCSL_ERR_UNSUPPORTED)
  *   other arguments as for gcsl_gauss_skeleton; pmax folds every test (the reference
  *   tests every rank, discrete_ci.cu:221-244). */
 size_t gcsl_disc_workspace_bytes(int32_t p, int64_t n, int32_t max_level, int32_t max_dim);
