@@ -12,7 +12,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libgpucsl_gb300.so"
-SOURCES = ["capi.cu", "gauss.cu", "corr.cu", "discrete.cu", "noalloc.cu", "tc_gemm.cu", "corr_tc.cu", "gauss_batch.cu", "orient.cu", "encode.cu"]
+SOURCES = ["gauss.cu", "capi.cu", "corr.cu", "discrete.cu", "noalloc.cu", "tc_gemm.cu", "corr_tc.cu", "gauss_batch.cu", "orient.cu", "encode.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

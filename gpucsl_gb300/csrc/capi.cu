@@ -30,7 +30,7 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
                                const long long *prefix, double tau, bool tau_valid, uint16_t *G, double *zmin,
                                double *r2min, int *sep_dense, int max_level, int *rec_pool, long long rec_cap,
                                DevState *st, int num_sms, const float *C32, int *qbuf, long long qcap,
-                               cudaStream_t s);
+                               const ChunkBufs &ck, cudaStream_t s);
 
 cudaError_t launch_to_f32(const double *x, long long n, float *y, int num_sms, cudaStream_t s);
 size_t orient_workspace_bytes(int p);
@@ -39,7 +39,7 @@ cudaError_t encode_columns(const void *X, int dtype, long long n, int p, long lo
 cudaError_t orient_edges(const uint16_t *S, int p, const int *sep, int L, uint8_t *D, void *ws, int num_sms,
                          int *host_word, int *passes, cudaStream_t s);
 cudaError_t launch_cand(int L, const double *C, int p, double tau, double *zmin, double *r2min, const int *qbuf,
-                        long long qcap, DevState *st, int num_sms, cudaStream_t s);
+                        long long qcap, DevState *st, const long long *chunk_first, int num_sms, cudaStream_t s);
 cudaError_t launch_pmax(const int *kept, const DevState *st, const double *zmin, const double *r2min, int p,
                         long long n_obs, const double *sftab, double *pmax, int num_sms,
                         cudaStream_t s);
@@ -280,16 +280,22 @@ struct GaussWs {
     double *sftab;    // erfc Taylor table of the pmax kernels
     int *cand;        // FP64 z* candidate queue
     long long cand_cap;
+    ChunkBufs ck;     // chunked edges of the current level (chunk_first: one region per level)
     size_t bytes;
 };
 
-// Ints of the z* candidate queue: entries hold 3 + level ints, about one or two per edge
+// Ints of the z* candidate queue: entries hold 5 + level ints, about one or two per edge
 // and level; a full queue only moves evaluations back into the level kernel.
 long long cand_queue_ints(int p) { return std::max<long long>(1ll << 20, 4ll * p * p); }
 
 // The queue holds one region per register level (1 .. GCSL_GAUSS_REG_LEVELS), so a
 // level's candidates can still be waiting on the side stream while the next levels append.
 long long cand_region_ints(long long cap) { return cap / GCSL_GAUSS_REG_LEVELS; }
+
+// Chunked edges per level and their units of 32 keys; a level that needs more walks the
+// excess edges whole in the level kernel.
+long long chunk_edges_cap(int p) { return std::max<long long>(1ll << 14, 16ll * p); }
+long long chunk_units_cap(int p) { return std::max<long long>(1ll << 16, 64ll * p); }
 
 // FP32-first level tests (default) or FP64 throughout (GCSL_F64_TESTS=1, for comparisons).
 bool mixed_tests() {
@@ -298,6 +304,15 @@ bool mixed_tests() {
         return !(e && e[0] == '1');
     }();
     return mixed;
+}
+
+// GCSL_CHUNKED=0 walks every edge whole in the level kernel (for comparisons).
+bool chunking_off() {
+    static const bool off = [] {
+        const char *e = getenv("GCSL_CHUNKED");
+        return e && e[0] == '0';
+    }();
+    return off;
 }
 
 GaussWs carve_gauss(void *ws, size_t cap, int p) {
@@ -315,6 +330,12 @@ GaussWs carve_gauss(void *ws, size_t cap, int p) {
     w.sftab = c.take<double>(32 * 13);
     w.cand_cap = cand_queue_ints(p);
     w.cand = c.take<int>((size_t)w.cand_cap);
+    w.ck.heavy_cap = chunk_edges_cap(p);
+    w.ck.unit_cap = chunk_units_cap(p);
+    w.ck.heavy = c.take<HeavyEdge>((size_t)w.ck.heavy_cap);
+    w.ck.chunk_first = c.take<long long>((size_t)w.ck.heavy_cap * GCSL_GAUSS_REG_LEVELS);
+    w.ck.unit_h = c.take<int>((size_t)w.ck.unit_cap);
+    w.ck.units = c.take<UnitRes>((size_t)w.ck.unit_cap);
     w.bytes = c.off;
     return w;
 }
@@ -445,7 +466,7 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
         host::launch_pmax_level0(C, w.zmin, p, n_obs, w.sftab, pmax, sms, ss->stream) != cudaSuccess)
         return GCSL_ERR_DEVICE;
     const long long region = cand_region_ints(w.cand_cap);
-    int rc = run_levels(max_level, w.st, s, [&](int level) -> cudaError_t {
+    auto enqueue = [&](int level) -> cudaError_t {
         // level 1 compacts the full matrix; later levels only shrink the previous lists;
         // (re)compaction writes the level's edge list; the row prefix is only needed by
         // the shared-memory kernel of levels above GCSL_GAUSS_REG_LEVELS
@@ -456,24 +477,32 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
         const double tau = tau_valid ? thresholds[level] : 0.0;
         const bool cand = mixed && level <= GCSL_GAUSS_REG_LEVELS;
         int *qbuf = cand ? w.cand + (size_t)(level - 1) * region : nullptr;
+        // level 1 walks its edges whole: its edges are many and short, so the level kernel
+        // alone keeps every SM busy
+        ChunkBufs ck = w.ck;
+        if (level >= 2 && level <= GCSL_GAUSS_REG_LEVELS) ck.chunk_first += (size_t)(level - 1) * ck.heavy_cap;
+        else ck.heavy = nullptr;
+        if (chunking_off()) ck.heavy = nullptr;
         if (e == cudaSuccess)
             e = host::launch_gauss_level(level, C, p, w.adj, w.up, w.elist, w.prefix, tau, tau_valid, G, w.zmin,
                                          w.r2min, sepsets, max_level, rec_pool, rec_cap, w.st, sms,
-                                         mixed ? w.c32 : nullptr, qbuf, region, s);
+                                         mixed ? w.c32 : nullptr, qbuf, region, ck, s);
         // the level's FP64 z* candidates only feed pmax: they run on the low-priority side
         // stream while the next levels proceed
         if (e == cudaSuccess && cand) {
             e = cudaEventRecord(ss->level[level], s);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(ss->stream, ss->level[level], 0);
             if (e == cudaSuccess)
-                e = host::launch_cand(level, C, p, tau, w.zmin, w.r2min, qbuf, region, w.st, sms, ss->stream);
+                e = host::launch_cand(level, C, p, tau, w.zmin, w.r2min, qbuf, region, w.st,
+                                      ck.heavy != nullptr ? ck.chunk_first : nullptr, sms, ss->stream);
         }
         if (lt && level + 1 < GCSL_MAX_LEVELS + 2) {
             cudaEventRecord(lt->ev[level + 1], s);
             n_timed = level + 1;
         }
         return e;
-    });
+    };
+    const int rc = run_levels(max_level, w.st, s, enqueue);
     if (cudaEventRecord(ss->join, ss->stream) != cudaSuccess || cudaStreamWaitEvent(s, ss->join, 0) != cudaSuccess)
         return GCSL_ERR_DEVICE;
     if (rc != GCSL_OK) return rc;

@@ -70,6 +70,35 @@ struct DevState {
     unsigned long long n_rec_ints;           // ints used in the record pool
     unsigned long long retests;              // FP64 re-tests of the split-precision path
     unsigned long long cand_ints[GCSL_MAX_LEVELS];  // ints queued for the FP64 z* candidate kernel
+    unsigned long long heavy[GCSL_MAX_LEVELS];      // chunked edges registered per level
+    unsigned long long units[GCSL_MAX_LEVELS];      // key units reserved per level
+};
+
+// Chunked edges of a Gaussian level (the unit kernel walks their keys after the first
+// step in parallel units of 32 keys; the last unit of an edge combines them).
+struct HeavyEdge {
+    int lo, hi;
+    long long T;
+    long long unit_base;  // units unit_base .. unit_base + n_units - 1 (keys 32 (k + 1) ..)
+    int n_units;
+    int done;             // units finished (atomic)
+    long long best;       // smallest removing key found so far (atomic min; T when none)
+    double r2_0, ze_0;    // minima of the first step (no remover there)
+    double floor;         // the pair's exact rho^2 minimum before the level
+};
+
+struct UnitRes {
+    long long first;  // first removing key of the unit (its end when none)
+    double r2, ze;    // minima over the unit's keys up to `first`
+};
+
+struct ChunkBufs {
+    HeavyEdge *heavy;
+    long long *chunk_first;  // canonical remover of each chunked edge (T when none)
+    long long heavy_cap;
+    int *unit_h;             // chunked edge of each unit (-1: unused slot)
+    UnitRes *units;
+    long long unit_cap;
 };
 
 // Arguments of one discrete test-kernel launch.

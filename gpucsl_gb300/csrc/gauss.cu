@@ -15,7 +15,7 @@
 // canonical remover (its set is the sepset) and z* folds the keys up to it.  Because
 // the warp owns the edge for the whole level, the skeleton, sepset and zmin writes
 // need no atomics, and the result does not depend on scheduling.
-#include "gauss_dev.cuh"
+#include "gauss_levels.cuh"
 
 namespace gcsl {
 
@@ -72,81 +72,35 @@ __global__ void row_scan_kernel(const T *__restrict__ cnt, int p, long long *__r
     block_scan_rows(cnt, p, prefix);
 }
 
-// Level kernel: groups of G lanes each own one edge (32 / G edges per warp) and walk its
-// merged key sequence G keys at a time.  Small groups keep the FP64 pipe busy at the
-// upper levels, where an edge has only a handful of candidate sets, and stop at most
-// G - 1 tests past the first remover.  MIXED: the tests run FP32-first (MixedTest) and
-// queue their FP64 z* candidates for gauss_cand_kernel.
-struct MixArgs {
-    const float *C32;  // FP32 copy of C
-    float t2lo, t2hi;  // FP32 bounds of the knife edge around tanh(tau)^2
-    CandQueue q;
-};
-
-template <int L, int G, bool MIXED>
-__global__ void __launch_bounds__(256) gauss_level_reg_kernel(const double *__restrict__ C, int p,
-                                                             const int *__restrict__ adj, const int2 *__restrict__ elist,
-                                                             const long long *__restrict__ prefix, double tau,
-                                                             double t2, bool tau_valid, uint16_t *G_, double *zmin,
-                                                             double *r2min_pair, int *sep_dense, int max_level,
-                                                             int *rec_pool, long long rec_cap, DevState *st,
-                                                             MixArgs mix) {
+// Level kernel of level L (1 <= L <= GCSL_GAUSS_REG_LEVELS): the edge phase over one
+// resident wave of warps.  The unit kernel follows it when edges are chunked.
+template <int L, bool MIXED>
+__global__ void __launch_bounds__(256) gauss_level_reg_kernel(LevelCtx x) {
     __shared__ BinomRows sb;
-    if (!level_active(st, L, tau_valid)) return;
-    const long long n_edges = (long long)st->edges[L];  // filled by the (re)compaction
-    if ((long long)blockIdx.x * (blockDim.x >> 5) * (32 / G) >= n_edges) return;  // no edge for this block
+    if (!level_active(x.st, L, x.tau_valid)) return;
+    const long long n_edges = (long long)x.st->edges[L];  // filled by the (re)compaction
+    if ((long long)blockIdx.x * (blockDim.x >> 5) >= n_edges) return;  // no edge for this block
     if (L >= 2) {
         binom_rows_load(sb);
         __syncthreads();
     }
-    constexpr int GPW = 32 / G;  // groups per warp
-    const int lane = threadIdx.x & 31, gl = lane & (G - 1), gw = lane / G;
-    const unsigned gshift = (unsigned)(gw * G);
-    const unsigned gbits = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
-    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
-    const double inf = __longlong_as_double(0x7ff0000000000000ll);
-    unsigned long long n_tests = 0, n_full = 0, n_removed = 0;
-    for (long long e0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * GPW; e0 < n_edges;
-         e0 += warps * GPW) {
-        const long long e = e0 + gw;
-        EdgeJob J;
-        J.T = 0;
-        bool has = e < n_edges;
-        if (has && !load_edge_list<L>(adj, elist, p, e, L, J)) {
-            if (gl == 0) set_status(st, GCSL_ERR_UNSUPPORTED);
-            J.T = 0;
-        }
-        if (has && gl == 0) n_full += J.T;
-        double r2min = inf, zmin_exact = inf;
-        bool removed = false;
-        if constexpr (MIXED) {
-            // the pair's exact rho^2 minimum from earlier levels (level 0 stored r^2)
-            const double floor = (has && J.T > 0) ? r2min_pair[(size_t)J.lo * p + J.hi] : 0.0;
-            walk_edge<L, G>(J, has, adj, p, gl, gshift, gbits,
-                            MixedTest<L>{C, mix.C32, p, tau, t2, mix.t2lo, mix.t2hi}, G_, sep_dense, max_level,
-                            rec_pool, rec_cap, st, r2min, zmin_exact, removed, n_tests, &mix.q,
-                            L >= 2 ? &sb : nullptr, floor);
-        } else {
-            walk_edge<L, G>(J, has, adj, p, gl, gshift, gbits, F64Test<L>{C, p, tau, t2}, G_, sep_dense, max_level,
-                            rec_pool, rec_cap, st, r2min, zmin_exact, removed, n_tests, nullptr,
-                            L >= 2 ? &sb : nullptr);
-        }
-        if (has && gl == 0 && J.T > 0) {
-            // z* candidates: exact Z into zmin, the monotone branch's min rho^2 into r2min
-            // (converted to Z once per pair by the pmax kernel)
-            // atomic minima: the candidate kernel of an earlier level may update the same
-            // pair concurrently from the side stream
-            const size_t ix = (size_t)J.lo * p + J.hi;
-            if (zmin_exact < inf) atomic_min_nonneg_f64(zmin + ix, zmin_exact);
-            if (r2min < inf) atomic_min_nonneg_f64(r2min_pair + ix, r2min);
-            n_removed += removed;
-        }
+    level_edge_phase<L, MIXED>(x, L >= 2 ? &sb : nullptr, ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                               ((long long)gridDim.x * blockDim.x) >> 5);
+}
+
+template <int L, bool MIXED>
+__global__ void __launch_bounds__(256) gauss_level_units_kernel(LevelCtx x) {
+    __shared__ BinomRows sb;
+    if (!level_active(x.st, L, x.tau_valid)) return;
+    const long long reserved = (long long)x.st->units[L];
+    const long long nu = reserved < x.ck.unit_cap ? reserved : x.ck.unit_cap;
+    if ((long long)blockIdx.x * (blockDim.x >> 5) >= nu) return;
+    if (L >= 2) {
+        binom_rows_load(sb);
+        __syncthreads();
     }
-    if (gl == 0) {
-        if (n_tests) atomicAdd(&st->tests[L], n_tests);
-        if (n_full) atomicAdd(&st->tests_full[L], n_full);
-        if (n_removed) atomicAdd(&st->removed[L], n_removed);
-    }
+    level_unit_phase<L, MIXED>(x, L >= 2 ? &sb : nullptr, ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                               ((long long)gridDim.x * blockDim.x) >> 5);
 }
 
 // FP64 evaluation of the z* candidates queued by the mixed level-L kernel (one thread
@@ -161,20 +115,23 @@ struct CandArgs {
     long long cap;
     const unsigned long long *count;
     double *zmin, *r2min;
+    const long long *chunk_first;  // canonical removers of the level's chunked edges
 };
 
 template <int L>
 __device__ __forceinline__ void cand_threads(const CandArgs &a, long long t0, long long stride) {
-    constexpr int W = 3 + L;
+    constexpr int W = CAND_HEADER + L;
     const long long used = (long long)*a.count;
     const long long n = (used < a.cap ? used : a.cap) / W;
-    for (long long t = t0; t < n; t += stride) eval_candidate<L>(a.C, a.p, a.q + t * W, a.tau, a.t2, a.zmin, a.r2min);
+    for (long long t = t0; t < n; t += stride)
+        eval_candidate<L>(a.C, a.p, a.q + t * W, a.tau, a.t2, a.zmin, a.r2min, a.chunk_first);
 }
 
 template <int L>
 __global__ void __launch_bounds__(32) gauss_cand_kernel(CandArgs a) {
     cand_threads<L>(a, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
 }
+
 
 
 // ---------------------------------------------------------- level l, any L
@@ -376,39 +333,66 @@ cudaError_t launch_scan_ll(const long long *cnt, int p, long long *prefix, DevSt
     return cudaGetLastError();
 }
 
+// The level's context (thresholds, FP32 bounds of the knife edge, queue) for launches.
+LevelCtx level_ctx(int L, const double *C, int p, const int *adj, const int2 *elist, double tau, bool tau_valid,
+                   uint16_t *G, double *zmin, double *r2min, int *sep_dense, int max_level, int *rec_pool,
+                   long long rec_cap, DevState *st, const float *C32, int *qbuf, long long qcap,
+                   const ChunkBufs &ck) {
+    LevelCtx x;
+    x.C = C;
+    x.p = p;
+    x.adj = adj;
+    x.elist = elist;
+    x.tau = tau;
+    const double th = tanh(tau);
+    x.t2 = th * th;  // Z < tau  <=>  rho^2 < tanh(tau)^2 for |rho| < 1
+    x.tau_valid = tau_valid;
+    x.G = G;
+    x.zmin = zmin;
+    x.r2min = r2min;
+    x.sep_dense = sep_dense;
+    x.max_level = max_level;
+    x.rec_pool = rec_pool;
+    x.rec_cap = rec_cap;
+    x.st = st;
+    x.mix.C32 = C32;
+    // FP32 bounds of the FP64 knife edge [t2 (1 - 1e-12), t2 (1 + 1e-12)], rounded outward
+    x.mix.t2lo = nextafterf((float)(x.t2 * (1.0 - 2e-12)), 0.0f);
+    x.mix.t2hi = nextafterf((float)(x.t2 * (1.0 + 2e-12)), 2.0f);
+    x.mix.q.buf = qbuf;
+    x.mix.q.cap = qcap;
+    x.mix.q.count = &st->cand_ints[L < GCSL_MAX_LEVELS ? L : 0];
+    x.ck = ck;
+    return x;
+}
+
 cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, const int *up, const int2 *elist,
                                const long long *prefix, double tau, bool tau_valid, uint16_t *G, double *zmin,
                                double *r2min, int *sep_dense, int max_level, int *rec_pool, long long rec_cap,
                                DevState *st, int num_sms, const float *C32, int *qbuf, long long qcap,
-                               cudaStream_t s) {
+                               const ChunkBufs &ck, cudaStream_t s) {
     // register-heavy upper levels run 128-thread blocks so a full wave of warps is resident
     // level 1 (tens of thousands of edges) strides over the edges with many blocks; the
     // upper levels have a few thousand edges, one warp each: one resident wave of blocks,
     // so no empty blocks queue behind the working ones
     const int threads = L >= 4 ? 128 : 256;
     const int blocks = L == 1 ? num_sms * 8 : num_sms * (L >= 4 ? 4 : 2);
-    const double th = tanh(tau);
-    const double t2 = th * th;  // Z < tau  <=>  rho^2 < tanh(tau)^2 for |rho| < 1
-    MixArgs mix;
-    mix.C32 = C32;
-    // FP32 bounds of the FP64 knife edge [t2 (1 - 1e-12), t2 (1 + 1e-12)], rounded outward
-    mix.t2lo = nextafterf((float)(t2 * (1.0 - 2e-12)), 0.0f);
-    mix.t2hi = nextafterf((float)(t2 * (1.0 + 2e-12)), 2.0f);
-    mix.q.buf = qbuf;
-    mix.q.cap = qcap;
-    mix.q.count = &st->cand_ints[L < GCSL_MAX_LEVELS ? L : 0];
     const bool mixed = C32 != nullptr && qbuf != nullptr;
-#define GCSL_LVL(K)                                                                                           \
-    case K:                                                                                                   \
-        if (mixed) {                                                                                          \
-            gauss_level_reg_kernel<K, 32, true><<<blocks, threads, 0, s>>>(C, p, adj, elist, prefix, tau, t2, \
-                                                                           tau_valid, G, zmin, r2min, sep_dense, \
-                                                                           max_level, rec_pool, rec_cap, st, mix); \
-        } else {                                                                                              \
-            gauss_level_reg_kernel<K, 32, false><<<blocks, threads, 0, s>>>(C, p, adj, elist, prefix, tau, t2, \
-                                                                            tau_valid, G, zmin, r2min, sep_dense, \
-                                                                            max_level, rec_pool, rec_cap, st, mix); \
-        }                                                                                                     \
+    const LevelCtx x = level_ctx(L, C, p, adj, elist, tau, tau_valid, G, zmin, r2min, sep_dense, max_level, rec_pool,
+                                 rec_cap, st, C32, qbuf, qcap, ck);
+    // chunked edges: the unit kernel follows the level kernel (it returns at once when no
+    // edge was chunked); one resident wave of warps strides over the units
+    const int ublocks = num_sms * (L >= 4 ? 4 : 2);
+#define GCSL_LVL(K)                                                                                \
+    case K:                                                                                        \
+        if (mixed) {                                                                               \
+            gauss_level_reg_kernel<K, true><<<blocks, threads, 0, s>>>(x);                         \
+            if (ck.heavy != nullptr) gauss_level_units_kernel<K, true><<<ublocks, threads, 0, s>>>(x); \
+        } else {                                                                                   \
+            gauss_level_reg_kernel<K, false><<<blocks, threads, 0, s>>>(x);                        \
+            if (ck.heavy != nullptr) gauss_level_units_kernel<K, false><<<ublocks, threads, 0, s>>>(x); \
+        }                                                                                          \
+        if (ck.heavy != nullptr) note_launch(1);                                                   \
         break;
     switch (L) {
         GCSL_LVL(1)
@@ -440,7 +424,7 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
 }
 
 static CandArgs cand_args(int L, const double *C, int p, double tau, double *zmin, double *r2min, const int *qbuf,
-                          long long qcap, DevState *st) {
+                          long long qcap, DevState *st, const long long *chunk_first) {
     const double th = tanh(tau);
     CandArgs a;
     a.C = C;
@@ -452,13 +436,14 @@ static CandArgs cand_args(int L, const double *C, int p, double tau, double *zmi
     a.count = &st->cand_ints[L];
     a.zmin = zmin;
     a.r2min = r2min;
+    a.chunk_first = chunk_first;
     return a;
 }
 
 // FP64 z* candidates of mixed level L (1 <= L <= GCSL_GAUSS_REG_LEVELS) on their own.
 cudaError_t launch_cand(int L, const double *C, int p, double tau, double *zmin, double *r2min, const int *qbuf,
-                        long long qcap, DevState *st, int num_sms, cudaStream_t s) {
-    const CandArgs a = cand_args(L, C, p, tau, zmin, r2min, qbuf, qcap, st);
+                        long long qcap, DevState *st, const long long *chunk_first, int num_sms, cudaStream_t s) {
+    const CandArgs a = cand_args(L, C, p, tau, zmin, r2min, qbuf, qcap, st, chunk_first);
     switch (L) {
 #define GCSL_CAND(K) \
     case K: gauss_cand_kernel<K><<<num_sms * 16, 32, 0, s>>>(a); break;

@@ -369,6 +369,21 @@ __device__ __forceinline__ bool load_edge_list(const int *__restrict__ adj, cons
     return J.R0 < GCSL_RANK_LIMIT && J.R1 < GCSL_RANK_LIMIT;
 }
 
+// The job of edge (lo, hi) from the current adjacency lists.
+template <int KMAX>
+__device__ __forceinline__ void edge_job_of(const int *__restrict__ adj, int p, int lo, int hi, int L, EdgeJob &J) {
+    J.lo = lo;
+    J.hi = hi;
+    J.deg_lo = adj[(size_t)lo * p];
+    J.deg_hi = adj[(size_t)hi * p];
+    const int K0 = J.deg_lo - 1, K1 = J.deg_hi - 1;
+    J.R0 = (K0 >= L) ? binom_fast<KMAX>(K0, L) : 0;
+    J.R1 = (K1 >= L) ? binom_fast<KMAX>(K1, L) : 0;
+    J.T = J.R0 + J.R1;
+    J.Rmin = J.R0 < J.R1 ? J.R0 : J.R1;
+    J.longer = J.R0 > J.R1 ? 0 : 1;
+}
+
 // merged key index m -> (rank, dir)
 __device__ __forceinline__ void key_of(const EdgeJob &J, long long m, long long &rank, int &dir) {
     if (m < 2 * J.Rmin) {
@@ -563,8 +578,10 @@ struct MixedTest {
     }
 };
 
-// Deferred FP64 evaluations of level L: entries [pair index lo * p + hi, vi, vj, S...]
-// appended by the level kernel, evaluated densely by the candidate kernel.
+// Deferred FP64 evaluations of level L: entries [pair index lo * p + hi, vi, vj, chunk tag,
+// merged key index, S...] appended by the level kernels, evaluated densely by the
+// candidate kernel (tag -1: the key always counts).
+constexpr int CAND_HEADER = 5;
 struct CandQueue {
     int *buf;
     long long cap;                 // ints
@@ -605,19 +622,32 @@ struct F64Test {
 // the smallest upper end in its step and the pair's minimum from earlier levels could
 // hold the minimum and is queued for the FP64 candidate kernel (or evaluated here when
 // the queue is full); exact keys fold directly.
+// A slice [m0, m1) of an edge's merged key sequence.  With defer set, the slice is one
+// unit of a chunked edge: its first removing key is reported in `first` (m1 when none)
+// instead of being written back, and its queued z* candidates carry (tag, key) so the
+// candidate kernel can drop the ones behind the edge's canonical remover.
+struct WalkRange {
+    long long m0, m1;
+    bool defer;
+    int tag;
+    long long first;
+};
+
 template <int L, int G, class Test>
 __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int *__restrict__ adj, int p, int gl,
                                           unsigned gshift, unsigned gbits, const Test &test, uint16_t *G_,
                                           int *sep_dense, int max_level, int *rec_pool, long long rec_cap,
                                           DevState *st, double &r2min, double &zmin_exact, bool &removed,
                                           unsigned long long &n_tests, const CandQueue *q = nullptr,
-                                          const BinomRows *sb = nullptr, double r2_floor = 0.0) {
+                                          const BinomRows *sb = nullptr, double r2_floor = 0.0,
+                                          WalkRange *rg = nullptr) {
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
-    bool done = !has || J.T == 0;
-    long long base = 0;
+    long long base = rg ? rg->m0 : 0;
+    const long long mend = rg ? rg->m1 : J.T;
+    bool done = !has || base >= mend;
     while (__any_sync(GCSL_FULL_MASK, !done)) {
         const long long m = base + gl;
-        const bool valid = !done && m < J.T;
+        const bool valid = !done && m < mend;
         TestOut o;
         o.rho2 = inf;
         o.zexact = inf;
@@ -650,7 +680,7 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
             bool cand = fold && !o.exact && lo32 <= hi && (double)lo32 <= r2_floor;
             const unsigned cm = __ballot_sync(GCSL_FULL_MASK, cand);
             if (cm) {
-                constexpr int W = 3 + L;
+                constexpr int W = CAND_HEADER + L;
                 unsigned long long b0 = 0;
                 const int leader = __ffs(cm) - 1;
                 if ((threadIdx.x & 31) == leader) b0 = atomicAdd(q->count, (unsigned long long)(W * __popc(cm)));
@@ -662,8 +692,10 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
                         e[0] = J.lo * p + J.hi;
                         e[1] = vi;
                         e[2] = vj;
+                        e[3] = (rg && rg->defer) ? rg->tag : -1;
+                        e[4] = (int)m;
 #pragma unroll
-                        for (int c = 0; c < L; ++c) e[3 + c] = S[c];
+                        for (int c = 0; c < L; ++c) e[CAND_HEADER + c] = S[c];
                         cand = false;
                     }
                 }
@@ -692,27 +724,74 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
             }
         }
         if (!done) {
-            const long long left = J.T - base;
+            const long long left = mend - base;
             if (gl == 0) n_tests += (unsigned long long)(bal ? first + 1 : (left < G ? left : G));
             if (bal) {
-                if (gl == first) write_removal(J, L, S, p, max_level, G_, sep_dense, rec_pool, rec_cap, st);
+                if (rg && rg->defer) rg->first = base + first;
+                else if (gl == first) write_removal(J, L, S, p, max_level, G_, sep_dense, rec_pool, rec_cap, st);
                 removed = true;
                 done = true;
             } else {
                 base += G;
-                if (base >= J.T) done = true;
+                if (base >= mend) done = true;
             }
         }
     }
 }
 
+// Chunked edges.  An edge whose merged key sequence spans more than one step has its first
+// step walked by the level kernel; when that step holds no remover, the rest is cut into
+// units of one step each (32 keys), which the unit kernel walks in parallel.  The last unit
+// of an edge to finish combines them in key order: the canonical remover is the smallest
+// removing key over all units, and z* folds every unit that starts at or before it (up to
+// its own first remover), exactly the keys the sequential walk would have folded.
+// Registers edge J (first step walked, no remover) for the unit kernel; false when the
+// buffers are full, and the caller walks the remaining keys itself.  Whole group calls.
+template <int G>
+__device__ __forceinline__ bool register_chunked(const EdgeJob &J, int gl, const ChunkBufs &ck, DevState *st, int L,
+                                                 double r2_0, double ze_0, double floor) {
+    const long long nu = (J.T - G + G - 1) / G;
+    long long h = 0, ub = 0;
+    if (gl == 0) {
+        h = (long long)atomicAdd(&st->heavy[L], 1ull);
+        ub = (long long)atomicAdd(&st->units[L], (unsigned long long)nu);
+    }
+    h = __shfl_sync(GCSL_FULL_MASK, h, 0, G);
+    ub = __shfl_sync(GCSL_FULL_MASK, ub, 0, G);
+    const bool ok = h < ck.heavy_cap && ub + nu <= ck.unit_cap && J.T < (1ll << 31);
+    if (ok) {
+        if (gl == 0) {
+            HeavyEdge H;
+            H.lo = J.lo;
+            H.hi = J.hi;
+            H.T = J.T;
+            H.unit_base = ub;
+            H.n_units = (int)nu;
+            H.done = 0;
+            H.best = J.T;
+            H.r2_0 = r2_0;
+            H.ze_0 = ze_0;
+            H.floor = floor;
+            ck.heavy[h] = H;
+        }
+        for (long long k = gl; k < nu; k += G) ck.unit_h[ub + k] = (int)h;
+    } else {
+        // reserved unit slots inside the buffer stay marked unused
+        for (long long k = ub + gl; k < ub + nu && k < ck.unit_cap; k += G) ck.unit_h[k] = -1;
+    }
+    return ok;
+}
+
 // Candidate kernel body: the FP64 test of queued entry e, folded into the pair's minima.
 template <int L>
 __device__ __forceinline__ void eval_candidate(const double *__restrict__ C, int p, const int *e, double tau,
-                                               double t2, double *zmin, double *r2min) {
+                                               double t2, double *zmin, double *r2min,
+                                               const long long *__restrict__ chunk_first = nullptr) {
+    // a key of a chunked edge behind the edge's canonical remover does not count
+    if (e[3] >= 0 && chunk_first != nullptr && (long long)e[4] > chunk_first[e[3]]) return;
     int S[L];
 #pragma unroll
-    for (int c = 0; c < L; ++c) S[c] = e[3 + c];
+    for (int c = 0; c < L; ++c) S[c] = e[CAND_HEADER + c];
     const TestOut o = gauss_test_reg<L>(C, p, e[1], e[2], S, tau, t2);
     const size_t ix = (size_t)e[0];
     if (o.rho2 < __longlong_as_double(0x7ff0000000000000ll)) atomic_min_nonneg_f64(r2min + ix, o.rho2);

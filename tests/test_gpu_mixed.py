@@ -1,8 +1,10 @@
 """The FP32-first level tests (default) against FP64 tests throughout
-(GCSL_F64_TESTS=1, read once per process, so that run is a subprocess): skeleton,
-sepsets, pmax and per-level test counts must be bit-identical, because every decision
-taken in FP32 has a bound that clears the FP64 knife edge and every test whose bound can
-hold the z* minimum is re-evaluated in FP64."""
+(GCSL_F64_TESTS=1), and the chunked walk of long edges (default) against walking every
+edge whole in one warp (GCSL_CHUNKED=0); both switches are read once per process, so
+each run is a subprocess.  Skeleton, sepsets, pmax and per-level test counts must be
+bit-identical: every decision taken in FP32 has a bound that clears the FP64 knife edge,
+every test whose bound can hold the z* minimum is re-evaluated in FP64, and the chunk
+combine picks the smallest removing key and folds exactly the keys before it."""
 import json
 import os
 import subprocess
@@ -15,7 +17,10 @@ import pytest
 pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parents[1]
 
-CASES = [(1000, 10000, 3, 2, 0.01, 998), (300, 2000, 4, 8, 0.05, 12), (120, 500, 3, 9, 0.2, 12)]
+CASES = [(1000, 10000, 3, 2, 0.01, 998), (300, 2000, 4, 8, 0.05, 12), (120, 500, 3, 9, 0.2, 12),
+         (200, 3000, 8, 5, 0.05, 12)]
+MODES = {"mixed": {}, "f64": {"GCSL_F64_TESTS": "1"}, "whole": {"GCSL_CHUNKED": "0"},
+         "whole_f64": {"GCSL_CHUNKED": "0", "GCSL_F64_TESTS": "1"}}
 
 SOLVE = r"""
 import json, sys, numpy as np, torch
@@ -33,21 +38,23 @@ np.savez({out!r}, G=G, sep=sep, pm=pm, tests=np.array(st.raw["tests"]), C=C.cpu(
 
 
 @pytest.mark.parametrize("case", CASES)
-def test_mixed_equals_fp64(cuda, tmp_path, case):
+def test_mixed_and_chunked_equal_fp64_whole(cuda, tmp_path, case):
     outs = {}
-    for mode in ("mixed", "f64"):
+    for mode, extra in MODES.items():
         out = str(tmp_path / f"{mode}.npz")
         env = dict(os.environ)
         env.pop("GCSL_F64_TESTS", None)
-        if mode == "f64":
-            env["GCSL_F64_TESTS"] = "1"
+        env.pop("GCSL_CHUNKED", None)
+        env.update(extra)
         r = subprocess.run([sys.executable, "-c", SOLVE.format(root=str(ROOT), case=case, out=out)], env=env,
                            capture_output=True, text=True, timeout=600)
         assert r.returncode == 0, r.stderr[-2000:]
         outs[mode] = np.load(out)
-    a, b = outs["mixed"], outs["f64"]
-    assert np.array_equal(a["C"], b["C"])
-    assert np.array_equal(a["G"], b["G"])
-    assert np.array_equal(a["sep"], b["sep"])
-    assert np.array_equal(a["tests"], b["tests"])
-    assert np.array_equal(a["pm"], b["pm"]), float(np.abs(a["pm"] - b["pm"]).max())
+    a = outs["mixed"]
+    for mode in ("f64", "whole", "whole_f64"):
+        b = outs[mode]
+        assert np.array_equal(a["C"], b["C"]), mode
+        assert np.array_equal(a["G"], b["G"]), mode
+        assert np.array_equal(a["sep"], b["sep"]), mode
+        assert np.array_equal(a["tests"], b["tests"]), mode
+        assert np.array_equal(a["pm"], b["pm"]), (mode, float(np.abs(a["pm"] - b["pm"]).max()))
