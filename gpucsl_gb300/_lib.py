@@ -191,7 +191,7 @@ def lib() -> ct.CDLL:
     L.gcsl_corr_tc_batch_run.restype = ct.c_int
     L.gcsl_corr_tc_batch_run.argtypes = [ct.POINTER(BatchPlan), _vp]
     L.gcsl_encode_workspace_bytes.restype = _sz
-    L.gcsl_encode_workspace_bytes.argtypes = []
+    L.gcsl_encode_workspace_bytes.argtypes = [_i32]
     L.gcsl_ordinal_encode.restype = ct.c_int
     L.gcsl_ordinal_encode.argtypes = [_vp, _i32, _i64, _i32, _i64, _vp, _i64, _vp, _vp, _sz, _vp]
     L.gcsl_orient_workspace_bytes.restype = _sz

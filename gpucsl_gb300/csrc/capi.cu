@@ -35,7 +35,8 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
 cudaError_t launch_to_f32(const double *x, long long n, float *y, int num_sms, cudaStream_t s);
 size_t orient_workspace_bytes(int p);
 cudaError_t encode_columns(const void *X, int dtype, long long n, int p, long long ld, uint8_t *codes, long long ldc,
-                           uint8_t *dims, int *status, cudaStream_t s);
+                           uint8_t *dims, void *workspace, cudaStream_t s);
+size_t encode_workspace_bytes(int p);
 cudaError_t orient_edges(const uint16_t *S, int p, const int *sep, int L, uint8_t *D, void *ws, int num_sms,
                          int *host_word, int *passes, cudaStream_t s);
 cudaError_t launch_cand(int L, const double *C, int p, double tau, double *zmin, double *r2min, const int *qbuf,
@@ -727,20 +728,21 @@ int gcsl_orient_edges(const uint16_t *G, int32_t p, const int32_t *sepsets, int3
 
 
 // ------------------------------------------------------------- ordinal encoding
-size_t gcsl_encode_workspace_bytes(void) { return 256; }
+size_t gcsl_encode_workspace_bytes(int32_t p) { return p < 1 ? 256 : host::encode_workspace_bytes(p); }
 
 int gcsl_ordinal_encode(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ld, uint8_t *codes, int64_t ldc,
                         uint8_t *dims, void *workspace, size_t workspace_bytes, void *stream) {
     if (!X || !codes || !dims || n < 0 || p < 1 || ld < p || ldc < n ||
         (dtype != GCSL_DTYPE_I32 && dtype != GCSL_DTYPE_I64 && dtype != GCSL_DTYPE_U8 && dtype != GCSL_DTYPE_F64))
         return GCSL_ERR_INVALID_ARG;
-    if (!workspace || workspace_bytes < gcsl_encode_workspace_bytes()) return GCSL_ERR_WORKSPACE;
+    if (!workspace || workspace_bytes < gcsl_encode_workspace_bytes(p) ||
+        reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
+        return GCSL_ERR_WORKSPACE;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    int *status = static_cast<int *>(workspace);
+    int *status = static_cast<int *>(workspace);  // the workspace starts with the status word
     HostCtl *hc = host_ctl();
     if (!hc) return GCSL_ERR_DEVICE;
-    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), s);
-    if (e == cudaSuccess) e = host::encode_columns(X, dtype, n, p, ld, codes, ldc, dims, status, s);
+    cudaError_t e = host::encode_columns(X, dtype, n, p, ld, codes, ldc, dims, workspace, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&hc->words[0], status, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return map_cuda(e);

@@ -227,7 +227,7 @@ def ordinal_encode_device(X, ld: int | None = None):
     codes = torch.zeros((p, ld), dtype=torch.uint8, device=X.device)
     dims = torch.empty(p, dtype=torch.uint8, device=X.device)
     L = _lib.lib()
-    ws = torch.empty(int(L.gcsl_encode_workspace_bytes()), dtype=torch.uint8, device=X.device)
+    ws = torch.empty(int(L.gcsl_encode_workspace_bytes(p)), dtype=torch.uint8, device=X.device)
     _lib.check(L.gcsl_ordinal_encode(X.data_ptr(), dt, n, p, p, codes.data_ptr(), ld, dims.data_ptr(), ws.data_ptr(),
                                      ws.numel(), _lib.stream_ptr()), "gcsl_ordinal_encode")
     return codes, dims

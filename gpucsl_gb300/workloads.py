@@ -9,6 +9,8 @@ wide   Gaussian p = 5000, n = 2000, degree 3, seed 5, alpha 0.01, levels <= 1: C
        run against HBM
 cfg3   discrete p = 200, n = 50000, cardinality 2..5, degree 2, seed 3, alpha 0.05, levels <= 3
 cfg4   512 uneven Gaussian instances (p 50..400, n 500..20000), split precision, levels <= 4
+orient edge orientation (v-structures and Meek's rules) of the cfg2 skeleton and sepsets
+encode device ordinal encoding of the cfg3 samples (200 int64 columns, n = 50000)
 
 Each repeat is one full solve from samples in device memory (correlation included for
 the Gaussian workloads); the script prints one line per repeat with its device time.
@@ -24,7 +26,7 @@ GAUSS = {"cfg1": (20, 1000, 2, 1, 0.05, 3), "cfg2": (1000, 10000, 3, 2, 0.01, 99
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="cfg2", choices=sorted(list(GAUSS) + ["cfg3", "cfg4"]))
+    ap.add_argument("--workload", default="cfg2", choices=sorted(list(GAUSS) + ["cfg3", "cfg4", "orient", "encode"]))
     ap.add_argument("--repeat", type=int, default=2)
     args = ap.parse_args(argv)
 
@@ -59,6 +61,26 @@ def main(argv=None):
             st, ms = timed(solve)
             print(json.dumps({"workload": args.workload, "repeat": r, "ms": round(ms, 3), "tests": st.tests,
                               "levels_run": st.levels_run}), flush=True)
+    elif args.workload == "orient":
+        from .orient import orient_edges_device
+
+        p, n, deg, seed, alpha, maxl = GAUSS["cfg2"]
+        X = torch.from_numpy(gaussian_dag_data(p, n, deg, seed).data).cuda()
+        solver = engine.GaussianSolver(p, 12)  # the cfg2 loop ends at level 10; 12 bounds the sepsets
+        st = solver.run(engine.correlation(X), n, engine.gaussian_thresholds(n, alpha))
+        G, sep, _ = solver.to_host()
+        Gd = torch.from_numpy(G.view("int16")).cuda()
+        sepd = torch.from_numpy(sep[:, :, :max(st.levels_run - 1, 1)].astype("int32")).cuda()
+        for r in range(args.repeat):
+            (_, passes), ms = timed(lambda: orient_edges_device(Gd, sepd))
+            print(json.dumps({"workload": "orient", "repeat": r, "ms": round(ms, 3), "passes": passes}), flush=True)
+    elif args.workload == "encode":
+        d = discrete_bn_data(200, 50000, 2, 3)
+        Xd = torch.from_numpy(d.data.astype("int64")).cuda()
+        for r in range(args.repeat):
+            (_, dims), ms = timed(lambda: engine.ordinal_encode_device(Xd))
+            print(json.dumps({"workload": "encode", "repeat": r, "ms": round(ms, 3),
+                              "max_dim": int(dims.max().item())}), flush=True)
     elif args.workload == "cfg3":
         d = discrete_bn_data(200, 50000, 2, 3)
         codes, dims = engine.ordinal_encode(d.data)

@@ -130,9 +130,10 @@ int gcsl_gauss_skeleton_noalloc(const double *C, int32_t p, int64_t n_obs, const
  *          or F64 holding integers
  *   codes  device out, column j at codes + j * ldc (the layout gcsl_disc_skeleton reads)
  *   dims   device p uint8 out
+ *   workspace  device scratch of gcsl_encode_workspace_bytes(p) bytes, 256-byte aligned
  * A column with more than 255 distinct values, a value range of 4096 or more, or a
  * non-integer value returns GCSL_ERR_UNSUPPORTED.  Synchronises `stream`. */
-size_t gcsl_encode_workspace_bytes(void);
+size_t gcsl_encode_workspace_bytes(int32_t p);
 int gcsl_ordinal_encode(const void *X, int32_t dtype, int64_t n, int32_t p, int64_t ld, uint8_t *codes, int64_t ldc,
                         uint8_t *dims, void *workspace, size_t workspace_bytes, void *stream);
 
