@@ -97,7 +97,11 @@ __global__ void __launch_bounds__(256) enc_bits_kernel(const T *__restrict__ X, 
             long long v;
             enc_value(X[t * ld + j], v);
             const unsigned long long o = (unsigned long long)v - (unsigned long long)base;
-            if (o < ENC_RANGE) atomicOr(&bits[lane][o >> 5], 1u << (o & 31));
+            // values repeat: set a bit only when it is not set yet (few atomics)
+            if (o < ENC_RANGE) {
+                const unsigned bit = 1u << (o & 31);
+                if (!(bits[lane][o >> 5] & bit)) atomicOr(&bits[lane][o >> 5], bit);
+            }
         }
     }
     __syncthreads();
@@ -171,10 +175,15 @@ __global__ void __launch_bounds__(256) enc_codes_kernel(const T *__restrict__ X,
         __syncthreads();
         {
             const int c = threadIdx.x >> 3, g = threadIdx.x & 7;  // column, 4-sample group
-            if (j0 + c < p) {
-                for (int e = 0; e < 4; ++e) {
-                    const long long t = ts + g * 4 + e;
-                    if (t < t1) codes[(size_t)(j0 + c) * ldc + t] = tile[g * 4 + e][c];
+            const long long t = ts + g * 4;
+            if (j0 + c < p && t < t1) {
+                uint8_t *dst = codes + (size_t)(j0 + c) * ldc + t;
+                if (t + 4 <= t1 && ((reinterpret_cast<uintptr_t>(dst) & 3u) == 0)) {
+                    *reinterpret_cast<uint32_t *>(dst) = (uint32_t)tile[g * 4][c] | ((uint32_t)tile[g * 4 + 1][c] << 8) |
+                                                         ((uint32_t)tile[g * 4 + 2][c] << 16) |
+                                                         ((uint32_t)tile[g * 4 + 3][c] << 24);
+                } else {
+                    for (int e = 0; e < 4 && t + e < t1; ++e) dst[e] = tile[g * 4 + e][c];
                 }
             }
         }
