@@ -98,6 +98,54 @@ __device__ double pchisq_dev(double x, long long df) {
     return __dadd_rn(__dmul_rn(c, y), s);
 }
 
+// pchisq_dev by the 32 lanes of one warp, with the same result bit for bit: the
+// quotients a / z (or logarithms log z) of the series are independent and computed one
+// per lane, and the recurrence and the sums run in the same order on every lane.  On a
+// GPU whose FP64 pipe is 1/64 of its FP32 pipe this takes the divisions off the serial
+// path.  All lanes of the warp must call it; every lane returns the value.
+__device__ double pchisq_warp(double x, long long df) {
+    const int lane = threadIdx.x & 31;
+    if (x <= 0.0 || df < 1) return 1.0;
+    const double a = 0.5 * x;
+    const bool even = (df & 1) == 0;
+    const double y = (df > 1) ? ex_dev(-a) : 0.0;
+    double s = even ? y : 2.0 * poz_dev(-sqrt(x));
+    if (df <= 2) return s;
+    const double half = 0.5 * ((double)df - 1.0);
+    const double z0 = even ? 1.0 : 0.5;
+    const long long K = (long long)floor(half - z0) + 1;  // iterations z = z0, z0 + 1, .. <= half
+    if (a > 20.0) {
+        double e = even ? 0.0 : 0.5723649429247000870717135;
+        const double c = log(a);
+        for (long long k0 = 0; k0 < K; k0 += 32) {
+            const long long k = k0 + lane;
+            const double z = z0 + (double)k;
+            const double lz = k < K ? log(z) : 0.0;
+            double ek = 0.0;
+            const int m = (int)(K - k0 < 32 ? K - k0 : 32);
+            for (int q = 0; q < m; ++q) {
+                e = __dadd_rn(__shfl_sync(GCSL_FULL_MASK, lz, q), e);
+                if (lane == q) ek = e;
+            }
+            const double term = k < K ? ex_dev(__dsub_rn(__dsub_rn(__dmul_rn(c, z), a), ek)) : 0.0;
+            for (int q = 0; q < m; ++q) s = __dadd_rn(s, __shfl_sync(GCSL_FULL_MASK, term, q));
+        }
+        return s;
+    }
+    double e = even ? 1.0 : 0.5641895835477562869480795 / sqrt(a);
+    double c = 0.0;
+    for (long long k0 = 0; k0 < K; k0 += 32) {
+        const long long k = k0 + lane;
+        const double q_k = k < K ? a / (z0 + (double)k) : 0.0;
+        const int m = (int)(K - k0 < 32 ? K - k0 : 32);
+        for (int q = 0; q < m; ++q) {
+            e = __dmul_rn(e, __shfl_sync(GCSL_FULL_MASK, q_k, q));
+            c = __dadd_rn(c, e);
+        }
+    }
+    return __dadd_rn(__dmul_rn(c, y), s);
+}
+
 // ------------------------------------------------------------ test kernel
 
 __device__ __forceinline__ void tri_pair(long long t, int &vi, int &vj) {
@@ -206,10 +254,59 @@ __device__ double stratum_chi2(const uint32_t *Ts, int di, int dj) {
     return part;
 }
 
-// Statistic of the counted table: strata in parallel, then added in ascending s by
-// thread 0 (the return value is meaningful in thread 0 only).
+// stratum_chi2 by the 32 lanes of one warp (di, dj <= 32), bit for bit: lane a / b holds
+// the row / column sums, every lane one cell's term (its two divisions), and the terms
+// are added in (a, b) order as in stratum_chi2.  The sum is meaningful in every lane.
+__device__ double stratum_chi2_warp(const uint32_t *Ts, int di, int dj) {
+    const int lane = threadIdx.x & 31;
+    uint32_t ma = 0, mb = 0;
+    if (lane < di)
+        for (int b = 0; b < dj; ++b) ma += Ts[lane * dj + b];
+    if (lane < dj)
+        for (int a = 0; a < di; ++a) mb += Ts[a * dj + lane];
+    uint32_t mt = lane < di ? ma : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mt += __shfl_xor_sync(GCSL_FULL_MASK, mt, o);
+    if (mt == 0) return 0.0;
+    double part = 0.0;
+    const int cells = di * dj;
+    for (int k0 = 0; k0 < cells; k0 += 32) {
+        const int k = k0 + lane;
+        const int a = k < cells ? k / dj : 0, b = k < cells ? k - (k / dj) * dj : 0;
+        const uint32_t mak = __shfl_sync(GCSL_FULL_MASK, ma, a), mbk = __shfl_sync(GCSL_FULL_MASK, mb, b);
+        double term = 0.0;
+        bool use = false;
+        if (k < cells) {
+            const double e = __ddiv_rn(__dmul_rn((double)mak, (double)mbk), (double)mt);
+            if (e != 0.0) {
+                const double d = __dsub_rn((double)Ts[k], e);
+                term = __ddiv_rn(__dmul_rn(d, d), e);
+                use = true;
+            }
+        }
+        const unsigned um = __ballot_sync(GCSL_FULL_MASK, use);
+        const int m = cells - k0 < 32 ? cells - k0 : 32;
+        for (int q = 0; q < m; ++q) {
+            const double t = __shfl_sync(GCSL_FULL_MASK, term, q);
+            if ((um >> q) & 1u) part = __dadd_rn(part, t);
+        }
+    }
+    return part;
+}
+
+// Statistic of the counted table: strata in parallel (a warp per stratum), then added in
+// ascending s by thread 0 (the return value is meaningful in thread 0 only).
 __device__ double table_chi2(const uint32_t *sm_tab, int dim_s, int di, int dj, double *s_part) {
-    for (int s = threadIdx.x; s < dim_s; s += blockDim.x) s_part[s] = stratum_chi2(sm_tab + (size_t)s * di * dj, di, dj);
+    if (di <= 32 && dj <= 32) {
+        const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+        for (int s = warp; s < dim_s; s += nwarps) {
+            const double part = stratum_chi2_warp(sm_tab + (size_t)s * di * dj, di, dj);
+            if ((threadIdx.x & 31) == 0) s_part[s] = part;
+        }
+    } else {
+        for (int s = threadIdx.x; s < dim_s; s += blockDim.x)
+            s_part[s] = stratum_chi2(sm_tab + (size_t)s * di * dj, di, dj);
+    }
     __syncthreads();
     double chi = 0.0;
     if (threadIdx.x == 0)
@@ -303,9 +400,12 @@ __global__ void __launch_bounds__(256) disc_test_kernel(DiscLevelArgs A) {
                     &s_bad);
         const double chi = table_chi2(sm_tab, dim_s, di, dj, s_part);
         if (tid == 0 && s_bad) set_status(st, GCSL_ERR_INVALID_ARG);
-        if (tid == 0) {
+        double pv = 1.0;
+        if (tid < 32) {  // warp 0: the p-value's series split over the lanes
             const long long df = (long long)(di - 1) * (long long)(dj - 1) * (long long)dim_s;
-            const double pv = pchisq_dev(chi, df);
+            pv = pchisq_warp(__shfl_sync(GCSL_FULL_MASK, chi, 0), df);
+        }
+        if (tid == 0) {
             const int lo = vi < vj ? vi : vj, hi = vi < vj ? vj : vi;
             const size_t ix = (size_t)lo * A.p + hi;
             if (L == 0) {

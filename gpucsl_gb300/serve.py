@@ -3,13 +3,13 @@
 Requests (Gaussian: FP32 samples; discrete: ordinal codes and cardinalities) arrive at
 arbitrary times.  A request is admitted once the device memory it needs fits in the
 budget next to the requests in flight (first come, first served: a large request at
-the head waits rather than being overtaken).  Two workers own one CUDA stream each:
+the head waits rather than being overtaken).  Workers own one CUDA stream each:
 
 * the Gaussian worker takes every admitted Gaussian request that is waiting when it
   becomes free and solves them as one `GaussianBatch` (batched tensor-core correlation
   + batched level loop), so requests that arrive while a batch runs join the next one;
-* the discrete worker solves admitted discrete requests one after another through
-  `DiscreteSolver`.
+* the discrete workers (three by default) each take the next admitted discrete request
+  and solve it through `DiscreteSolver`, so discrete solves overlap on the device.
 
 Latency is measured from a request's arrival to the moment its results are on the
 host.  `serve_plain` serves the same trace one request at a time through the plain
@@ -107,10 +107,14 @@ class _Admission:
 class SkeletonServer:
     """Continuous-batching server for one device."""
 
-    def __init__(self, budget_bytes: float = 120e9, max_batch: int = 256, precision: str = "f64"):
+    def __init__(self, budget_bytes: float = 120e9, max_batch: int = 256, precision: str = "f64",
+                 discrete_workers: int = 3):
         self.budget = int(budget_bytes)
         self.max_batch = int(max_batch)
         self.precision = precision
+        # discrete solves of different requests overlap on the device: each worker owns a
+        # stream, and one solve's host reads between levels leave the GPU to the others
+        self.discrete_workers = max(1, int(discrete_workers))
 
     # ----------------------------------------------------------- workers
     def _guard(self, fn, errors, stop, *args):
@@ -189,10 +193,12 @@ class SkeletonServer:
         t0 = clock()
         wg = threading.Thread(target=self._guard, args=(self._gaussian_worker, errors, stop, qg, cvg, stop, adm, out,
                                                         t0, clock), daemon=True)
-        wd = threading.Thread(target=self._guard, args=(self._discrete_worker, errors, stop, qd, cvd, stop, adm, out,
-                                                        t0, clock), daemon=True)
+        wds = [threading.Thread(target=self._guard, args=(self._discrete_worker, errors, stop, qd, cvd, stop, adm,
+                                                          out, t0, clock), daemon=True)
+               for _ in range(self.discrete_workers)]
         wg.start()
-        wd.start()
+        for wd in wds:
+            wd.start()
         pending = deque(sorted(trace, key=lambda r: r.arrival))
         waiting: deque = deque()  # arrived, not admitted (FIFO)
         try:
@@ -228,7 +234,8 @@ class SkeletonServer:
             with cvd:
                 cvd.notify_all()
             wg.join()
-            wd.join()
+            for wd in wds:
+                wd.join()
         if errors:
             raise errors[0]
         return out
