@@ -55,6 +55,30 @@ __host__ inline L0Bounds level0_bounds(double t0sq) {
     return B;
 }
 
+// Programmatic dependent launch.  A kernel launched by launch_pdl may begin while the
+// kernel before it in the stream is still running: it must call pdl_wait() before it
+// reads anything that kernel wrote (a no-op when launched normally), and pdl_trigger()
+// lets the kernel after it begin early in turn.  The waits are the hardware's grid
+// dependency, which ends when the previous grid has completed.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+__host__ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                       Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // Device-side state of one skeleton solve.  Per-level slots are written once per
 // level, so no counter has to be reset between levels.
 struct DevState {

@@ -31,6 +31,8 @@ __global__ void gauss_level0_kernel(const double *__restrict__ C, int p, double 
 // once when the level loop is already finished.
 __global__ void compact_kernel(const uint16_t *__restrict__ G, int p, int *__restrict__ adj, int *__restrict__ up,
                                DevState *st, int level, int2 *elist) {
+    pdl_wait();
+    pdl_trigger();
     if (st != nullptr && st->done) return;
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -63,6 +65,8 @@ __device__ __forceinline__ void recompact_blocks(const uint16_t *__restrict__ G,
 
 __global__ void recompact_kernel(const uint16_t *__restrict__ G, int p, int *__restrict__ adj, int *__restrict__ up,
                                  DevState *st, int level, int2 *elist) {
+    pdl_wait();
+    pdl_trigger();
     recompact_blocks(G, p, adj, up, st, level, elist, (int)blockIdx.x, (int)gridDim.x);
 }
 
@@ -77,13 +81,13 @@ __global__ void row_scan_kernel(const T *__restrict__ cnt, int p, long long *__r
 template <int L, bool MIXED>
 __global__ void __launch_bounds__(256) gauss_level_reg_kernel(LevelCtx x) {
     __shared__ BinomRows sb;
+    if (L >= 2) binom_rows_load(sb);  // constant table: before the wait on the previous kernel
+    pdl_wait();
+    pdl_trigger();
+    if (L >= 2) __syncthreads();
     if (!level_active(x.st, L, x.tau_valid)) return;
     const long long n_edges = (long long)x.st->edges[L];  // filled by the (re)compaction
     if ((long long)blockIdx.x * (blockDim.x >> 5) >= n_edges) return;  // no edge for this block
-    if (L >= 2) {
-        binom_rows_load(sb);
-        __syncthreads();
-    }
     level_edge_phase<L, MIXED>(x, L >= 2 ? &sb : nullptr, ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
                                ((long long)gridDim.x * blockDim.x) >> 5);
 }
@@ -91,14 +95,14 @@ __global__ void __launch_bounds__(256) gauss_level_reg_kernel(LevelCtx x) {
 template <int L, bool MIXED>
 __global__ void __launch_bounds__(256) gauss_level_units_kernel(LevelCtx x) {
     __shared__ BinomRows sb;
+    if (L >= 2) binom_rows_load(sb);  // constant table: before the wait on the level kernel
+    pdl_wait();
+    pdl_trigger();
+    if (L >= 2) __syncthreads();
     if (!level_active(x.st, L, x.tau_valid)) return;
     const long long reserved = (long long)x.st->units[L];
     const long long nu = reserved < x.ck.unit_cap ? reserved : x.ck.unit_cap;
     if ((long long)blockIdx.x * (blockDim.x >> 5) >= nu) return;
-    if (L >= 2) {
-        binom_rows_load(sb);
-        __syncthreads();
-    }
     level_unit_phase<L, MIXED>(x, L >= 2 ? &sb : nullptr, ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
                                ((long long)gridDim.x * blockDim.x) >> 5);
 }
@@ -308,17 +312,18 @@ cudaError_t launch_compact(const uint16_t *G, int p, int *adj, int *up, DevState
                            cudaStream_t s) {
     const int threads = 256, wpb = threads / 32;
     int blocks = (p + wpb - 1) / wpb;
-    compact_kernel<<<blocks, threads, 0, s>>>(G, p, adj, up, st, level, elist);
+    const cudaError_t e = launch_pdl(compact_kernel, dim3(blocks), dim3(threads), 0, s, G, p, adj, up, st, level, elist);
     note_launch(1);
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_recompact(const uint16_t *G, int p, int *adj, int *up, DevState *st, int level, int2 *elist,
                              cudaStream_t s) {
     const int threads = 256, wpb = threads / 32;
-    recompact_kernel<<<(p + wpb - 1) / wpb, threads, 0, s>>>(G, p, adj, up, st, level, elist);
+    const cudaError_t e =
+        launch_pdl(recompact_kernel, dim3((p + wpb - 1) / wpb), dim3(threads), 0, s, G, p, adj, up, st, level, elist);
     note_launch(1);
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_scan_int(const int *cnt, int p, long long *prefix, DevState *st, cudaStream_t s) {
@@ -383,16 +388,20 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
     // chunked edges: the unit kernel follows the level kernel (it returns at once when no
     // edge was chunked); one resident wave of warps strides over the units
     const int ublocks = num_sms * (L >= 4 ? 4 : 2);
-#define GCSL_LVL(K)                                                                                \
-    case K:                                                                                        \
-        if (mixed) {                                                                               \
-            gauss_level_reg_kernel<K, true><<<blocks, threads, 0, s>>>(x);                         \
-            if (ck.heavy != nullptr) gauss_level_units_kernel<K, true><<<ublocks, threads, 0, s>>>(x); \
-        } else {                                                                                   \
-            gauss_level_reg_kernel<K, false><<<blocks, threads, 0, s>>>(x);                        \
-            if (ck.heavy != nullptr) gauss_level_units_kernel<K, false><<<ublocks, threads, 0, s>>>(x); \
-        }                                                                                          \
-        if (ck.heavy != nullptr) note_launch(1);                                                   \
+    cudaError_t el = cudaSuccess;
+#define GCSL_LVL(K)                                                                                         \
+    case K:                                                                                                 \
+        if (mixed) {                                                                                        \
+            el = launch_pdl(gauss_level_reg_kernel<K, true>, dim3(blocks), dim3(threads), 0, s, x);         \
+            if (el == cudaSuccess && ck.heavy != nullptr)                                                   \
+                el = launch_pdl(gauss_level_units_kernel<K, true>, dim3(ublocks), dim3(threads), 0, s, x);  \
+        } else {                                                                                            \
+            el = launch_pdl(gauss_level_reg_kernel<K, false>, dim3(blocks), dim3(threads), 0, s, x);        \
+            if (el == cudaSuccess && ck.heavy != nullptr)                                                   \
+                el = launch_pdl(gauss_level_units_kernel<K, false>, dim3(ublocks), dim3(threads), 0, s, x); \
+        }                                                                                                   \
+        if (ck.heavy != nullptr) note_launch(1);                                                            \
+        if (el != cudaSuccess) return note_error("gauss level kernel launch", el);                          \
         break;
     switch (L) {
         GCSL_LVL(1)
