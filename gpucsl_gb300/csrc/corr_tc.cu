@@ -21,6 +21,7 @@
 // the rounding of an FP64 GEMM.  Tile: 128 rows (i) x 64 columns (j), 7 accumulators
 // = 448 TMEM columns, K staged 32 samples at a time into two shared-memory buffers
 // (84 KB each) while the tensor core consumes the other.
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -98,6 +99,8 @@ constexpr int OZ_STAT_ROWS = 512;  // samples per column-statistics block
 
 template <class Src>
 __global__ void colstats_init_kernel(Src src) {
+    pdl_wait();
+    pdl_trigger();
     long long lb;
     const OzJob &J = src.get(blockIdx.x, lb);
     const int j = (int)lb * blockDim.x + threadIdx.x;
@@ -114,6 +117,8 @@ template <typename T, class Src>
 __global__ void colstats_kernel(Src src) {
     __shared__ double ssum[8][32];
     __shared__ long long smin[8][32], smax[8][32];
+    pdl_wait();
+    pdl_trigger();
     long long lb;
     const OzJob &Jb = src.get(blockIdx.x, lb);
     const T *__restrict__ X = static_cast<const T *>(Jb.X);
@@ -158,6 +163,8 @@ __global__ void colstats_kernel(Src src) {
 // max(fl(max - mean), fl(mean - min)) (rounding is monotone), so |x - mean| < 2^E.
 template <class Src>
 __global__ void col_mean_exp_kernel(Src src) {
+    pdl_wait();
+    pdl_trigger();
     long long lb;
     const OzJob &J = src.get(blockIdx.x, lb);
     const int p = J.p;
@@ -181,6 +188,8 @@ __global__ void col_mean_exp_kernel(Src src) {
 template <typename T, class Src>
 __global__ void digit_split_kernel(Src src) {
     __shared__ int16_t tile[OZ_S][32][33];  // [digit][sample][column]
+    pdl_wait();
+    pdl_trigger();
     long long lb;
     const OzJob &Jb = src.get(blockIdx.x, lb);
     const T *__restrict__ X = static_cast<const T *>(Jb.X);
@@ -323,6 +332,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
     __shared__ OzJob s_job;
     __shared__ long long s_lb;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    pdl_wait();
+    pdl_trigger();
     if (tid == 0) {
         long long lb0;
         s_job = src.get(blockIdx.x, lb0);
@@ -492,6 +503,8 @@ __device__ __forceinline__ double oz_cov(const long long *__restrict__ part_hi, 
 
 template <class Src>
 __global__ void ozaki_diag_kernel(Src src) {
+    pdl_wait();
+    pdl_trigger();
     long long lb;
     const OzJob &J = src.get(blockIdx.x, lb);
     const int i = (int)lb * blockDim.x + threadIdx.x;
@@ -506,6 +519,8 @@ __global__ void ozaki_diag_kernel(Src src) {
 template <class Src>
 __global__ void ozaki_finish_kernel(Src src) {
     __shared__ double tv[32][33];
+    pdl_wait();
+    pdl_trigger();
     long long lb;
     const OzJob &J = src.get(blockIdx.x, lb);
     const int p = J.p;
@@ -630,20 +645,37 @@ static cudaError_t set_ozaki_smem() {
 }
 
 // Stage launches shared by the single-job and batched paths; nb[] = blocks per stage.
+// One stage: the single-job path launches with programmatic dependent launch (each
+// kernel waits for its predecessor with pdl_wait); the batched path, captured into CUDA
+// graphs, launches plainly.
+template <class Src, typename K>
+static cudaError_t launch_stage(K kernel, long long blocks, int threads, size_t smem, const Src &src, cudaStream_t s,
+                                const char *what) {
+    cudaError_t e;
+    if constexpr (std::is_same<Src, OneJob>::value) {
+        e = launch_pdl(kernel, dim3((unsigned)blocks), dim3(threads), smem, s, src);
+    } else {
+        kernel<<<(unsigned)blocks, threads, smem, s>>>(src);
+        e = cudaGetLastError();
+    }
+    return note_error(what, e);
+}
+
+// Stage launches shared by the single-job and batched paths; nb[] = blocks per stage.
 template <class Src>
 static cudaError_t launch_digits(const Src &src, const long long *nb, int dtype, cudaStream_t s) {
     note_launch(4);
-    colstats_init_kernel<Src><<<(unsigned)nb[OZ_INIT], 256, 0, s>>>(src);
-    cudaError_t e = note_error("colstats_init_kernel launch", cudaGetLastError());
+    cudaError_t e = launch_stage(colstats_init_kernel<Src>, nb[OZ_INIT], 256, 0, src, s, "colstats_init_kernel launch");
     if (e != cudaSuccess) return e;
-    if (dtype == GCSL_DTYPE_F64) colstats_kernel<double, Src><<<(unsigned)nb[OZ_STATS], 256, 0, s>>>(src);
-    else colstats_kernel<float, Src><<<(unsigned)nb[OZ_STATS], 256, 0, s>>>(src);
-    if ((e = note_error("colstats_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
-    col_mean_exp_kernel<Src><<<(unsigned)nb[OZ_MEAN], 256, 0, s>>>(src);
-    if ((e = note_error("col_mean_exp_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
-    if (dtype == GCSL_DTYPE_F64) digit_split_kernel<double, Src><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(src);
-    else digit_split_kernel<float, Src><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(src);
-    return note_error("digit_split_kernel launch", cudaGetLastError());
+    e = dtype == GCSL_DTYPE_F64
+            ? launch_stage(colstats_kernel<double, Src>, nb[OZ_STATS], 256, 0, src, s, "colstats_kernel launch")
+            : launch_stage(colstats_kernel<float, Src>, nb[OZ_STATS], 256, 0, src, s, "colstats_kernel launch");
+    if (e != cudaSuccess) return e;
+    e = launch_stage(col_mean_exp_kernel<Src>, nb[OZ_MEAN], 256, 0, src, s, "col_mean_exp_kernel launch");
+    if (e != cudaSuccess) return e;
+    return dtype == GCSL_DTYPE_F64
+               ? launch_stage(digit_split_kernel<double, Src>, nb[OZ_DIGITS], 256, 0, src, s, "digit_split_kernel launch")
+               : launch_stage(digit_split_kernel<float, Src>, nb[OZ_DIGITS], 256, 0, src, s, "digit_split_kernel launch");
 }
 
 template <class Src>
@@ -651,12 +683,12 @@ static cudaError_t launch_product(const Src &src, const long long *nb, cudaStrea
     note_launch(3);
     cudaError_t e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<Src>());
     if (e != cudaSuccess) return e;
-    corr_ozaki_kernel<Src><<<(unsigned)nb[OZ_PRODUCT], OZ_THREADS, OZ_NST * OZ_STAGE_BYTES, s>>>(src);
-    if ((e = note_error("corr_ozaki_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
-    ozaki_diag_kernel<Src><<<(unsigned)nb[OZ_DIAG], 256, 0, s>>>(src);
-    if ((e = note_error("ozaki_diag_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
-    ozaki_finish_kernel<Src><<<(unsigned)nb[OZ_FINISH], 256, 0, s>>>(src);
-    return note_error("ozaki_finish_kernel launch", cudaGetLastError());
+    e = launch_stage(corr_ozaki_kernel<Src>, nb[OZ_PRODUCT], OZ_THREADS, (size_t)OZ_NST * OZ_STAGE_BYTES, src, s,
+                     "corr_ozaki_kernel launch");
+    if (e != cudaSuccess) return e;
+    e = launch_stage(ozaki_diag_kernel<Src>, nb[OZ_DIAG], 256, 0, src, s, "ozaki_diag_kernel launch");
+    if (e != cudaSuccess) return e;
+    return launch_stage(ozaki_finish_kernel<Src>, nb[OZ_FINISH], 256, 0, src, s, "ozaki_finish_kernel launch");
 }
 
 static bool one_job(OneJob &o, long long *nb, const void *X, long long n, int p, long long ldx, double *C, void *ws,
