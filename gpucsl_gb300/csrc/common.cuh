@@ -55,6 +55,21 @@ __host__ inline L0Bounds level0_bounds(double t0sq) {
     return B;
 }
 
+// fl32(v) rounded to nearest even, from the bits (results in the normal float range;
+// others, and NaN / inf, through the conversion instruction): integer work instead of a
+// conversion on the FP64 pipe, which is 1/64 of the FP32 pipe on GB300.
+__device__ __forceinline__ float f64_to_f32_rn(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    if (e < -126 || e > 127) return (float)v;
+    const unsigned long long m = b & 0xfffffffffffffull;
+    unsigned r = (unsigned)(m >> 29);
+    const unsigned long long rem = m & ((1ull << 29) - 1ull), half = 1ull << 28;
+    r += (rem > half || (rem == half && (r & 1u))) ? 1u : 0u;
+    const unsigned fb = ((unsigned)(b >> 63) << 31) | (((unsigned)(e + 127) << 23) + r);  // a carry bumps the exponent
+    return __uint_as_float(fb);
+}
+
 // Programmatic dependent launch.  A kernel launched by launch_pdl may begin while the
 // kernel before it in the stream is still running: it must call pdl_wait() before it
 // reads anything that kernel wrote (a no-op when launched normally), and pdl_trigger()

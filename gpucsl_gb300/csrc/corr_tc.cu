@@ -488,6 +488,54 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
 
 __device__ __forceinline__ double pow2(int e) { return __longlong_as_double((long long)(1023 + e) << 52); }
 
+// fl(2^28 H + L) for integers H, L, rounded to nearest even once, from the exact 128-bit
+// sum in integer arithmetic (the value fma((double)H, 2^28, (double)L) gives when H and
+// L convert exactly) -- GB300's FP64 pipe is 1/64 of its integer and FP32 pipes.
+__device__ __forceinline__ double exact_sum_to_f64(long long H, long long L) {
+    unsigned long long lo = (unsigned long long)H << 28;
+    long long hi = H >> 36;
+    const unsigned long long lo2 = lo + (unsigned long long)L;
+    hi += (L >> 63) + (lo2 < lo ? 1 : 0);
+    lo = lo2;
+    const bool neg = hi < 0;
+    unsigned long long uh = (unsigned long long)hi;
+    if (neg) {
+        lo = ~lo + 1ull;
+        uh = ~uh + (lo == 0ull ? 1ull : 0ull);
+    }
+    if (uh == 0ull && lo == 0ull) return 0.0;
+    const int nb = uh ? 128 - __clzll((long long)uh) : 64 - __clzll((long long)lo);  // bit length
+    unsigned long long m;
+    if (nb <= 53) {
+        m = lo << (53 - nb);
+    } else {
+        const int sh = nb - 53;  // 1 .. 75
+        m = sh < 64 ? (lo >> sh) | (uh << (64 - sh)) : uh >> (sh - 64);
+        const int rb = sh - 1;   // round bit position
+        const bool round_bit = rb < 64 ? (lo >> rb) & 1ull : (uh >> (rb - 64)) & 1ull;
+        const bool sticky = rb <= 64 ? (rb == 64 ? lo != 0ull : (lo & ((1ull << rb) - 1ull)) != 0ull)
+                                     : lo != 0ull || (uh & ((1ull << (rb - 64)) - 1ull)) != 0ull;
+        m += (round_bit && (sticky || (m & 1ull))) ? 1ull : 0ull;
+    }
+    int e = nb - 1;
+    if (m >> 53) {  // rounding carried into a new bit
+        m >>= 1;
+        ++e;
+    }
+    const unsigned long long bits =
+        (neg ? 0x8000000000000000ull : 0ull) | ((unsigned long long)(e + 1023) << 52) | (m & 0xfffffffffffffull);
+    return __longlong_as_double((long long)bits);
+}
+
+// x 2^e for a normal x whose result stays normal (exact): exponent arithmetic on the bits;
+// anything else through the multiplication.
+__device__ __forceinline__ double scale_pow2(double x, int e) {
+    const long long b = __double_as_longlong(x);
+    const int ef = (int)((b >> 52) & 0x7ff);
+    if (ef == 0 || ef == 0x7ff || ef + e < 1 || ef + e > 2046) return x * pow2(e);
+    return __longlong_as_double(b + ((long long)e << 52));
+}
+
 // Covariance of (i, j) from the exact split sums: (2^28 H + L) 2^(E_i + E_j - 56) / (n - 1).
 __device__ __forceinline__ double oz_cov(const long long *__restrict__ part_hi, const long long *__restrict__ part_lo,
                                          const OzDims &D, const int *__restrict__ expo, double scale, int i, int j) {
@@ -497,8 +545,8 @@ __device__ __forceinline__ double oz_cov(const long long *__restrict__ part_hi, 
         H += part_hi[ix];
         Lo += part_lo[ix];
     }
-    const double val = fma((double)H, 268435456.0, (double)Lo);  // exact terms, one rounding
-    return (val * pow2(expo[i] + expo[j] - 56)) * scale;
+    const double val = exact_sum_to_f64(H, Lo);  // exact terms, one rounding
+    return scale_pow2(val, expo[i] + expo[j] - 56) * scale;
 }
 
 template <class Src>
@@ -539,10 +587,14 @@ __global__ void ozaki_finish_kernel(Src src) {
         double v = 0.0;
         if (i < p && j < p && (bi != bj || i <= j)) {
             v = oz_cov(J.phi, J.plo, J.D, J.expo, scale, i, j) * J.inv_sd[i] * J.inv_sd[j];
-            v = fmin(fmax(v, -1.0), 1.0);
+            // clip to [-1, 1] on the bits, as fmin(fmax(v, -1), 1) (NaN gives -1)
+            const unsigned long long vb = (unsigned long long)__double_as_longlong(v);
+            const unsigned long long mag = vb & 0x7fffffffffffffffull;
+            if (mag > 0x7ff0000000000000ull) v = -1.0;
+            else if (mag > 0x3ff0000000000000ull) v = (vb >> 63) ? -1.0 : 1.0;
             if (failed) v = __longlong_as_double(0x7ff8000000000000ll);
             J.C[(size_t)i * p + j] = v;
-            if (J.C32 != nullptr) J.C32[(size_t)i * p + j] = (float)v;
+            if (J.C32 != nullptr) J.C32[(size_t)i * p + j] = f64_to_f32_rn(v);
         }
         tv[r][tx] = v;
     }
@@ -551,7 +603,7 @@ __global__ void ozaki_finish_kernel(Src src) {
         const int j = bj * 32 + r, i = bi * 32 + tx;  // lower triangle (j, i)
         if (i < p && j < p && (bi != bj || j > i)) {
             J.C[(size_t)j * p + i] = tv[tx][r];
-            if (J.C32 != nullptr) J.C32[(size_t)j * p + i] = (float)tv[tx][r];
+            if (J.C32 != nullptr) J.C32[(size_t)j * p + i] = f64_to_f32_rn(tv[tx][r]);
         }
     }
 }

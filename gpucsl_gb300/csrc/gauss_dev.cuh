@@ -35,12 +35,13 @@ __device__ __forceinline__ void level0_tile(const double *__restrict__ C, int p,
     for (int r = ty; r < 32; r += 8) {
         const int i = bi * 32 + r, j = bj * 32 + tx;
         uint16_t g = 0;
-        if (C32 != nullptr && i == j && i < p) C32[(size_t)i * p + i] = (float)__ldg(C + (size_t)i * p + i);
+        if (C32 != nullptr && i == j && i < p) C32[(size_t)i * p + i] = f64_to_f32_rn(__ldg(C + (size_t)i * p + i));
         if (i < p && j < p && i < j) {
             const double c = __ldg(C + (size_t)i * p + j);
             if (C32 != nullptr) {  // the FP32 copy of C for the FP32-first levels, both triangles
-                C32[(size_t)i * p + j] = (float)c;
-                tc[r][tx] = (float)c;
+                const float c32 = f64_to_f32_rn(c);
+                C32[(size_t)i * p + j] = c32;
+                tc[r][tx] = c32;
             }
             // Z0 = atanh-like in |r| on [0, 1): Z0 < tau0 <=> r^2 < tanh(tau0)^2, decided
             // on the bits of |r| outside the knife edge; the knife edge, |r| >= 1 and NaN
