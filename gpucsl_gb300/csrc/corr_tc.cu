@@ -187,7 +187,7 @@ __global__ void col_mean_exp_kernel(Src src) {
 // block.  One CTA handles 32 samples x 32 columns.
 template <typename T, class Src>
 __global__ void digit_split_kernel(Src src) {
-    __shared__ int16_t tile[OZ_S][32][33];  // [digit][sample][column]
+    __shared__ int16_t tile[OZ_S][32][33];  // [digit][sample][column]; the top digit reaches 128
     pdl_wait();
     pdl_trigger();
     long long lb;
@@ -220,15 +220,25 @@ __global__ void digit_split_kernel(Src src) {
             if (sh < 63) mag = (m + (1ll << (sh - 1))) >> sh;
             I = bits < 0 ? -mag : mag;
         }
+        // digits by rounding half up (arithmetic shifts); after the third digit the
+        // remainder is below 2^27 in magnitude and the rest runs in 32-bit arithmetic
         long long rem = I;
 #pragma unroll
-        for (int k = 0; k < OZ_S - 1; ++k) {
+        for (int k = 0; k < 3; ++k) {
             const int sh = 7 * (OZ_S - 1 - k);
-            const long long d = (rem + (1ll << (sh - 1))) >> sh;  // round half up (arithmetic shift)
+            const long long d = (rem + (1ll << (sh - 1))) >> sh;
             rem -= d * (1ll << sh);
             tile[k][r][tx] = (int16_t)d;
         }
-        tile[OZ_S - 1][r][tx] = (int16_t)rem;
+        int rem32 = (int)rem;
+#pragma unroll
+        for (int k = 3; k < OZ_S - 1; ++k) {
+            const int sh = 7 * (OZ_S - 1 - k);
+            const int d = (rem32 + (1 << (sh - 1))) >> sh;
+            rem32 -= d * (1 << sh);
+            tile[k][r][tx] = (int16_t)d;
+        }
+        tile[OZ_S - 1][r][tx] = (int16_t)rem32;
     }
     __syncthreads();
     const int nI = p_pad / OZ_TM;
@@ -239,11 +249,15 @@ __global__ void digit_split_kernel(Src src) {
         const int j = j0 + c;
         const long long t = t0 + g8 * 8;
         if (j >= p_pad || t >= n_pad) continue;
+        // small integers to float exactly by the 1.5 * 2^23 offset (an integer add and an
+        // FP32 subtraction); a digit (|d| <= 128) has at most 8 significant bits, so the
+        // upper half of its float is the exact BF16
         uint32_t word[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-            const float lo = (float)tile[k][g8 * 8 + 2 * e][c], hi = (float)tile[k][g8 * 8 + 2 * e + 1][c];
-            word[e] = (__float_as_uint(lo) >> 16) | (__float_as_uint(hi) & 0xffff0000u);  // exact BF16 pair
+            const float lo = __int_as_float(0x4B400000 + (int)tile[k][g8 * 8 + 2 * e][c]) - 12582912.0f;
+            const float hi = __int_as_float(0x4B400000 + (int)tile[k][g8 * 8 + 2 * e + 1][c]) - 12582912.0f;
+            word[e] = (__float_as_uint(lo) >> 16) | (__float_as_uint(hi) & 0xffff0000u);
         }
         const long long q = t / 16;
         const size_t off = (((size_t)k * nI + j / OZ_TM) * nq + q) * 4096 +

@@ -376,32 +376,31 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
                                double *r2min, int *sep_dense, int max_level, int *rec_pool, long long rec_cap,
                                DevState *st, int num_sms, const float *C32, int *qbuf, long long qcap,
                                const ChunkBufs &ck, cudaStream_t s) {
-    // register-heavy upper levels run 128-thread blocks so a full wave of warps is resident
-    // level 1 (tens of thousands of edges) strides over the edges with many blocks; the
-    // upper levels have a few thousand edges, one warp each: one resident wave of blocks,
-    // so no empty blocks queue behind the working ones
+    // register-heavy upper levels run 128-thread blocks
     const int threads = L >= 4 ? 128 : 256;
-    const int blocks = L == 1 ? num_sms * 8 : num_sms * (L >= 4 ? 4 : 2);
+    const int blocks = num_sms * 8;
     const bool mixed = C32 != nullptr && qbuf != nullptr;
     const LevelCtx x = level_ctx(L, C, p, adj, elist, tau, tau_valid, G, zmin, r2min, sep_dense, max_level, rec_pool,
                                  rec_cap, st, C32, qbuf, qcap, ck);
     // chunked edges: the unit kernel follows the level kernel (it returns at once when no
-    // edge was chunked); one resident wave of warps strides over the units
-    const int ublocks = num_sms * (L >= 4 ? 4 : 2);
+    // edge was chunked).  Both kernels launch 8 blocks per SM whose warps stride over the
+    // edges / units: more than one resident wave at every level's register count, so blocks
+    // of later waves pick up the work of the slow ones (measured on p = 1000: 0.771 ms per
+    // solve against 0.801 ms with one resident wave and 0.80 / 0.85 ms with 16 / 32 per SM)
     cudaError_t el = cudaSuccess;
-#define GCSL_LVL(K)                                                                                         \
-    case K:                                                                                                 \
-        if (mixed) {                                                                                        \
-            el = launch_pdl(gauss_level_reg_kernel<K, true>, dim3(blocks), dim3(threads), 0, s, x);         \
-            if (el == cudaSuccess && ck.heavy != nullptr)                                                   \
-                el = launch_pdl(gauss_level_units_kernel<K, true>, dim3(ublocks), dim3(threads), 0, s, x);  \
-        } else {                                                                                            \
-            el = launch_pdl(gauss_level_reg_kernel<K, false>, dim3(blocks), dim3(threads), 0, s, x);        \
-            if (el == cudaSuccess && ck.heavy != nullptr)                                                   \
-                el = launch_pdl(gauss_level_units_kernel<K, false>, dim3(ublocks), dim3(threads), 0, s, x); \
-        }                                                                                                   \
-        if (ck.heavy != nullptr) note_launch(1);                                                            \
-        if (el != cudaSuccess) return note_error("gauss level kernel launch", el);                          \
+#define GCSL_LVL(K)                                                                                      \
+    case K:                                                                                              \
+        if (mixed) {                                                                                     \
+            el = launch_pdl(gauss_level_reg_kernel<K, true>, dim3(blocks), dim3(threads), 0, s, x);      \
+            if (el == cudaSuccess && ck.heavy != nullptr)                                                \
+                el = launch_pdl(gauss_level_units_kernel<K, true>, dim3(blocks), dim3(threads), 0, s, x); \
+        } else {                                                                                         \
+            el = launch_pdl(gauss_level_reg_kernel<K, false>, dim3(blocks), dim3(threads), 0, s, x);     \
+            if (el == cudaSuccess && ck.heavy != nullptr)                                                \
+                el = launch_pdl(gauss_level_units_kernel<K, false>, dim3(blocks), dim3(threads), 0, s, x); \
+        }                                                                                                \
+        if (ck.heavy != nullptr) note_launch(1);                                                         \
+        if (el != cudaSuccess) return note_error("gauss level kernel launch", el);                       \
         break;
     switch (L) {
         GCSL_LVL(1)
