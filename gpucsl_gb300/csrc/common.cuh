@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cmath>
 #include <stdint.h>
 
@@ -92,6 +93,26 @@ __host__ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+// Raises `kernel`'s dynamic shared-memory limit to everything the device allows next to
+// its static shared memory, once per device (bit d of `mask`).  The attribute belongs to
+// the context, not to a host thread: raising it to one fixed maximum means concurrent
+// solves never lower it under each other's launches.
+template <typename K>
+__host__ inline cudaError_t raise_dyn_smem_limit(K kernel, std::atomic<unsigned long long> &mask) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 64) return e;
+    if ((mask.load() >> dev) & 1ull) return cudaSuccess;
+    cudaFuncAttributes fa;
+    int optin = 0;
+    e = cudaFuncGetAttributes(&fa, kernel);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    if (e == cudaSuccess) mask.fetch_or(1ull << dev);
+    return e;
 }
 
 // Device-side state of one skeleton solve.  Per-level slots are written once per

@@ -587,19 +587,16 @@ void disc_level_caps(int cap_full, int max_dim, int L, int &table_cap, int &part
 
 cudaError_t launch_disc_tests(const DiscLevelArgs &A, int num_sms, cudaStream_t s) {
     const size_t smem = (size_t)((A.table_cap + 1) & ~1) * sizeof(uint32_t) + (size_t)A.part_cap * sizeof(double);
-    static thread_local int attr_bytes = 0;
-    if ((int)smem > attr_bytes) {
-        cudaError_t e = cudaFuncSetAttribute(disc_test_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return note_error("disc_test_kernel shared memory", e);
-        attr_bytes = (int)smem;
-    }
+    static std::atomic<unsigned long long> limit_set{0};
+    const cudaError_t ea = raise_dyn_smem_limit(disc_test_kernel, limit_set);
+    if (ea != cudaSuccess) return note_error("disc_test_kernel shared memory", ea);
     int per_sm = 1;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, disc_test_kernel, 256, smem) != cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
     disc_test_kernel<<<num_sms * per_sm, 256, smem, s>>>(A);
     note_launch(1);
-    return cudaGetLastError();
+    return note_error("disc_test_kernel launch", cudaGetLastError());
 }
 
 cudaError_t launch_disc_weights(const int *adj, int p, int L, long long *w, DevState *st, cudaStream_t s) {

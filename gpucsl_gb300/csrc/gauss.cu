@@ -420,8 +420,11 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
         const int D = L + 2;
         const size_t smem = (size_t)wpb * (D * (D + 1) / 2 + 2) * sizeof(double) +
                             (size_t)wpb * (GCSL_MAX_LEVELS + 2) * sizeof(int);
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(gauss_level_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        static std::atomic<unsigned long long> limit_set{0};
+        if (smem > 48 * 1024) {
+            const cudaError_t ea = raise_dyn_smem_limit(gauss_level_smem_kernel, limit_set);
+            if (ea != cudaSuccess) return note_error("gauss_level_smem_kernel shared memory", ea);
+        }
         gauss_level_smem_kernel<<<num_sms * 4, t, smem, s>>>(C, p, adj, up, prefix, L, tau, tau_valid, G, zmin,
                                                                sep_dense, max_level, rec_pool, rec_cap, st);
     }

@@ -5,9 +5,11 @@ arbitrary times.  A request is admitted once the device memory it needs fits in 
 budget next to the requests in flight (first come, first served: a large request at
 the head waits rather than being overtaken).  Workers own one CUDA stream each:
 
-* the Gaussian worker takes every admitted Gaussian request that is waiting when it
-  becomes free and solves them as one `GaussianBatch` (batched tensor-core correlation
-  + batched level loop), so requests that arrive while a batch runs join the next one;
+* the Gaussian workers (two by default) each take every admitted Gaussian request that
+  is waiting when they become free and solve them as one `GaussianBatch` (batched
+  tensor-core correlation + batched level loop), so requests that arrive while a batch
+  runs join the next one; one or two waiting requests go through the single-problem
+  path instead, whose solve is shorter than a batch's setup;
 * the discrete workers (three by default) each take the next admitted discrete request
   and solve it through `DiscreteSolver`, so discrete solves overlap on the device.
 
@@ -108,10 +110,15 @@ class SkeletonServer:
     """Continuous-batching server for one device."""
 
     def __init__(self, budget_bytes: float = 120e9, max_batch: int = 256, precision: str = "f64",
-                 discrete_workers: int = 3):
+                 discrete_workers: int = 3, gaussian_workers: int = 2, solo_max: int = 2):
         self.budget = int(budget_bytes)
         self.max_batch = int(max_batch)
         self.precision = precision
+        # Gaussian workers: each takes every waiting request it can batch; up to solo_max
+        # requests are solved one by one through the single-problem path (its solve is
+        # shorter than a batch's setup), more form one GaussianBatch
+        self.gaussian_workers = max(1, int(gaussian_workers))
+        self.solo_max = int(solo_max)
         # discrete solves of different requests overlap on the device: each worker owns a
         # stream, and one solve's host reads between levels leave the GPU to the others
         self.discrete_workers = max(1, int(discrete_workers))
@@ -145,6 +152,17 @@ class SkeletonServer:
                     else:
                         rest.append(item)
                 q.extend(rest)
+            if len(batch) <= self.solo_max:
+                for r, adm_t, nbytes in batch:
+                    with torch.cuda.stream(stream):
+                        X = r.samples.to("cuda", non_blocking=True)
+                        s = GaussianSolver(r.p, r.max_level)
+                        s.run(correlation(X), r.n, gaussian_thresholds(r.n, r.alpha))
+                        G, sep, pm = s.to_host()
+                    out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, adm_t, clock() - t0, 1))
+                    adm.release(nbytes)
+                    del s, X
+                continue
             with torch.cuda.stream(stream):
                 Xs = [r.samples.to("cuda", non_blocking=True) for r, _, _ in batch]
                 b = GaussianBatch([r.p for r, _, _ in batch], [r.n for r, _, _ in batch], key[0], key[1],
@@ -191,14 +209,14 @@ class SkeletonServer:
         errors: list[BaseException] = []
         out: list[Response] = []
         t0 = clock()
-        wg = threading.Thread(target=self._guard, args=(self._gaussian_worker, errors, stop, qg, cvg, stop, adm, out,
-                                                        t0, clock), daemon=True)
+        wgs = [threading.Thread(target=self._guard, args=(self._gaussian_worker, errors, stop, qg, cvg, stop, adm,
+                                                          out, t0, clock), daemon=True)
+               for _ in range(self.gaussian_workers)]
         wds = [threading.Thread(target=self._guard, args=(self._discrete_worker, errors, stop, qd, cvd, stop, adm,
                                                           out, t0, clock), daemon=True)
                for _ in range(self.discrete_workers)]
-        wg.start()
-        for wd in wds:
-            wd.start()
+        for w in wgs + wds:
+            w.start()
         pending = deque(sorted(trace, key=lambda r: r.arrival))
         waiting: deque = deque()  # arrived, not admitted (FIFO)
         try:
@@ -233,9 +251,8 @@ class SkeletonServer:
                 cvg.notify_all()
             with cvd:
                 cvd.notify_all()
-            wg.join()
-            for wd in wds:
-                wd.join()
+            for w in wgs + wds:
+                w.join()
         if errors:
             raise errors[0]
         return out

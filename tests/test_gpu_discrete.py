@@ -87,3 +87,45 @@ def test_discrete_edge_cases(cuda):
     codes, dims = ordinal_encode(X)
     assert dims.tolist()[1] == 1
     assert_parity(run_gpu(codes, dims, 0.05, 3), oracle_discrete(codes, dims, 0.05, 3))
+
+
+def test_concurrent_solves_of_different_table_sizes(cuda):
+    """Solves on several host threads whose levels need different shared-memory tables
+    (cardinality 2 vs up to 5, levels up to 3) give the results of solving them one by one:
+    no launch of one thread depends on a limit another thread set."""
+    import threading
+
+    import torch
+
+    probs = [discrete_bn_data(40, 4000, 2, 11, card_lo=2, card_hi=2), discrete_bn_data(60, 6000, 3, 12)]
+    from gpucsl_gb300 import engine
+
+    alone = []
+    for d in probs:
+        codes, dims = engine.ordinal_encode(d.data)
+        alone.append(run_gpu(codes, dims, 0.05, 3)[:3])
+    results = {}
+    errors = []
+
+    def worker(k):
+        try:
+            stream = torch.cuda.Stream()
+            codes, dims = engine.ordinal_encode(probs[k % 2].data)
+            out = []
+            with torch.cuda.stream(stream):
+                for _ in range(4):
+                    out.append(run_gpu(codes, dims, 0.05, 3)[:3])
+            results[k] = out
+        except BaseException as e:  # surfaced below
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(k,)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors[0]
+    for k, outs in results.items():
+        for G, sep, pm in outs:
+            G0, sep0, pm0 = alone[k % 2]
+            assert np.array_equal(G, G0) and np.array_equal(sep, sep0) and np.array_equal(pm, pm0)
