@@ -32,7 +32,6 @@ cudaError_t launch_gauss_level(int L, const double *C, int p, const int *adj, co
                                DevState *st, int num_sms, const float *C32, int *qbuf, long long qcap,
                                const ChunkBufs &ck, cudaStream_t s);
 
-cudaError_t launch_to_f32(const double *x, long long n, float *y, int num_sms, cudaStream_t s);
 size_t orient_workspace_bytes(int p);
 cudaError_t encode_columns(const void *X, int dtype, long long n, int p, long long ld, uint8_t *codes, long long ldc,
                            uint8_t *dims, void *workspace, cudaStream_t s);

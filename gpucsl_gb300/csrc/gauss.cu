@@ -468,19 +468,6 @@ cudaError_t launch_cand(int L, const double *C, int p, double tau, double *zmin,
 }
 
 
-// FP32 copy of an FP64 array (round to nearest).
-__global__ void to_f32_kernel(const double *__restrict__ x, long long n, float *__restrict__ y) {
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
-        y[k] = (float)x[k];
-}
-
-cudaError_t launch_to_f32(const double *x, long long n, float *y, int num_sms, cudaStream_t s) {
-    const long long want = (n + 255) / 256;
-    to_f32_kernel<<<(int)(want < (long long)num_sms * 8 ? want : (long long)num_sms * 8), 256, 0, s>>>(x, n, y);
-    note_launch(1);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_unrank(int K, int L, long long count, int *out, cudaStream_t s) {
     const long long blocks = (count + 127) / 128;
     unrank_kernel<<<(int)(blocks > 0 ? (blocks < 65535 ? blocks : 65535) : 1), 128, 0, s>>>(K, L, count, out);
