@@ -3,18 +3,19 @@
 //   level 0        gauss_level0_kernel     (reference: gpucsl/pc/cuda/gaussian_ci.cu:18-51)
 //   compaction     compact_kernel          (reference: gpucsl/pc/cuda/helpers/graph_helpers.cu:35-56)
 //   edge prefix    row_scan_kernel
-//   level l <= 12  gauss_level_reg_kernel  (reference: gaussian_ci.cu:66-120,
-//                                           helpers/gaussian_helpers.cu:240-262)
+//   level l <= 12  gauss_level_reg_kernel + gauss_level_units_kernel (reference:
+//                  gaussian_ci.cu:66-120, helpers/gaussian_helpers.cu:240-262)
+//   z* candidates  gauss_cand_kernel (FP64, side stream)
 //   level l > 12   gauss_level_smem_kernel
 //   zmin -> pmax   pmax_level0_kernel, pmax_kept_kernel (reference: gpucsl/pc/helpers.py:62-82)
 //
-// Work decomposition of a level: one warp owns one undirected edge {lo, hi} alive at
-// level start and walks the merged key sequence of both directions, key = (rank, dir)
-// with dir 0 for v_i = lo, 32 keys per step (one test per lane).  The warp stops after
-// the first step that contains a removing test; the lowest removing lane is the
-// canonical remover (its set is the sepset) and z* folds the keys up to it.  Because
-// the warp owns the edge for the whole level, the skeleton, sepset and zmin writes
-// need no atomics, and the result does not depend on scheduling.
+// Work decomposition of a level (gauss_levels.cuh): one warp owns one undirected edge
+// {lo, hi} alive at level start and walks the merged key sequence of both directions,
+// key = (rank, dir) with dir 0 for v_i = lo, 32 keys per step (one test per lane); a
+// longer walk is cut into units of 32 keys that the unit kernel walks in parallel and
+// its last unit combines in key order.  The canonical remover is the smallest removing
+// key (its set is the sepset) and z* folds the keys up to it, so the result does not
+// depend on scheduling.
 #include "gauss_levels.cuh"
 
 namespace gcsl {
