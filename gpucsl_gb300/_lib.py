@@ -40,6 +40,7 @@ EXPORTED = [
     "gcsl_gauss_batch_collect", "gcsl_gauss_batch_set_lanes",
     "gcsl_corr_tc_batch_workspace_bytes", "gcsl_corr_tc_batch_prepare", "gcsl_corr_tc_batch_run",
     "gcsl_orient_workspace_bytes", "gcsl_orient_edges", "gcsl_encode_workspace_bytes", "gcsl_ordinal_encode",
+    "gcsl_set_test_precision",
 ]
 
 GCSL_PREC_F64 = 0
@@ -190,6 +191,8 @@ def lib() -> ct.CDLL:
                                              ct.POINTER(BatchPlan), _vp]
     L.gcsl_corr_tc_batch_run.restype = ct.c_int
     L.gcsl_corr_tc_batch_run.argtypes = [ct.POINTER(BatchPlan), _vp]
+    L.gcsl_set_test_precision.restype = ct.c_int
+    L.gcsl_set_test_precision.argtypes = [_i32]
     L.gcsl_encode_workspace_bytes.restype = _sz
     L.gcsl_encode_workspace_bytes.argtypes = [_i32]
     L.gcsl_ordinal_encode.restype = ct.c_int

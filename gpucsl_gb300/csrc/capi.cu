@@ -298,12 +298,17 @@ long long chunk_edges_cap(int p) { return std::max<long long>(1ll << 14, 16ll * 
 long long chunk_units_cap(int p) { return std::max<long long>(1ll << 16, 64ll * p); }
 
 // FP32-first level tests (default) or FP64 throughout (GCSL_F64_TESTS=1, for comparisons).
+// Precision of the plain path's level tests for the calling thread: 0 = the process
+// default (FP32 first; GCSL_F64_TESTS=1 makes it FP64 throughout), 1 = FP32 first,
+// 2 = FP64 throughout.
+static thread_local int g_test_precision = 0;
+
 bool mixed_tests() {
     static const bool mixed = [] {
         const char *e = getenv("GCSL_F64_TESTS");
         return !(e && e[0] == '1');
     }();
-    return mixed;
+    return g_test_precision == 0 ? mixed : g_test_precision == 1;
 }
 
 // GCSL_CHUNKED=0 walks every edge whole in the level kernel (for comparisons).
@@ -369,6 +374,12 @@ int gcsl_version(void) { return GCSL_ABI_VERSION; }
 int64_t gcsl_kernel_launches(void) { return (int64_t)g_kernel_launches.load(std::memory_order_relaxed); }
 
 const char *gcsl_last_error(void) { return g_last_error; }
+
+int gcsl_set_test_precision(int32_t mode) {
+    if (mode < 0 || mode > 2) return GCSL_ERR_INVALID_ARG;
+    g_test_precision = mode;
+    return GCSL_OK;
+}
 
 const char *gcsl_status_string(int status) {
     switch (status) {

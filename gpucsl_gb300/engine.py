@@ -93,6 +93,25 @@ class SolveStats:
         return int(self.raw["levels_run"])
 
 
+class test_precision:
+    """Context manager for the precision of the Gaussian level tests on this thread:
+    "default", "fp32_first" or "fp64" (gcsl_set_test_precision).  All give the same
+    results; "fp64" exists to show it."""
+
+    _modes = {"default": 0, "fp32_first": 1, "fp64": 2}
+
+    def __init__(self, mode: str):
+        self.mode = self._modes[mode]
+
+    def __enter__(self):
+        _lib.check(_lib.lib().gcsl_set_test_precision(self.mode), "gcsl_set_test_precision")
+        return self
+
+    def __exit__(self, *exc):
+        _lib.lib().gcsl_set_test_precision(0)
+        return False
+
+
 class GaussianSolver:
     """Gaussian PC-stable skeleton of p variables up to max_level on one device."""
 

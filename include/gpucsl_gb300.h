@@ -63,6 +63,11 @@ const char *gcsl_status_string(int status);
 /* Number of kernels this library has launched in this process (instrumentation; no
  * reference counterpart). */
 int64_t gcsl_kernel_launches(void);
+/* Precision of gcsl_gauss_skeleton's level tests for the calling thread (no reference
+ * counterpart): 0 = process default (FP32 first with FP64 where FP32 cannot decide, or
+ * FP64 throughout when GCSL_F64_TESTS=1 is set), 1 = FP32 first, 2 = FP64 throughout.
+ * Both give the same skeleton, sepsets, test counts and pmax; mode 2 exists to show it. */
+int gcsl_set_test_precision(int32_t mode);
 
 /* ------------------------------------------------------------ correlation (a) */
 /* Replaces gpucsl/pc/helpers.py:58-59 (correlation_matrix_of = np.corrcoef(data,

@@ -58,3 +58,27 @@ def test_mixed_and_chunked_equal_fp64_whole(cuda, tmp_path, case):
         assert np.array_equal(a["sep"], b["sep"]), mode
         assert np.array_equal(a["tests"], b["tests"]), mode
         assert np.array_equal(a["pm"], b["pm"]), (mode, float(np.abs(a["pm"] - b["pm"]).max()))
+
+
+def test_precision_switch_in_process(cuda):
+    """gcsl_set_test_precision: FP64 tests throughout on this thread give the FP32-first
+    results bit for bit (same skeleton, sepsets, test counts, pmax)."""
+    import torch
+
+    from gpucsl_gb300 import engine
+    from gpucsl_gb300.synthetic import gaussian_dag_data
+
+    p, n = 300, 2000
+    X = torch.from_numpy(gaussian_dag_data(p, n, 4, 8).data).cuda()
+    C = engine.correlation(X)
+    thr = engine.gaussian_thresholds(n, 0.05)
+    s = engine.GaussianSolver(p, 12)
+    with engine.test_precision("fp32_first"):
+        a = s.run(C, n, thr)
+        ra = s.to_host()
+    with engine.test_precision("fp64"):
+        b = s.run(C, n, thr)
+        rb = s.to_host()
+    assert a.raw["tests"] == b.raw["tests"]
+    for x, y in zip(ra, rb):
+        assert np.array_equal(x, y)
