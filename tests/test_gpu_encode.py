@@ -56,3 +56,27 @@ def test_discrete_driver_uses_device_encoding(cuda):
     G, sep, pm = ds.to_host()
     assert np.array_equal(res.skeleton, G) and np.array_equal(res.seperation_sets, sep)  # reference spelling
     assert np.array_equal(res.pmax, pm)
+
+
+def test_device_encoding_boundaries(cuda):
+    """255 distinct values pass and 256 do not; a constant column has dims 1; values far
+    from zero (a small range around 10^15) and a single sample encode like the host."""
+    from gpucsl_gb300 import _lib, engine
+
+    torch = cuda
+    rng = np.random.default_rng(3)
+    n = 700
+    c255 = rng.permutation(np.arange(n) % 255)
+    const = np.full(n, 42)
+    far = 10**15 + rng.integers(0, 7, n)
+    data = np.stack([c255, const, far], axis=1).astype(np.int64)
+    codes, dims = engine.ordinal_encode(data)
+    cdev, ddev = engine.ordinal_encode_device(torch.from_numpy(data).cuda())
+    assert list(ddev.cpu().numpy()) == [255, 1, int(dims[2])]
+    assert np.array_equal(cdev.cpu().numpy()[:, :n], codes)
+    c256 = (np.arange(n) % 256).astype(np.int64).reshape(-1, 1)
+    with pytest.raises(_lib.GcslError):
+        engine.ordinal_encode_device(torch.from_numpy(c256).cuda())
+    one = np.array([[3, 9, 0]], dtype=np.int64)
+    cdev, ddev = engine.ordinal_encode_device(torch.from_numpy(one).cuda())
+    assert list(ddev.cpu().numpy()) == [1, 1, 1] and cdev.cpu().numpy()[:, 0].tolist() == [0, 0, 0]
