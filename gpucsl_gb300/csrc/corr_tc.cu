@@ -702,11 +702,11 @@ size_t corr_tc_workspace_bytes(long long n, int p, int num_sms) {
 
 template <class Src>
 static cudaError_t set_ozaki_smem() {
-    static bool done = false;  // per instantiation
-    if (done) return cudaSuccess;
+    static std::atomic<bool> done{false};  // per instantiation; the value set is the same for every caller
+    if (done.load()) return cudaSuccess;
     const cudaError_t e = cudaFuncSetAttribute(corr_ozaki_kernel<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                OZ_NST * OZ_STAGE_BYTES);
-    done = e == cudaSuccess;
+    if (e == cudaSuccess) done.store(true);
     return e;
 }
 
