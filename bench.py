@@ -193,12 +193,18 @@ def read_profile_traffic() -> int | None:
     return None
 
 
+def cpu_workers() -> int:
+    return os.cpu_count() or 1
+
+
 def cpu_oracle_solve(data):
-    """One CPU solve with the oracle (numpy FP64): correlation + level loop + pmax."""
+    """One CPU solve with the oracle (numpy FP64) on every host core: correlation (BLAS
+    threads) + level loop (each level's edges split over a spawned process per core) +
+    pmax.  The pool is started by the first call and reused."""
     from oracle import gaussian as og
 
     C = og.corrcoef(data)
-    return og.skeleton(C, data.shape[0], ALPHA, P - 2)
+    return og.skeleton(C, data.shape[0], ALPHA, P - 2, workers=cpu_workers())
 
 
 def blas_threads() -> int:
@@ -577,14 +583,15 @@ def run_ours(args, world, rank, local):
             s = time.perf_counter()
             r = cpu_oracle_solve(w.data)
             times.append(time.perf_counter() - s)
-            if time.perf_counter() - t0 > 10.0 or len(times) >= 3:
+            if time.perf_counter() - t0 > 10.0 or len(times) >= 4:
                 break
         assert r.tests_canonical == E, (r.tests_canonical, E)
+        times = times[1:] if len(times) > 1 else times  # the first solve starts the process pool
         out["cpu_baseline"] = {"value": round(E / statistics.mean(times), 1), "unit": UNIT,
-                               "cores": blas_threads(), "kind": "port",
+                               "cores": cpu_workers(), "kind": "port",
                                "sample": f"{len(times)} full solves of the same workload "
-                                         f"(numpy corrcoef on {blas_threads()} BLAS threads, level loop "
-                                         f"single-threaded numpy), mean {statistics.mean(times):.2f} s"}
+                                         f"(numpy corrcoef on {blas_threads()} BLAS threads, each level's edges "
+                                         f"over {cpu_workers()} processes), mean {statistics.mean(times):.2f} s"}
     if rank == 0:
         print(json.dumps(out), flush=True)
 
@@ -606,7 +613,7 @@ def run_reference(args, world, rank):
         cpu_oracle_solve(w.data)
         times.append(time.perf_counter() - s)
     value = E * len(times) / sum(times)
-    cores = blas_threads()
+    cores = cpu_workers()
     out = {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "solves_timed": len(times), "ms_per_step": round(1e3 * sum(times) / len(times), 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -614,9 +621,9 @@ def run_reference(args, world, rank):
            "config": {"workload": WORKLOAD, "p": P, "n": N, "alpha": ALPHA, "tests_per_step": E,
                       "levels_run": len(r.levels)},
            "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": f"{len(times)} full solves (numpy corrcoef on {cores} BLAS threads, "
-                                      "level loop single-threaded numpy); the reference itself has no CPU path "
-                                      "and its GPU code needs cupy, absent here"},
+                            "sample": f"{len(times)} full solves (numpy corrcoef on {blas_threads()} BLAS "
+                                      f"threads, each level's edges over {cores} processes); the reference itself "
+                                      "has no CPU path and its GPU code needs cupy, absent here"},
            "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 

@@ -262,9 +262,116 @@ class GaussianResult:
         return sum(s.tests_canonical for s in self.levels)
 
 
+def _walk_level(C, adj, deg, ei, ej, level, tau, BT, chunk, z_fn):
+    """Level `level` for the edges (ei, ej) against the level-start lists `adj`: every
+    edge independent of the others (PC-stable).  Returns (zlev per edge, [(edge index,
+    sepset)] of removed edges, canonical tests, full tests, smallest decision margin)."""
+    K0 = deg[ei] - 1
+    K1 = deg[ej] - 1
+    R0 = np.where(K0 >= level, BT[np.clip(K0, 0, None), level], 0)
+    R1 = np.where(K1 >= level, BT[np.clip(K1, 0, None), level], 0)
+    T = R0 + R1
+    tests_full = int(T.sum())
+    tests_canonical = 0
+    min_margin = float("inf")
+    removed = []
+    Rmin = np.minimum(R0, R1)
+    longer_dir = np.where(R0 > R1, 0, 1)
+    active = np.nonzero(T > 0)[0]
+    zlev = np.full(ei.size, np.inf)
+    base = 0
+    while active.size:
+        m = np.broadcast_to(base + np.arange(chunk)[None, :], (active.size, chunk))
+        e = np.broadcast_to(active[:, None], m.shape)
+        valid = m < T[e]
+        ev, mv = e[valid], m[valid]
+        inter = mv < 2 * Rmin[ev]
+        rank = np.where(inter, mv >> 1, mv - Rmin[ev])
+        dirn = np.where(inter, mv & 1, longer_dir[ev])
+        vi = np.where(dirn == 0, ei[ev], ej[ev])
+        vj = np.where(dirn == 0, ej[ev], ei[ev])
+        K = deg[vi] - 1
+        pos = unrank_batched(K, rank, level, BT)
+        S = resolve_batched(adj, vi, vj, pos)
+        Z = z_fn(C, vi, vj, S)
+        with np.errstate(invalid="ignore"):
+            rem = Z < tau
+            marg = np.abs(Z - tau) / tau if tau > 0 else np.full(Z.shape, np.inf)
+        # scatter back to (a, chunk)
+        Zg = np.full(m.shape, np.nan)
+        Zg[valid] = Z
+        remg = np.zeros(m.shape, bool)
+        remg[valid] = rem
+        Mg = np.full(m.shape, np.inf)
+        Mg[valid] = marg
+        Sg = np.full(m.shape + (level,), -1, np.int64)
+        Sg[valid] = S
+        has = remg.any(1)
+        first = np.where(has, remg.argmax(1), chunk)
+        upto = np.arange(chunk)[None, :] <= first[:, None]
+        take = upto & valid
+        zt = np.where(take & ~np.isnan(Zg), Zg, np.inf)
+        zlev[active] = np.minimum(zlev[active], zt.min(1))
+        tests_canonical += int(take.sum())
+        mm = np.where(take, Mg, np.inf).min(1)
+        min_margin = min(min_margin, float(mm.min(initial=np.inf)))
+        for a_idx in np.nonzero(has)[0]:
+            removed.append((int(active[a_idx]), Sg[a_idx, first[a_idx]].copy()))
+        done = has | (base + chunk >= T[active])
+        active = active[~done]
+        base += chunk
+    return zlev, removed, tests_canonical, tests_full, min_margin
+
+
+# Worker side of the process pool: the solve's C and the level's lists are shared memory
+# blocks that the parent fills; a task attaches them by name and detaches before it
+# returns (its results are fresh arrays).
+def _pool_level(args):
+    from multiprocessing import shared_memory
+
+    c_name, adj_name, p, deg, ei, ej, level, tau, BT, chunk, z_fn = args
+    c_shm = shared_memory.SharedMemory(name=c_name)
+    adj_shm = shared_memory.SharedMemory(name=adj_name)
+    try:
+        C = np.ndarray((p, p), np.float64, buffer=c_shm.buf)
+        adj = np.ndarray((p, p), np.int32, buffer=adj_shm.buf)
+        out = _walk_level(C, adj, deg, ei, ej, level, tau, BT, chunk, z_fn)
+        del C, adj
+        return out
+    finally:
+        c_shm.close()
+        adj_shm.close()
+
+
+_POOLS = {}
+
+
+def _pool(workers):
+    """One process pool per worker count for the process's lifetime (started with spawn,
+    so it is safe in a process that uses a GPU)."""
+    if workers not in _POOLS:
+        import multiprocessing as mp
+        import os
+
+        # one BLAS thread per worker process (the workers are the parallelism)
+        keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+        saved = {k: os.environ.get(k) for k in keys}
+        os.environ.update({k: "1" for k in keys})
+        try:
+            _POOLS[workers] = mp.get_context("spawn").Pool(workers)
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+    return _POOLS[workers]
+
+
 def skeleton(C: np.ndarray, num_observations: int, alpha: float, max_level: int,
-             thr: list | None = None, chunk: int = 64, z_fn=gaussian_ci_z) -> GaussianResult:
-    """Gaussian PC-stable skeleton on correlation matrix C (FP64)."""
+             thr: list | None = None, chunk: int = 64, z_fn=gaussian_ci_z, workers: int = 0) -> GaussianResult:
+    """Gaussian PC-stable skeleton on correlation matrix C (FP64).  workers > 1 splits each
+    level's edges over that many processes (started with spawn); the result is the same."""
     C = np.ascontiguousarray(C, dtype=np.float64)
     p = C.shape[0]
     if thr is None:
@@ -290,79 +397,66 @@ def skeleton(C: np.ndarray, num_observations: int, alpha: float, max_level: int,
             st0.min_margin = float(np.nanmin(np.abs(z0 - tau0)) / tau0) if tau0 > 0 else float("inf")
     stats.append(st0)
 
-    for level in range(1, max_level + 1):
-        adj = compact(G)
-        deg = adj[:, 0].astype(np.int64)
-        if deg.max(initial=0) - 1 < level:
-            break
-        if level >= len(thr):
-            raise IndexError(f"no Fisher-z threshold for level {level}")
-        tau = thr[level]
-        st = LevelStats(level)
-        ei, ej = np.nonzero(np.triu(G, 1))
-        st.edges = ei.size
-        BT = binom_table(int(max(deg.max(), 1)), level)
-        K0 = deg[ei] - 1
-        K1 = deg[ej] - 1
-        R0 = np.where(K0 >= level, BT[np.clip(K0, 0, None), level], 0)
-        R1 = np.where(K1 >= level, BT[np.clip(K1, 0, None), level], 0)
-        T = R0 + R1
-        st.tests_full = int(T.sum())
-        Rmin = np.minimum(R0, R1)
-        longer_dir = np.where(R0 > R1, 0, 1)
-        active = np.nonzero(T > 0)[0]
-        zlev = np.full(ei.size, np.inf)
-        base = 0
-        while active.size:
-            m = np.broadcast_to(base + np.arange(chunk)[None, :], (active.size, chunk))
-            e = np.broadcast_to(active[:, None], m.shape)
-            valid = m < T[e]
-            ev, mv = e[valid], m[valid]
-            inter = mv < 2 * Rmin[ev]
-            rank = np.where(inter, mv >> 1, mv - Rmin[ev])
-            dirn = np.where(inter, mv & 1, longer_dir[ev])
-            vi = np.where(dirn == 0, ei[ev], ej[ev])
-            vj = np.where(dirn == 0, ej[ev], ei[ev])
-            K = deg[vi] - 1
-            pos = unrank_batched(K, rank, level, BT)
-            S = resolve_batched(adj, vi, vj, pos)
-            Z = z_fn(C, vi, vj, S)
-            with np.errstate(invalid="ignore"):
-                rem = Z < tau
-                marg = np.abs(Z - tau) / tau if tau > 0 else np.full(Z.shape, np.inf)
-            # scatter back to (a, chunk)
-            Zg = np.full(m.shape, np.nan)
-            Zg[valid] = Z
-            remg = np.zeros(m.shape, bool)
-            remg[valid] = rem
-            Mg = np.full(m.shape, np.inf)
-            Mg[valid] = marg
-            Sg = np.full(m.shape + (level,), -1, np.int64)
-            Sg[valid] = S
-            has = remg.any(1)
-            first = np.where(has, remg.argmax(1), chunk)
-            upto = np.arange(chunk)[None, :] <= first[:, None]
-            take = upto & valid
-            zt = np.where(take & ~np.isnan(Zg), Zg, np.inf)
-            zlev[active] = np.minimum(zlev[active], zt.min(1))
-            st.tests_canonical += int(take.sum())
-            mm = np.where(take, Mg, np.inf).min(1)
-            st.min_margin = min(st.min_margin, float(mm.min(initial=np.inf)))
-            # finalize removed edges
-            for a_idx in np.nonzero(has)[0]:
-                eidx = active[a_idx]
-                lo, hi = int(ei[eidx]), int(ej[eidx])
-                s = Sg[a_idx, first[a_idx]]
-                G[lo, hi] = 0
-                G[hi, lo] = 0
-                sepsets[lo, hi, :level] = s
-                sepsets[hi, lo, :level] = s
-                st.removed += 1
-            done = has | (base + chunk >= T[active])
-            active = active[~done]
-            base += chunk
-        zmin[ei, ej] = np.minimum(zmin[ei, ej], zlev)
-        stats.append(st)
+    pool = c_shm = adj_shm = None
+    if workers > 1 and max_level >= 1 and p > 1:
+        from multiprocessing import shared_memory
+
+        pool = _pool(workers)
+        c_shm = shared_memory.SharedMemory(create=True, size=C.nbytes)
+        np.ndarray(C.shape, np.float64, buffer=c_shm.buf)[:] = C
+    try:
+        for level in range(1, max_level + 1):
+            adj = compact(G)
+            deg = adj[:, 0].astype(np.int64)
+            if deg.max(initial=0) - 1 < level:
+                break
+            if level >= len(thr):
+                raise IndexError(f"no Fisher-z threshold for level {level}")
+            tau = thr[level]
+            st = LevelStats(level)
+            ei, ej = np.nonzero(np.triu(G, 1))
+            st.edges = ei.size
+            BT = binom_table(int(max(deg.max(), 1)), level)
+            if pool is None:
+                parts = [(np.arange(ei.size), _walk_level(C, adj, deg, ei, ej, level, tau, BT, chunk, z_fn))]
+            else:
+                # a fresh block per level: workers may still hold the previous level's
+                from multiprocessing import shared_memory
+
+                if adj_shm is not None:
+                    adj_shm.close()
+                    adj_shm.unlink()
+                adj_shm = shared_memory.SharedMemory(create=True, size=p * p * 4)
+                np.ndarray((p, p), np.int32, buffer=adj_shm.buf)[:] = adj
+                # contiguous slices of about equal test counts
+                K0, K1 = deg[ei] - 1, deg[ej] - 1
+                w = (np.where(K0 >= level, BT[np.clip(K0, 0, None), level], 0)
+                     + np.where(K1 >= level, BT[np.clip(K1, 0, None), level], 0) + 1).astype(np.float64)
+                cuts = np.searchsorted(np.cumsum(w), np.linspace(0, w.sum(), 4 * workers + 1)[1:-1])
+                idx = [x for x in np.split(np.arange(ei.size), cuts) if x.size]
+                outs = pool.map(_pool_level, [(c_shm.name, adj_shm.name, p, deg, ei[x], ej[x], level, tau, BT,
+                                               chunk, z_fn) for x in idx])
+                parts = list(zip(idx, outs))
+            zlev = np.full(ei.size, np.inf)
+            for x, (zl, removed, tc, tf, mm) in parts:
+                zlev[x] = zl
+                st.tests_canonical += tc
+                st.tests_full += tf
+                st.min_margin = min(st.min_margin, mm)
+                for a, s in removed:
+                    lo, hi = int(ei[x[a]]), int(ej[x[a]])
+                    G[lo, hi] = 0
+                    G[hi, lo] = 0
+                    sepsets[lo, hi, :level] = s
+                    sepsets[hi, lo, :level] = s
+                    st.removed += 1
+            zmin[ei, ej] = np.minimum(zmin[ei, ej], zlev)
+            stats.append(st)
+    finally:
+        for shm in (c_shm, adj_shm):
+            if shm is not None:
+                shm.close()
+                shm.unlink()
 
     pmax = pmax_from_zmin(zmin, num_observations)
     return GaussianResult(G, sepsets, pmax, zmin, stats)

@@ -162,3 +162,17 @@ def test_ref_lib_pins_when_available():
             for r in range(0, comb(K, L), 7):
                 R.ref_sepset_indices(L, K, r, ct.addressof(buf))
                 assert list(cbind.unrank(K, L, r)) == [buf[i] for i in range(L)]
+
+
+def test_oracle_process_pool_matches_serial():
+    """The oracle's level loop split over spawned processes gives the serial answer:
+    same skeleton, sepsets, pmax and per-level test counts."""
+    from gpucsl_gb300.synthetic import gaussian_dag_data
+
+    C = og.corrcoef(gaussian_dag_data(60, 800, 3.0, seed=5).data)
+    a = og.skeleton(C, 800, 0.05, 4)
+    b = og.skeleton(C, 800, 0.05, 4, workers=2)
+    assert np.array_equal(a.skeleton, b.skeleton)
+    assert np.array_equal(a.sepsets, b.sepsets)
+    assert np.array_equal(a.pmax, b.pmax)
+    assert [s.tests_canonical for s in a.levels] == [s.tests_canonical for s in b.levels]
