@@ -7,7 +7,16 @@ Compiles
     (only where the reference sources are present; they are read in place from
      gpucsl/pc/cuda/helpers/ of the reference checkout, never copied).
 
-Both are plain gcc/g++ invocations; no build system of the reference is run.
+  * the reference's own Gaussian level kernels (gpucsl/pc/cuda/gaussian_ci.cu with the
+    helpers it includes, read in place) -> oracle/_ref/ref_gauss_p{P}_l{L}.cubin, one
+    device-only module per (variables, max_level) shape, as the reference's runtime
+    compiler instantiates them (kernel_management.py:199-221, :154-166): the level-0 and
+    level-n templates for levels 0..L and compact<P, P>.  The instantiation list is
+    written by this recipe; the kernels themselves are the reference's.  Built with
+    NDEBUG, so the reference's device asserts compile away.
+
+The host builds are plain gcc/g++ invocations and the kernels one nvcc call per shape;
+no build system of the reference is run.
 """
 from __future__ import annotations
 
@@ -40,6 +49,43 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_SO
 
 
+REF_CUDA = REF_ROOT / "gpucsl" / "pc" / "cuda"
+# (variables, max_level): the p = 20 workload at max_level 3 and the p = 1000 workload to
+# its terminal level 10 (levels 0..10 run).
+REF_GPU_SHAPES = ((20, 3), (1000, 10))
+
+
+def ref_gpu_cubin(p: int, max_level: int) -> Path:
+    return HERE / "_ref" / f"ref_gauss_p{p}_l{max_level}.cubin"
+
+
+def build_ref_gpu(force: bool = False, shapes=REF_GPU_SHAPES) -> list[Path]:
+    """Compile the reference's Gaussian CI kernels for sm_103a; [] when the reference
+    checkout is absent.  Each module holds gaussian_ci_level_0<0, P, L>,
+    gaussian_ci_level_n<l, P, L> for l = 1..L and compact<P, P>."""
+    src = REF_CUDA / "gaussian_ci.cu"
+    if not src.exists():
+        return []
+    deps = [src] + [REF_CUDA / "helpers" / f for f in ("gaussian_helpers.cu", "graph_helpers.cu", "set_helpers.cu")]
+    out = []
+    for p, L in shapes:
+        cubin = ref_gpu_cubin(p, L)
+        cubin.parent.mkdir(exist_ok=True)
+        if force or _stale(cubin, *deps, Path(__file__)):
+            sig = "(double *, unsigned short *, int *, double, int *, float *, int)"
+            lines = ['#include "gaussian_ci.cu"',
+                     f"template __global__ void gaussian_ci_level_0<0, {p}, {L}>{sig};"]
+            lines += [f"template __global__ void gaussian_ci_level_n<{l}, {p}, {L}>{sig};" for l in range(1, L + 1)]
+            lines.append(f"template __global__ void compact<{p}, {p}u>(unsigned short *, unsigned int *, unsigned int);")
+            inst = cubin.with_suffix(".cu")
+            inst.write_text("\n".join(lines) + "\n")
+            cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-DNDEBUG",
+                   f"-I{REF_CUDA}", f"-I{REF_CUDA / 'helpers'}", str(inst), "-o", str(cubin)]
+            subprocess.run(cmd, check=True)
+        out.append(cubin)
+    return out
+
+
 def build_ref(force: bool = False) -> Path | None:
     """Build the reference-helper shim; returns None when the reference is absent."""
     if not (REF_HELPERS / "math_helpers.cu").exists():
@@ -57,3 +103,4 @@ def build_ref(force: bool = False) -> Path | None:
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))
+    print(build_ref_gpu(force="--force" in sys.argv))
