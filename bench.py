@@ -645,6 +645,54 @@ def reference_gpu_leg(data, oracle_result, E, steps: int) -> dict:
             "note": "tests/s counts the canonical executed tests of the workload, as every other figure here"}
 
 
+def reference_gpu_discrete_leg() -> dict:
+    """The reference's own discrete kernels (discrete_ci.cu, oracle/_ref/) on this GPU at
+    p = 200, n = 50000, cardinality 2..5, alpha 0.05, max level 3, driven as the
+    reference's discrete skeleton loop drives them; skeleton checked against the C
+    oracle; tests/s over the oracle's canonical test count."""
+    try:
+        import ctypes as ct
+
+        import numpy as np
+        import torch
+        from gpucsl_gb300.synthetic import discrete_bn_data
+        from oracle import cbind, ref_gpu
+
+        if not torch.cuda.is_available():
+            return {"unavailable": "no GPU"}
+        p, n, L, alpha = 200, 50000, 3, 0.05
+        codes, dims = ref_gpu.ordinal_encode(discrete_bn_data(p, n, 2, 3).data)
+        K = ref_gpu.RefDiscreteKernels(p, n, int(dims.max()), L)
+    except Exception as e:  # noqa: BLE001 - a baseline, reported as unavailable
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+    Go = np.zeros((p, p), np.uint16)
+    sepo = np.full((p, p, L), -1, np.int32)
+    pmo = np.zeros((p, p))
+    st = cbind.OrcStats()
+    cbind.lib().orc_discrete_skeleton(cbind.ptr(codes), n, n, p, cbind.ptr(dims), alpha, L, cbind.ptr(Go),
+                                      cbind.ptr(sepo), cbind.ptr(pmo), 0, ct.byref(st))
+    E = int(sum(st.tests[:st.levels_run]))
+    bufs = K.alloc(codes, dims)
+    K.run(alpha, bufs)
+    torch.cuda.synchronize()
+    same = bool(np.array_equal(bufs["G"].cpu().numpy() != 0, Go != 0))
+    times = []
+    for _ in range(3):
+        K.reset(bufs)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        levels = K.run(alpha, bufs)
+        b.record()
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b) / 1e3)
+    t = statistics.mean(times)
+    return {"workload": "discrete_skeleton_p200_n50000_card2-5_alpha0.05_L3", "value": round(E / t, 1),
+            "unit": UNIT, "ms_per_solve": round(1e3 * t, 3), "levels_run": levels, "tests_per_solve": E,
+            "skeleton_identical_to_oracle": same,
+            "kernels": "discrete_ci.cu level kernels (templates <l, 200, 2, max_dim, 50000, 3>) and compact<200, "
+                       "200>, each behind an extern \"C\" kernel, nvcc -cubin sm_103a -DNDEBUG"}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -675,6 +723,7 @@ def run_reference(args, world, rank):
                                       "are timed in reference_gpu_kernels)"},
            "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     out["reference_gpu_kernels"] = reference_gpu_leg(w.data, r, E, args.steps)
+    out["reference_gpu_kernels_discrete"] = reference_gpu_discrete_leg()
     print(json.dumps(out), flush=True)
 
 

@@ -15,6 +15,16 @@ Compiles
     written by this recipe; the kernels themselves are the reference's.  Built with
     NDEBUG, so the reference's device asserts compile away.
 
+  * the reference's own discrete kernels (gpucsl/pc/cuda/discrete_ci.cu, read in place)
+    -> oracle/_ref/ref_disc_p{P}_n{N}_d{D}_l{L}.cubin per (variables, samples, max_dim,
+    max_level) shape.  CUDA 13 rejects the file as it stands: discrete_ci.cu:114
+    declares execute_ci_test_for_sepset __global__ and :231 calls it without a launch
+    configuration.  The recipe therefore includes the file with __global__ defined as
+    __device__ (no source is edited or copied) and launches the reference's kernel
+    bodies through extern "C" kernels of its own, one per level plus compact, each a
+    single call with the reference's template arguments (kernel_management.py:259-268,
+    parallel_ci_tests = 2 from find_execution_specification, :395-397).
+
 The host builds are plain gcc/g++ invocations and the kernels one nvcc call per shape;
 no build system of the reference is run.
 """
@@ -86,6 +96,50 @@ def build_ref_gpu(force: bool = False, shapes=REF_GPU_SHAPES) -> list[Path]:
     return out
 
 
+# (variables, samples, max_dim, max_level): the p = 200, n = 50000 discrete workload and
+# a small case for the parity test; max_dim is the largest observed cardinality.
+REF_DISC_SHAPES = ((200, 50000, 5, 3), (24, 4000, 5, 3))
+REF_DISC_PARALLEL_TESTS = 2
+
+
+def ref_disc_cubin(p: int, n: int, max_dim: int, max_level: int) -> Path:
+    return HERE / "_ref" / f"ref_disc_p{p}_n{n}_d{max_dim}_l{max_level}.cubin"
+
+
+def build_ref_gpu_discrete(force: bool = False, shapes=REF_DISC_SHAPES) -> list[Path]:
+    """Compile the reference's discrete CI kernels for sm_103a; [] when the reference
+    checkout is absent.  Exported names: ref_disc_level_{l} for l = 0..L, ref_compact."""
+    src = REF_CUDA / "discrete_ci.cu"
+    if not src.exists():
+        return []
+    deps = [src] + [REF_CUDA / "helpers" / f for f in ("discrete_helpers.cu", "graph_helpers.cu", "set_helpers.cu",
+                                                          "math_helpers.cu")]
+    out = []
+    for p, n, md, L in shapes:
+        cubin = ref_disc_cubin(p, n, md, L)
+        cubin.parent.mkdir(exist_ok=True)
+        if force or _stale(cubin, *deps, Path(__file__)):
+            sig = ("(uint8_t *d, unsigned short *G, int *Gc, uint8_t *dims, double alpha, uint32_t *wm, int *sep, "
+                   "float *pmax)")
+            args = "(d, G, Gc, dims, alpha, wm, sep, pmax)"
+            targs = f"{p}, {REF_DISC_PARALLEL_TESTS}, {md}, {n}, {L}"
+            lines = ["#include <cstdint>", '#pragma push_macro("__global__")', "#undef __global__",
+                     "#define __global__ __device__", '#include "discrete_ci.cu"', '#pragma pop_macro("__global__")']
+            for l in range(L + 1):
+                body = "discrete_ci_level_0" if l == 0 else "discrete_ci_level_n"
+                lines.append(f'extern "C" __global__ void ref_disc_level_{l}{sig} '
+                             f"{{ {body}<{l}, {targs}>{args}; }}")
+            lines.append('extern "C" __global__ void ref_compact(unsigned short *G, unsigned int *Gc, unsigned int di) '
+                         f"{{ compact<{p}, {p}u>(G, Gc, di); }}")
+            inst = cubin.with_suffix(".cu")
+            inst.write_text("\n".join(lines) + "\n")
+            cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-DNDEBUG",
+                   f"-I{REF_CUDA}", f"-I{REF_CUDA / 'helpers'}", str(inst), "-o", str(cubin)]
+            subprocess.run(cmd, check=True)
+        out.append(cubin)
+    return out
+
+
 def build_ref(force: bool = False) -> Path | None:
     """Build the reference-helper shim; returns None when the reference is absent."""
     if not (REF_HELPERS / "math_helpers.cu").exists():
@@ -104,3 +158,4 @@ if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))
     print(build_ref_gpu(force="--force" in sys.argv))
+    print(build_ref_gpu_discrete(force="--force" in sys.argv))

@@ -1,6 +1,9 @@
 """ORACLE — test and baseline infrastructure only; never imported by the product.
 
-Runs the reference's own Gaussian CI kernels (gpucsl/pc/cuda/gaussian_ci.cu, compiled
+Runs the reference's own Gaussian and discrete CI kernels (RefGaussianKernels,
+RefDiscreteKernels).
+
+Gaussian: runs the reference's own Gaussian CI kernels (gpucsl/pc/cuda/gaussian_ci.cu, compiled
 unchanged by oracle/build.py into oracle/_ref/ref_gauss_p{P}_l{L}.cubin) on the current
 GPU, driven by a host loop that follows the reference's single-GPU worker
 (discover_skeleton_gaussian.py:29-108):
@@ -16,6 +19,16 @@ separation sets -1, zmin FLT_MAX).  The module is loaded with the CUDA driver AP
 torch's current stream.  The reference writes the skeleton deterministically (an edge
 is removed iff some test removes it) but its separation sets and zmin depend on thread
 timing, so only the skeleton is compared with the oracle.
+
+Discrete: the kernels of gpucsl/pc/cuda/discrete_ci.cu (compiled into
+oracle/_ref/ref_disc_p{P}_n{N}_d{D}_l{L}.cubin, each level's kernel body behind an
+extern "C" kernel ref_disc_level_{l}) driven as discover_skeleton_discrete.py:24-128
+drives them: ordinal-encoded samples column-major as uint8, dims = largest code + 1,
+pmax 0, separation sets -1, one working-memory block sized by
+find_execution_specification (kernel_management.py:378-465; the memory reduction
+factor stays 1 for the shapes built here); level 0 on a (p, p) grid of 32 threads,
+level l on a (p, p) grid of (64, 2, 1) threads after compact and the host read of the
+largest neighbour count.
 """
 from __future__ import annotations
 
@@ -51,6 +64,7 @@ def _driver():
         lib.cuCtxGetCurrent.argtypes = [ct.POINTER(ct.c_void_p)]
         lib.cuModuleLoadData.argtypes = [ct.POINTER(ct.c_void_p), ct.c_char_p]
         lib.cuModuleUnload.argtypes = [ct.c_void_p]
+        lib.cuModuleGetFunction.argtypes = [ct.POINTER(ct.c_void_p), ct.c_void_p, ct.c_char_p]
         lib.cuModuleGetFunctionCount.argtypes = [ct.POINTER(ct.c_uint), ct.c_void_p]
         lib.cuModuleEnumerateFunctions.argtypes = [ct.POINTER(ct.c_void_p), ct.c_uint, ct.c_void_p]
         lib.cuFuncGetName.argtypes = [ct.POINTER(ct.c_char_p), ct.c_void_p]
@@ -66,26 +80,40 @@ def _check(rc: int, what: str):
         raise RuntimeError(f"CUDA driver error {rc} in {what}")
 
 
+def _launch(f, grid, block, args, stream):
+    params = (ct.c_void_p * len(args))(*[ct.addressof(a) for a in args])
+    gx, gy = grid
+    bx, by, bz = block
+    _check(_driver().cuLaunchKernel(f, gx, gy, 1, bx, by, bz, 0, ct.c_void_p(stream), params, None),
+           "cuLaunchKernel")
+
+
+def _load_module(path: Path):
+    import torch
+
+    torch.cuda.init()
+    torch.empty(1, device="cuda")  # the primary context is current on this thread
+    cu = _driver()
+    ctx = ct.c_void_p()
+    _check(cu.cuCtxGetCurrent(ct.byref(ctx)), "cuCtxGetCurrent")
+    if not ctx.value:
+        raise RefGpuUnavailable("no current CUDA context")
+    image = path.read_bytes()
+    mod = ct.c_void_p()
+    _check(cu.cuModuleLoadData(ct.byref(mod), image), "cuModuleLoadData")
+    return mod
+
+
 class RefGaussianKernels:
     """The reference's kernels for one (variables, max_level) shape."""
 
     def __init__(self, p: int, max_level: int):
-        import torch
-
         path = cubin_path(p, max_level)
         if not path.exists():
             raise RefGpuUnavailable(f"{path.name} not built (the reference checkout was absent at build time)")
         self.p, self.max_level = p, max_level
-        torch.cuda.init()
-        torch.empty(1, device="cuda")  # the primary context is current on this thread
+        self.mod = _load_module(path)
         cu = _driver()
-        ctx = ct.c_void_p()
-        _check(cu.cuCtxGetCurrent(ct.byref(ctx)), "cuCtxGetCurrent")
-        if not ctx.value:
-            raise RefGpuUnavailable("no current CUDA context")
-        self._image = path.read_bytes()
-        self.mod = ct.c_void_p()
-        _check(cu.cuModuleLoadData(ct.byref(self.mod), self._image), "cuModuleLoadData")
         count = ct.c_uint()
         _check(cu.cuModuleGetFunctionCount(ct.byref(count), self.mod), "cuModuleGetFunctionCount")
         funcs = (ct.c_void_p * count.value)()
@@ -117,10 +145,7 @@ class RefGaussianKernels:
             pass
 
     def _launch(self, f, grid, block, args, stream):
-        params = (ct.c_void_p * len(args))(*[ct.addressof(a) for a in args])
-        gx, gy = grid
-        _check(_driver().cuLaunchKernel(f, gx, gy, 1, block, 1, 1, 0, ct.c_void_p(stream), params, None),
-               "cuLaunchKernel")
+        _launch(f, grid, (block, 1, 1), args, stream)
 
     def alloc(self):
         """Device buffers as the reference allocates them for one call."""
@@ -161,5 +186,113 @@ class RefGaussianKernels:
             self._launch(self.level[level], grid, block,
                          [ptr(C), ptr(G), ptr(Gc), ct.c_double(float(thresholds[level])), ptr(sep), ptr(zmin),
                           ct.c_int(0)], stream)
+            levels += 1
+        return levels
+
+
+# ------------------------------------------------------------------ discrete
+DISC_PARALLEL_TESTS = 2  # find_execution_specification: 2 tests per edge, 1 edge per block
+
+
+def disc_cubin_path(p: int, n: int, max_dim: int, max_level: int) -> Path:
+    return _HERE / "_ref" / f"ref_disc_p{p}_n{n}_d{max_dim}_l{max_level}.cubin"
+
+
+def disc_working_memory_bytes(p: int, max_dim: int, max_level: int) -> int:
+    """find_execution_specification with memory reduction factor 1: the largest over
+    levels 1..L of 4 bytes x (contingency + marginal tables) x parallel tests."""
+    best = 0
+    for level in range(1, max_level + 1):
+        ds = max_dim ** level
+        storage = ds * max_dim * max_dim + 2 * ds * max_dim + ds
+        best = max(best, 4 * storage * (p * p * DISC_PARALLEL_TESTS))
+    return best
+
+
+def ordinal_encode(data):
+    """Per column, each value's rank among the column's distinct values (what
+    sklearn's OrdinalEncoder gives for integer columns), column-major uint8, and dims."""
+    import numpy as np
+
+    n, p = data.shape
+    codes = np.empty((p, n), np.uint8)
+    for j in range(p):
+        _, inv = np.unique(data[:, j], return_inverse=True)
+        codes[j] = inv.astype(np.uint8)
+    dims = (codes.max(axis=1).astype(np.int64) + 1).astype(np.uint8) if n else np.zeros(p, np.uint8)
+    return codes, dims
+
+
+class RefDiscreteKernels:
+    """The reference's discrete kernels for one (variables, samples, max_dim, max_level)
+    shape."""
+
+    def __init__(self, p: int, n: int, max_dim: int, max_level: int):
+        path = disc_cubin_path(p, n, max_dim, max_level)
+        if not path.exists():
+            raise RefGpuUnavailable(f"{path.name} not built (the reference checkout was absent at build time)")
+        self.p, self.n, self.max_dim, self.max_level = p, n, max_dim, max_level
+        self.mod = _load_module(path)
+        cu = _driver()
+        self.level = {}
+        for l in range(max_level + 1):
+            f = ct.c_void_p()
+            _check(cu.cuModuleGetFunction(ct.byref(f), self.mod, f"ref_disc_level_{l}".encode()), "cuModuleGetFunction")
+            self.level[l] = f
+        self.compact = ct.c_void_p()
+        _check(cu.cuModuleGetFunction(ct.byref(self.compact), self.mod, b"ref_compact"), "cuModuleGetFunction")
+
+    def __del__(self):
+        try:
+            if _cuda is not None and self.mod:
+                _cuda.cuModuleUnload(self.mod)
+        except Exception:
+            pass
+
+    def alloc(self, codes, dims):
+        """Device buffers as discover_skeleton_discrete.py:38-70 allocates them."""
+        import numpy as np
+        import torch
+
+        p, n, L = self.p, self.n, self.max_level
+        if codes.shape != (p, n) or codes.dtype != np.uint8:
+            raise ValueError("codes must be (p, n) uint8, column-major samples")
+        if int(dims.max()) != self.max_dim:
+            raise ValueError(f"largest cardinality {int(dims.max())} != the module's max_dim {self.max_dim}")
+        if np.any(codes.max(axis=1) >= dims):
+            raise ValueError("a code is not below its column's cardinality")
+        return {"data": torch.from_numpy(np.ascontiguousarray(codes)).cuda(),
+                "dims": torch.from_numpy(np.ascontiguousarray(dims)).cuda(),
+                "G": torch.ones((p, p), dtype=torch.int16, device="cuda"),
+                "Gc": torch.ones((p, p), dtype=torch.int32, device="cuda"),
+                "sep": torch.full((p * p * max(L, 1),), -1, dtype=torch.int32, device="cuda"),
+                "pmax": torch.zeros((p, p), dtype=torch.float32, device="cuda"),
+                "wm": torch.empty(disc_working_memory_bytes(p, self.max_dim, L), dtype=torch.uint8, device="cuda")}
+
+    def reset(self, bufs):
+        bufs["G"].fill_(1)
+        bufs["sep"].fill_(-1)
+        bufs["pmax"].zero_()
+
+    def run(self, alpha: float, bufs) -> int:
+        """One skeleton level loop; returns the number of levels run."""
+        import torch
+
+        p, L = self.p, self.max_level
+        stream = torch.cuda.current_stream().cuda_stream
+        ptr = lambda t: ct.c_void_p(t.data_ptr())  # noqa: E731
+        levels = 0
+        for level in range(L + 1):
+            if level == 0:
+                grid, block = (p, p), (32, 1, 1)
+            else:
+                _launch(self.compact, (math.ceil(p / 512), 1), (min(512, p), 1, 1),
+                        [ptr(bufs["G"]), ptr(bufs["Gc"]), ct.c_uint(0)], stream)
+                if int(bufs["Gc"][:, 0].max().item()) - 1 < level:
+                    break
+                grid, block = (p, p), (64, DISC_PARALLEL_TESTS, 1)
+            _launch(self.level[level], grid, block,
+                    [ptr(bufs["data"]), ptr(bufs["G"]), ptr(bufs["Gc"]), ptr(bufs["dims"]), ct.c_double(alpha),
+                     ptr(bufs["wm"]), ptr(bufs["sep"]), ptr(bufs["pmax"])], stream)
             levels += 1
         return levels

@@ -43,3 +43,45 @@ def test_reference_kernels_skeleton_equals_oracle(p, n, deg, seed, alpha, L):
         assert list(sep[b, a][sep[b, a] >= 0]) == list(S)
         z = og.gaussian_ci_z(C, np.array([a]), np.array([b]), S[None, :].astype(np.int64))[0]
         assert z < thr[len(S)], (a, b, S, z)
+
+
+DCASES = [(24, 4000, 2.0, 5, 0.05, 3), (200, 50000, 2.0, 3, 0.05, 3)]
+
+
+@pytest.mark.parametrize("p,n,deg,seed,alpha,L", DCASES)
+def test_reference_discrete_kernels_skeleton_equals_oracle(p, n, deg, seed, alpha, L):
+    """discrete_ci.cu on the GPU: skeleton equal to the C oracle's, and each separation
+    set it records gives p >= alpha under the oracle's test."""
+    import ctypes as ct
+
+    import torch
+
+    from gpucsl_gb300.synthetic import discrete_bn_data
+    from oracle import cbind, ref_gpu
+
+    codes, dims = ref_gpu.ordinal_encode(discrete_bn_data(p, n, deg, seed).data)
+    try:
+        K = ref_gpu.RefDiscreteKernels(p, n, int(dims.max()), L)
+    except ref_gpu.RefGpuUnavailable as e:
+        pytest.skip(str(e))
+    Go = np.zeros((p, p), np.uint16)
+    sepo = np.full((p, p, L), -1, np.int32)
+    pmo = np.zeros((p, p))
+    st = cbind.OrcStats()
+    cbind.lib().orc_discrete_skeleton(cbind.ptr(codes), n, n, p, cbind.ptr(dims), alpha, L, cbind.ptr(Go),
+                                      cbind.ptr(sepo), cbind.ptr(pmo), 0, ct.byref(st))
+    bufs = K.alloc(codes, dims)
+    K.run(alpha, bufs)
+    torch.cuda.synchronize()
+    G = bufs["G"].cpu().numpy() != 0
+    assert np.array_equal(G, Go != 0), int((G != (Go != 0)).sum())
+
+    sep = bufs["sep"].cpu().numpy().reshape(p, p, L)
+    work = np.zeros(int(dims.max()) ** (L + 2) + 4, np.uint32)
+    iu, ju = np.nonzero(np.triu(~G & (sep[:, :, 0] >= 0), 1))
+    for a, b in list(zip(iu, ju))[:200]:
+        S = np.ascontiguousarray(sep[a, b][sep[a, b] >= 0]).astype(np.int32)
+        assert list(sep[b, a][sep[b, a] >= 0]) == list(S)
+        pv = cbind.lib().orc_discrete_test(cbind.ptr(codes), n, n, cbind.ptr(dims), int(a), int(b), cbind.ptr(S),
+                                           len(S), cbind.ptr(work), None)
+        assert pv >= alpha, (a, b, S, pv)
