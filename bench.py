@@ -16,8 +16,11 @@ sepset records inside the timed region.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpucsl_gb300|reference]
 
 --impl reference times the CPU restatement of the reference's skeleton loop (the
-reference has no CPU path of its own; its GPU code needs cupy, which is not installed)
-on the host cores, on the same workload and metric.  Under torchrun each rank solves
+reference has no CPU path of its own; its cupy host layer is not installed) on the host
+cores, on the same workload and metric, as the line's value.  The same line carries the
+reference's own Gaussian and discrete kernels, compiled unchanged for sm_103a and run
+on this GPU with the reference's launch geometry and level loop
+(`reference_gpu_kernels`, `reference_gpu_kernels_discrete`).  Under torchrun each rank solves
 its own instance (replicas; the skeleton has no data-path exchange), and the value is
 the tests of all ranks divided by the slowest rank's time.
 """
