@@ -176,3 +176,19 @@ def test_oracle_process_pool_matches_serial():
     assert np.array_equal(a.sepsets, b.sepsets)
     assert np.array_equal(a.pmax, b.pmax)
     assert [s.tests_canonical for s in a.levels] == [s.tests_canonical for s in b.levels]
+
+
+def test_reference_kernel_host_sizing():
+    """Host-side sizing of the reference-kernel baseline: the discrete working memory is
+    find_execution_specification's figure (4 bytes x (D^l D^2 + 2 D^l D + D^l) x p x p x 2
+    parallel tests, largest over levels), and the ordinal codes are per-column ranks of
+    the distinct values with dims = largest code + 1 (a constant column has dims 1)."""
+    from oracle import ref_gpu
+
+    assert ref_gpu.disc_working_memory_bytes(200, 5, 3) == 4 * (125 * 25 + 2 * 125 * 5 + 125) * 200 * 200 * 2
+    assert ref_gpu.disc_working_memory_bytes(24, 5, 1) == 4 * (5 * 25 + 2 * 5 * 5 + 5) * 24 * 24 * 2
+    X = np.array([[7, 3, 9], [2, 3, 9], [7, 3, 4], [5, 3, 9]], dtype=np.uint8)
+    codes, dims = ref_gpu.ordinal_encode(X)
+    assert codes.shape == (3, 4) and codes.dtype == np.uint8
+    assert codes[0].tolist() == [2, 0, 2, 1] and codes[1].tolist() == [0, 0, 0, 0] and codes[2].tolist() == [1, 1, 0, 1]
+    assert dims.tolist() == [3, 1, 2]
