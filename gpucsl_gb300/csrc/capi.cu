@@ -52,6 +52,8 @@ cudaError_t corr_f64(const void *X, int dtype, long long n, int p, long long ldx
 int disc_table_cap(int device);
 void disc_level_caps(int cap_full, int max_dim, int L, int &table_cap, int &part_cap);
 cudaError_t launch_disc_tests(const DiscLevelArgs &A, int num_sms, cudaStream_t s);
+cudaError_t launch_disc_validate(const uint8_t *data, long long ld, long long n, int p, const uint8_t *dims,
+                                 DevState *st, int num_sms, cudaStream_t s);
 cudaError_t launch_disc_weights(const int *adj, int p, int L, long long *w, DevState *st, cudaStream_t s);
 cudaError_t launch_disc_finalize(const int *adj, int p, int L, uint16_t *G, unsigned long long *win, int *sep,
                                  int max_level, int *rec, long long rec_cap, DevState *st, int num_sms,
@@ -562,6 +564,8 @@ int gcsl_disc_skeleton(const uint8_t *data, int64_t ld, int64_t n, int32_t p, co
     if (e != cudaSuccess) return GCSL_ERR_DEVICE;
     DiscLevelArgs A{data, ld, n, p, dims, alpha, 0, w.adj, w.prefix, G, pmax, w.win, cap, 1024, w.st};
     host::disc_level_caps(cap, max_dim, 0, A.table_cap, A.part_cap);
+    // codes in range once per solve; the test kernels skip the per-sample checks then
+    if (host::launch_disc_validate(data, ld, n, p, dims, w.st, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
     if (host::launch_disc_tests(A, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
     int last_enqueued = 0;
     int rc = run_levels(max_level, w.st, s, [&](int level) -> cudaError_t {

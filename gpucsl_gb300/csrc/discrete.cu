@@ -160,9 +160,16 @@ __device__ __forceinline__ void tri_pair(long long t, int &vi, int &vj) {
 // Count the table N[s][a][b] of one test into shared memory (all threads of the CTA).
 // S / mult live in shared memory; `copies` replicas of T counters are merged into the
 // first one before returning.
+//
+// `trusted`: every code of every column is below its cardinality (checked once per
+// solve by disc_validate_kernel), so no sample needs a range check.  Tables of at most
+// 256 cells then take the packed path: with every code in range each byte lane of
+// ((sum_k s_k m_k) * di + a) * dj + b stays below T <= 256, so 32-bit multiplies and
+// adds on four samples' bytes at once carry nothing between lanes and give the four
+// cell indices of the scalar formula.
 __device__ void count_table(const uint8_t *__restrict__ data, long long ld, long long n, int vi, int vj,
                             const int *S, const int *mult, int L, int di, int dj, int T, int copies,
-                            uint32_t *sm_tab, int *bad) {
+                            uint32_t *sm_tab, int *bad, bool trusted) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int k = tid; k < T * copies; k += nt) sm_tab[k] = 0;
     __syncthreads();
@@ -170,6 +177,39 @@ __device__ void count_table(const uint8_t *__restrict__ data, long long ld, long
     const uint4 *ci = reinterpret_cast<const uint4 *>(data + (size_t)vi * ld);
     const uint4 *cj = reinterpret_cast<const uint4 *>(data + (size_t)vj * ld);
     const long long nvec = (n + 15) >> 4;
+    if (trusted && T <= 256) {
+        const long long nfull = n >> 4;  // vectors of 16 samples, all valid
+        for (long long v = tid; v < nfull; v += nt) {
+            uint32_t s4[4] = {0u, 0u, 0u, 0u};
+            for (int k = 0; k < L; ++k) {
+                const uint4 w = __ldg(reinterpret_cast<const uint4 *>(data + (size_t)S[k] * ld) + v);
+                const uint32_t mk = (uint32_t)mult[k];
+                s4[0] += w.x * mk;
+                s4[1] += w.y * mk;
+                s4[2] += w.z * mk;
+                s4[3] += w.w * mk;
+            }
+            const uint4 xi = __ldg(ci + v), xj = __ldg(cj + v);
+            const uint32_t idx4[4] = {(s4[0] * (uint32_t)di + xi.x) * (uint32_t)dj + xj.x,
+                                      (s4[1] * (uint32_t)di + xi.y) * (uint32_t)dj + xj.y,
+                                      (s4[2] * (uint32_t)di + xi.z) * (uint32_t)dj + xj.z,
+                                      (s4[3] * (uint32_t)di + xi.w) * (uint32_t)dj + xj.w};
+#pragma unroll
+            for (int q = 0; q < 16; ++q) atomicAdd(&tab[(idx4[q >> 2] >> (8 * (q & 3))) & 0xffu], 1u);
+        }
+        // the last, partial vector
+        if (tid == 0 && (n & 15)) {
+            const long long v = nfull;
+            const int nvalid = (int)(n & 15);
+            for (int q = 0; q < nvalid; ++q) {
+                const size_t off = (size_t)(v << 4) + q;
+                int sidx = 0;
+                for (int k = 0; k < L; ++k) sidx += (int)data[(size_t)S[k] * ld + off] * mult[k];
+                const int a = data[(size_t)vi * ld + off], b = data[(size_t)vj * ld + off];
+                atomicAdd(&tab[(sidx * di + a) * dj + b], 1u);
+            }
+        }
+    } else
     for (long long v = tid; v < nvec; v += nt) {
         int sidx[16];
 #pragma unroll
@@ -345,8 +385,15 @@ __global__ void __launch_bounds__(256) disc_test_kernel(DiscLevelArgs A) {
     __shared__ int s_bad;
     // per-stratum statistics follow the counters (8-byte aligned)
     double *s_part = reinterpret_cast<double *>(sm_tab + ((A.table_cap + 1) & ~1));
+    __shared__ int s_trusted;
     DevState *st = A.st;
-    if (threadIdx.x == 0) s_bad = 0;
+    if (threadIdx.x == 0) {
+        s_bad = 0;
+        // codes checked in range for this solve: disc_validate_kernel ran before level 0
+        // and leaves the status 0 only then (any other error also selects the checked
+        // path); read once per CTA, seen by all threads after the first barrier below
+        s_trusted = *(volatile const int32_t *)&st->status == 0;
+    }
     const int L = A.level;
     if (L > 0) {
         if (st->done) return;
@@ -359,6 +406,7 @@ __global__ void __launch_bounds__(256) disc_test_kernel(DiscLevelArgs A) {
     }
     const long long total = (L == 0) ? (long long)A.p * (A.p - 1) / 2 : A.prefix[A.p];
     const int tid = threadIdx.x;
+
     for (long long t = blockIdx.x; t < total; t += gridDim.x) {
         if (tid == 0) {
             int vi, vj;
@@ -397,7 +445,7 @@ __global__ void __launch_bounds__(256) disc_test_kernel(DiscLevelArgs A) {
         }
         const int vi = s_hdr[0], vj = s_hdr[1], di = s_hdr[2], dj = s_hdr[3], dim_s = s_hdr[4];
         count_table(A.data, A.ld, A.n, vi, vj, s_S, s_mult, L, di, dj, dim_s * di * dj, s_hdr[5], sm_tab,
-                    &s_bad);
+                    &s_bad, s_trusted != 0);
         const double chi = table_chi2(sm_tab, dim_s, di, dj, s_part);
         if (tid == 0 && s_bad) set_status(st, GCSL_ERR_INVALID_ARG);
         double pv = 1.0;
@@ -459,7 +507,7 @@ __global__ void __launch_bounds__(256) disc_table_kernel(const uint8_t *data, lo
     const int T = dim_s * di * dj;
     __shared__ int s_bad;
     if (threadIdx.x == 0) s_bad = 0;
-    count_table(data, ld, n, vi, vj, s_S, s_mult, L, di, dj, T, s_hdr[3], sm_tab, &s_bad);
+    count_table(data, ld, n, vi, vj, s_S, s_mult, L, di, dj, T, s_hdr[3], sm_tab, &s_bad, false);
     for (int k = threadIdx.x; k < T; k += blockDim.x) counts[k] = sm_tab[k];
     const double chi = table_chi2(sm_tab, dim_s, di, dj, s_part);
     if (threadIdx.x == 0) {
@@ -473,6 +521,38 @@ __global__ void __launch_bounds__(256) disc_table_kernel(const uint8_t *data, lo
 }
 
 // Per-row weights deg_r * C(deg_r - 1, L) of the level's flattened test list.
+// Codes in range: every code of columns 0..p-1 (samples 0..n-1) below its cardinality.
+// Sets GCSL_ERR_INVALID_ARG otherwise, which makes the test kernels check every sample.
+// A byte x of a word is >= d (1 <= d <= 128) iff the high bit of (x + 128 - d) | x is
+// set; with all bytes below d nothing carries between bytes, and a byte >= 128 (which
+// may carry) has its own high bit set, so the word test is exact.
+__global__ void __launch_bounds__(256) disc_validate_kernel(const uint8_t *__restrict__ data, long long ld,
+                                                            long long n, int p, const uint8_t *__restrict__ dims,
+                                                            DevState *st) {
+    const long long nvec = (n + 15) >> 4;
+    const long long total = nvec * p;
+    bool bad = false;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int col = (int)(i / nvec);
+        const long long v = i - (long long)col * nvec;
+        const uint32_t d = dims[col];
+        const uint4 w = __ldg(reinterpret_cast<const uint4 *>(data + (size_t)col * ld) + v);
+        const long long rem = n - (v << 4);
+        if (d == 0 || d > 128 || rem < 16) {  // rare: byte by byte
+            const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+            const int nvalid = rem >= 16 ? 16 : (int)rem;
+            for (int q = 0; q < nvalid; ++q) bad |= ((ww[q >> 2] >> (8 * (q & 3))) & 0xffu) >= d;
+        } else {
+            const uint32_t add = (0x80u - d) * 0x01010101u;
+            const uint32_t hit = (((w.x + add) | w.x) | ((w.y + add) | w.y) | ((w.z + add) | w.z) |
+                                  ((w.w + add) | w.w)) & 0x80808080u;
+            bad |= hit != 0;
+        }
+    }
+    if (__any_sync(GCSL_FULL_MASK, bad) && (threadIdx.x & 31) == 0) set_status(st, GCSL_ERR_INVALID_ARG);
+}
+
 __global__ void disc_weights_kernel(const int *__restrict__ adj, int p, int L, long long *__restrict__ w,
                                     DevState *st) {
     if (st->done) return;
@@ -597,6 +677,13 @@ cudaError_t launch_disc_tests(const DiscLevelArgs &A, int num_sms, cudaStream_t 
     disc_test_kernel<<<num_sms * per_sm, 256, smem, s>>>(A);
     note_launch(1);
     return note_error("disc_test_kernel launch", cudaGetLastError());
+}
+
+cudaError_t launch_disc_validate(const uint8_t *data, long long ld, long long n, int p, const uint8_t *dims,
+                                 DevState *st, int num_sms, cudaStream_t s) {
+    disc_validate_kernel<<<num_sms * 4, 256, 0, s>>>(data, ld, n, p, dims, st);
+    note_launch(1);
+    return note_error("disc_validate_kernel launch", cudaGetLastError());
 }
 
 cudaError_t launch_disc_weights(const int *adj, int p, int L, long long *w, DevState *st, cudaStream_t s) {
