@@ -110,7 +110,8 @@ class RefGaussianKernels:
     def __init__(self, p: int, max_level: int):
         path = cubin_path(p, max_level)
         if not path.exists():
-            raise RefGpuUnavailable(f"{path.name} not built (the reference checkout was absent at build time)")
+            raise RefGpuUnavailable(f"oracle/_ref/{path.name} is absent: oracle/build.py builds it only where the "
+                                    "reference sources are present, and it is not part of the committed tree")
         self.p, self.max_level = p, max_level
         self.mod = _load_module(path)
         cu = _driver()
@@ -230,7 +231,8 @@ class RefDiscreteKernels:
     def __init__(self, p: int, n: int, max_dim: int, max_level: int):
         path = disc_cubin_path(p, n, max_dim, max_level)
         if not path.exists():
-            raise RefGpuUnavailable(f"{path.name} not built (the reference checkout was absent at build time)")
+            raise RefGpuUnavailable(f"oracle/_ref/{path.name} is absent: oracle/build.py builds it only where the "
+                                    "reference sources are present, and it is not part of the committed tree")
         self.p, self.n, self.max_dim, self.max_level = p, n, max_dim, max_level
         self.mod = _load_module(path)
         cu = _driver()
