@@ -88,3 +88,33 @@ def test_gauss_rejects_pair_index_overflow(built_lib):
     dummy = ct.c_void_p(16)  # never dereferenced: the size check comes first
     rc = L.gcsl_gauss_skeleton(dummy, p, 100, thr, 1, 0, dummy, None, None, 0, dummy, None, dummy, 1 << 40, None)
     assert rc == _lib.GCSL_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("case", ["ld_not_16", "ld_below_n", "misaligned", "max_dim_0", "max_dim_256", "p_0",
+                                  "no_workspace"])
+def test_disc_argument_checks(built_lib, case):
+    """gcsl_disc_skeleton's argument checks run on the host before any device call and
+    before any pointer is dereferenced (the addresses below are never read)."""
+    from gpucsl_gb300 import _lib
+
+    L = _lib.lib()
+    a = dict(data=16, ld=64, n=50, p=4, dims=16, max_dim=5, G=16, pmax=16, ws=16, ws_bytes=1 << 40)
+    expect = _lib.GCSL_ERR_INVALID_ARG
+    if case == "ld_not_16":
+        a["ld"] = 60
+    elif case == "ld_below_n":
+        a["ld"], a["n"] = 48, 50
+    elif case == "misaligned":
+        a["data"] = 24
+    elif case == "max_dim_0":
+        a["max_dim"] = 0
+    elif case == "max_dim_256":
+        a["max_dim"] = 256
+    elif case == "p_0":
+        a["p"] = 0
+    elif case == "no_workspace":
+        a["ws"], expect = None, _lib.GCSL_ERR_WORKSPACE
+    vp = lambda x: None if x is None else ct.c_void_p(x)  # noqa: E731
+    rc = L.gcsl_disc_skeleton(vp(a["data"]), a["ld"], a["n"], a["p"], vp(a["dims"]), a["max_dim"], 0.05, 3,
+                              vp(a["G"]), None, None, 0, vp(a["pmax"]), None, vp(a["ws"]), a["ws_bytes"], None)
+    assert rc == expect, (case, rc)
