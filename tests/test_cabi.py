@@ -118,3 +118,42 @@ def test_disc_argument_checks(built_lib, case):
     rc = L.gcsl_disc_skeleton(vp(a["data"]), a["ld"], a["n"], a["p"], vp(a["dims"]), a["max_dim"], 0.05, 3,
                               vp(a["G"]), None, None, 0, vp(a["pmax"]), None, vp(a["ws"]), a["ws_bytes"], None)
     assert rc == expect, (case, rc)
+
+
+NULL_CALLS = {
+    # entry point: arguments with a null required pointer (or a size out of range)
+    "gcsl_corr_f64": (None, 0, 100, 4, 4, None, None, 0, None),
+    "gcsl_corr_f64_tc": (None, 0, 100, 4, 4, None, None, 0, None),
+    "gcsl_corr_tc_digits": (None, 0, 100, 4, 4, None, 0, None),
+    "gcsl_corr_tc_product": (100, 4, None, None, 0, None),
+    "gcsl_orient_edges": (None, 4, None, 0, None, None, None, 0, None),
+    "gcsl_gauss_batch_run": (None, None),
+    "gcsl_corr_tc_batch_run": (None, None),
+    "gcsl_gauss_batch_set_lanes": (None, 1, 32),
+    "gcsl_compact": (None, 4, None, None),
+    "gcsl_unrank": (5, 0, 1, None, None),
+    "gcsl_pchisq": (None, None, 1, None, None),
+    "gcsl_tc_gemm_bf16": (None, None, None, 128, 128, 64, None, None),
+}
+
+
+@pytest.mark.parametrize("name", sorted(NULL_CALLS))
+def test_null_or_out_of_range_arguments_are_rejected_on_the_host(built_lib, name):
+    """Each compute entry point rejects a null required pointer (or a size out of range)
+    with GCSL_ERR_INVALID_ARG before any device call."""
+    from gpucsl_gb300 import _lib
+
+    L = _lib.lib()
+    fn = getattr(L, name)
+    if fn.argtypes is None or len(fn.argtypes) != len(NULL_CALLS[name]):
+        pytest.skip(f"{name}: argtypes not declared with this arity")
+    assert fn(*NULL_CALLS[name]) == _lib.GCSL_ERR_INVALID_ARG
+
+
+def test_precision_switch_range(built_lib):
+    from gpucsl_gb300 import _lib
+
+    L = _lib.lib()
+    assert L.gcsl_set_test_precision(3) == _lib.GCSL_ERR_INVALID_ARG
+    assert L.gcsl_set_test_precision(-1) == _lib.GCSL_ERR_INVALID_ARG
+    assert L.gcsl_set_test_precision(0) == _lib.GCSL_OK
