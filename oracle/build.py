@@ -69,6 +69,16 @@ def ref_gpu_cubin(p: int, max_level: int) -> Path:
     return HERE / "_ref" / f"ref_gauss_p{p}_l{max_level}.cubin"
 
 
+def ref_gauss_instantiations(p: int, L: int) -> str:
+    """The translation unit compiled for one Gaussian shape: the reference's file and the
+    template instances its runtime compiler would request (kernel_management.py:199-221)."""
+    sig = "(double *, unsigned short *, int *, double, int *, float *, int)"
+    lines = ['#include "gaussian_ci.cu"', f"template __global__ void gaussian_ci_level_0<0, {p}, {L}>{sig};"]
+    lines += [f"template __global__ void gaussian_ci_level_n<{l}, {p}, {L}>{sig};" for l in range(1, L + 1)]
+    lines.append(f"template __global__ void compact<{p}, {p}u>(unsigned short *, unsigned int *, unsigned int);")
+    return "\n".join(lines) + "\n"
+
+
 def build_ref_gpu(force: bool = False, shapes=REF_GPU_SHAPES) -> list[Path]:
     """Compile the reference's Gaussian CI kernels for sm_103a; [] when the reference
     checkout is absent.  Each module holds gaussian_ci_level_0<0, P, L>,
@@ -82,13 +92,8 @@ def build_ref_gpu(force: bool = False, shapes=REF_GPU_SHAPES) -> list[Path]:
         cubin = ref_gpu_cubin(p, L)
         cubin.parent.mkdir(exist_ok=True)
         if force or _stale(cubin, *deps, Path(__file__)):
-            sig = "(double *, unsigned short *, int *, double, int *, float *, int)"
-            lines = ['#include "gaussian_ci.cu"',
-                     f"template __global__ void gaussian_ci_level_0<0, {p}, {L}>{sig};"]
-            lines += [f"template __global__ void gaussian_ci_level_n<{l}, {p}, {L}>{sig};" for l in range(1, L + 1)]
-            lines.append(f"template __global__ void compact<{p}, {p}u>(unsigned short *, unsigned int *, unsigned int);")
             inst = cubin.with_suffix(".cu")
-            inst.write_text("\n".join(lines) + "\n")
+            inst.write_text(ref_gauss_instantiations(p, L))
             cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-DNDEBUG",
                    f"-I{REF_CUDA}", f"-I{REF_CUDA / 'helpers'}", str(inst), "-o", str(cubin)]
             subprocess.run(cmd, check=True)
@@ -106,6 +111,23 @@ def ref_disc_cubin(p: int, n: int, max_dim: int, max_level: int) -> Path:
     return HERE / "_ref" / f"ref_disc_p{p}_n{n}_d{max_dim}_l{max_level}.cubin"
 
 
+def ref_disc_instantiations(p: int, n: int, md: int, L: int) -> str:
+    """The translation unit compiled for one discrete shape: the reference's file read
+    with __global__ as __device__, and one extern "C" kernel per level (and compact)
+    that calls the reference's kernel body with its template arguments."""
+    sig = "(uint8_t *d, unsigned short *G, int *Gc, uint8_t *dims, double alpha, uint32_t *wm, int *sep, float *pmax)"
+    args = "(d, G, Gc, dims, alpha, wm, sep, pmax)"
+    targs = f"{p}, {REF_DISC_PARALLEL_TESTS}, {md}, {n}, {L}"
+    lines = ["#include <cstdint>", '#pragma push_macro("__global__")', "#undef __global__",
+             "#define __global__ __device__", '#include "discrete_ci.cu"', '#pragma pop_macro("__global__")']
+    for l in range(L + 1):
+        body = "discrete_ci_level_0" if l == 0 else "discrete_ci_level_n"
+        lines.append(f'extern "C" __global__ void ref_disc_level_{l}{sig} {{ {body}<{l}, {targs}>{args}; }}')
+    lines.append('extern "C" __global__ void ref_compact(unsigned short *G, unsigned int *Gc, unsigned int di) '
+                 f"{{ compact<{p}, {p}u>(G, Gc, di); }}")
+    return "\n".join(lines) + "\n"
+
+
 def build_ref_gpu_discrete(force: bool = False, shapes=REF_DISC_SHAPES) -> list[Path]:
     """Compile the reference's discrete CI kernels for sm_103a; [] when the reference
     checkout is absent.  Exported names: ref_disc_level_{l} for l = 0..L, ref_compact."""
@@ -119,20 +141,8 @@ def build_ref_gpu_discrete(force: bool = False, shapes=REF_DISC_SHAPES) -> list[
         cubin = ref_disc_cubin(p, n, md, L)
         cubin.parent.mkdir(exist_ok=True)
         if force or _stale(cubin, *deps, Path(__file__)):
-            sig = ("(uint8_t *d, unsigned short *G, int *Gc, uint8_t *dims, double alpha, uint32_t *wm, int *sep, "
-                   "float *pmax)")
-            args = "(d, G, Gc, dims, alpha, wm, sep, pmax)"
-            targs = f"{p}, {REF_DISC_PARALLEL_TESTS}, {md}, {n}, {L}"
-            lines = ["#include <cstdint>", '#pragma push_macro("__global__")', "#undef __global__",
-                     "#define __global__ __device__", '#include "discrete_ci.cu"', '#pragma pop_macro("__global__")']
-            for l in range(L + 1):
-                body = "discrete_ci_level_0" if l == 0 else "discrete_ci_level_n"
-                lines.append(f'extern "C" __global__ void ref_disc_level_{l}{sig} '
-                             f"{{ {body}<{l}, {targs}>{args}; }}")
-            lines.append('extern "C" __global__ void ref_compact(unsigned short *G, unsigned int *Gc, unsigned int di) '
-                         f"{{ compact<{p}, {p}u>(G, Gc, di); }}")
             inst = cubin.with_suffix(".cu")
-            inst.write_text("\n".join(lines) + "\n")
+            inst.write_text(ref_disc_instantiations(p, n, md, L))
             cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-DNDEBUG",
                    f"-I{REF_CUDA}", f"-I{REF_CUDA / 'helpers'}", str(inst), "-o", str(cubin)]
             subprocess.run(cmd, check=True)

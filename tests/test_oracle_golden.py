@@ -192,3 +192,23 @@ def test_reference_kernel_host_sizing():
     assert codes.shape == (3, 4) and codes.dtype == np.uint8
     assert codes[0].tolist() == [2, 0, 2, 1] and codes[1].tolist() == [0, 0, 0, 0] and codes[2].tolist() == [1, 1, 0, 1]
     assert dims.tolist() == [3, 1, 2]
+
+
+def test_reference_kernel_instantiation_lists():
+    """The translation units oracle/build.py compiles for the reference's kernels: every
+    level 0..L instantiated once, with the names oracle/ref_gpu.py looks up."""
+    from oracle import build as ob
+
+    g = ob.ref_gauss_instantiations(1000, 10)
+    assert g.startswith('#include "gaussian_ci.cu"')
+    assert g.count("gaussian_ci_level_0<0, 1000, 10>") == 1
+    for l in range(1, 11):
+        assert g.count(f"gaussian_ci_level_n<{l}, 1000, 10>") == 1
+    assert "gaussian_ci_level_n<11," not in g and "compact<1000, 1000u>" in g
+    d = ob.ref_disc_instantiations(200, 50000, 5, 3)
+    assert "#define __global__ __device__" in d and '#include "discrete_ci.cu"' in d
+    for l in range(4):
+        assert d.count(f'extern "C" __global__ void ref_disc_level_{l}(') == 1
+        body = "discrete_ci_level_0" if l == 0 else "discrete_ci_level_n"
+        assert f"{body}<{l}, 200, 2, 5, 50000, 3>" in d
+    assert 'extern "C" __global__ void ref_compact(' in d
