@@ -200,6 +200,36 @@ def cpu_workers() -> int:
     return os.cpu_count() or 1
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), with the architecture."""
+    import platform
+
+    name = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not name:
+        try:
+            for line in Path("/proc/cpuinfo").read_text().splitlines():
+                if line.lower().startswith(("model name", "cpu part")):
+                    name = line.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            pass
+    return f"{name or 'unknown'} ({platform.machine()})"
+
+
+def workload_config(levels_run: int, E: int, world: int) -> dict:
+    """The workload's config, printed identically by both arms."""
+    return {"workload": WORKLOAD, "p": P, "n": N, "expected_degree": DEG, "alpha": ALPHA, "max_level": P - 2,
+            "levels_run": levels_run, "tests_per_step": E, "parallelism": f"replicas x{world}"}
+
+
 def cpu_oracle_solve(data):
     """One CPU solve with the oracle (numpy FP64) on every host core: correlation (BLAS
     threads) + level loop (each level's edges split over a spawned process per core) +
@@ -220,6 +250,99 @@ def blas_threads() -> int:
     except Exception:
         pass
     return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------ discrete leg
+DISC_P, DISC_N, DISC_L, DISC_ALPHA = 200, 50000, 3, 0.05
+
+
+def discrete_leg(flush, reps: int = 12) -> dict:
+    """Discrete skeleton (p = 200, n = 50000 ordinal codes, cardinality 2..5, alpha 0.05,
+    levels <= 3), L2 flushed before every timed solve.  Roofline: each test scans its
+    l + 2 code columns once, n * (l + 2) bytes, so the algorithmic bytes of a solve are
+    sum_l tests_l * n * (l + 2); the 10 MB of codes stay in the 129 MB L2 after the
+    first pass, so the figure is relative to HBM bandwidth but served from L2 and can
+    exceed 1."""
+    import torch
+
+    from gpucsl_gb300 import engine
+    from gpucsl_gb300.synthetic import discrete_bn_data
+
+    d = discrete_bn_data(DISC_P, DISC_N, 2, 3)
+    codes, dims = engine.ordinal_encode(d.data)
+    ds = engine.DiscreteSolver(DISC_P, DISC_N, DISC_L, int(dims.max()))
+    ds.load(codes, dims)
+    for _ in range(3):
+        std = ds.run(DISC_ALPHA)
+    torch.cuda.synchronize()
+    td = []
+    for _ in range(reps):
+        flush.zero_()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        std = ds.run(DISC_ALPHA)
+        s1.record()
+        torch.cuda.synchronize()
+        td.append(s0.elapsed_time(s1) / 1e3)
+    tests = [int(t) for t in std.raw["tests"]]
+    Ed = sum(tests)
+    alg_bytes = sum(t * DISC_N * (l + 2) for l, t in enumerate(tests))
+    t = statistics.mean(td)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = alg_bytes / t / 1e9
+    return {"workload": "discrete_skeleton_p200_n50000_card2-5_alpha0.05_L3", "value": round(Ed / t, 1),
+            "unit": UNIT, "ms_per_solve": round(1e3 * t, 3), "solves_timed": reps, "tests_per_solve": Ed,
+            "tests_per_level": tests, "levels_run": std.raw["levels_run"],
+            "l2": "flushed before every timed solve (256 MB write outside the events)",
+            "roofline": {"bound": "hbm", "kernel": "disc_test_kernel (whole solve time: a lower bound for the "
+                                                  "kernel)",
+                         "algorithmic_bytes_per_solve": int(alg_bytes), "achieved": round(achieved, 1),
+                         "peak": round(peak, 1), "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
+                         "note": "codes are L2-resident after the first pass: L2-relative figure, may exceed 1"}}
+
+
+def e2e_api_leg(data, solver, E: int, levels_run: int, reps: int = 10) -> dict:
+    """The reference's public call, discover_skeleton_gpu_gaussian, end to end on the
+    headline workload: NumPy FP64 samples in, NumPy skeleton, dense (p, p, L) sepsets and
+    pmax out (host copies, the correlation, the level loop and the dense sepset scatter
+    all inside the wall-clock time of the call).  max_level = the workload's terminal
+    level L* (the dense sepset array is p * p * L int32), and a `kernels=` object holds
+    the preallocated solver, as the reference's benchmark passes precompiled kernels."""
+    import numpy as np
+    import torch
+
+    from gpucsl_gb300.pc.discover_skeleton_gaussian import discover_skeleton_gpu_gaussian
+    from gpucsl_gb300.pc.kernel_management import Kernels
+
+    L = max(levels_run - 1, 0)
+    kernels = Kernels.for_gaussian_ci(P, 1, L)
+    skel = np.ones((P, P), np.uint16)
+    res = None
+    for _ in range(2):
+        res = discover_skeleton_gpu_gaussian(skel, data, None, ALPHA, L, P, N, kernels=kernels)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        res = discover_skeleton_gpu_gaussian(skel, data, None, ALPHA, L, P, N, kernels=kernels)
+        times.append(time.perf_counter() - t0)
+    G0, _, _ = solver.to_host()
+    out_res = res.result
+    t = statistics.mean(times)
+    return {"value": round(E / t, 1), "unit": UNIT, "ms_per_call": round(1e3 * t, 3), "calls_timed": reps,
+            "call": f"discover_skeleton_gpu_gaussian(skeleton, data (NumPy {N}x{P} float64), None, {ALPHA}, {L}, "
+                    f"{P}, {N}, kernels=Kernels.for_gaussian_ci({P}, 1, {L}))",
+            "h2d_bytes_per_call": int(data.nbytes),
+            "d2h_bytes_per_call": int(out_res.skeleton.nbytes + out_res.pmax.nbytes),
+            "host_outputs": f"skeleton {out_res.skeleton.shape}, sepsets {out_res.seperation_sets.shape} "
+                            f"(dense, scattered from the record pool), pmax {out_res.pmax.shape}",
+            "skeleton_identical_to_timed_solve": bool(np.array_equal(out_res.skeleton, G0))}
 
 
 # ------------------------------------------------------------ batched leg
@@ -490,12 +613,9 @@ def run_ours(args, world, rank, local):
            "warmup": max(args.warmup, 3), "ms_per_step": round(1e3 * total / args.steps, 4),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded linear-Gaussian DAG, numpy PCG64 seed 2)",
-           "config": {"workload": WORKLOAD, "p": P, "n": N, "expected_degree": DEG, "alpha": ALPHA,
-                      "max_level": P - 2, "levels_run": levels_run, "tests_per_step": E,
-                      "step": "FP64-accurate correlation (tensor cores) + levels 0..termination + pmax, samples "
-                              "resident in HBM",
-                      "l2": "flushed between steps (256 MB write outside the timed events)",
-                      "parallelism": f"replicas x{world}"},
+           "config": workload_config(levels_run, E, world),
+           "step": "FP64-accurate correlation (tensor cores) + levels 0..termination + pmax, samples resident in HBM",
+           "l2": "flushed between steps (256 MB write outside the timed events)",
            "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": int(Xh.numel() * 8),
                    "d2h_bytes_per_step": int(d2h_bytes), "ms_per_step": round(1e3 * e2e_total / len(t_e2e), 4)},
            "level_loop": {"value": round(E / statistics.mean(t_lv), 1), "unit": UNIT,
@@ -524,26 +644,11 @@ def run_ours(args, world, rank, local):
 
     # ---- discrete workload (p=200, n=50000, cardinality 2..5, alpha 0.05, max level 3)
     if not args.no_extras and rank == 0:
-        d = discrete_bn_data(200, 50000, 2, 3)
-        codes, dims = engine.ordinal_encode(d.data)
-        ds = engine.DiscreteSolver(200, 50000, 3, int(dims.max()))
-        ds.load(codes, dims)
-        ds.run(0.05)
-        torch.cuda.synchronize()
-        td = []
-        for _ in range(3):
-            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s0.record()
-            std = ds.run(0.05)
-            s1.record()
-            torch.cuda.synchronize()
-            td.append(s0.elapsed_time(s1) / 1e3)
-        Ed = int(sum(std.raw["tests"]))
-        nb = sum(int(t) for t in std.raw["tests"])
-        out["discrete"] = {"workload": "discrete_skeleton_p200_n50000_card2-5_alpha0.05_L3",
-                           "value": round(Ed / statistics.mean(td), 1), "unit": UNIT,
-                           "ms_per_solve": round(1e3 * statistics.mean(td), 3), "tests_per_solve": Ed,
-                           "levels_run": std.raw["levels_run"]}
+        out["discrete"] = discrete_leg(flush)
+
+    # ---- the drop-in API end to end: NumPy samples in, NumPy skeleton / dense sepsets / pmax out
+    if not args.no_extras and rank == 0:
+        out["e2e_api"] = e2e_api_leg(w.data, solver, E, levels_run)
 
     # ---- batched instances (split precision and FP64) against the plain per-instance path
     if not args.no_extras and rank == 0:
@@ -596,7 +701,7 @@ def run_ours(args, world, rank, local):
             out["orientation"]["cpu_oracle_ms"] = round(1e3 * (time.perf_counter() - t0), 1)
             out["orientation"]["identical_to_cpu"] = bool(np.array_equal(D_gpu, Dref))
         out["cpu_baseline"] = {"value": round(E / statistics.mean(times), 1), "unit": UNIT,
-                               "cores": cpu_workers(), "kind": "port",
+                               "cores": cpu_workers(), "kind": "port", "cpu_model": cpu_model(),
                                "sample": f"{len(times)} full solves of the same workload "
                                          f"(numpy corrcoef on {blas_threads()} BLAS threads, each level's edges "
                                          f"over {cpu_workers()} processes), mean {statistics.mean(times):.2f} s"}
@@ -722,9 +827,9 @@ def run_reference(args, world, rank):
            "steps": args.steps, "warmup": args.warmup, "solves_timed": len(times), "ms_per_step": round(1e3 * sum(times) / len(times), 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded linear-Gaussian DAG, numpy PCG64 seed 2)",
-           "config": {"workload": WORKLOAD, "p": P, "n": N, "alpha": ALPHA, "tests_per_step": E,
-                      "levels_run": len(r.levels)},
+           "config": workload_config(len(r.levels), E, world),
            "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "port",
+                            "cpu_model": cpu_model(),
                             "sample": f"{len(times)} full solves (numpy corrcoef on {blas_threads()} BLAS "
                                       f"threads, each level's edges over {cores} processes); the reference itself "
                                       "has no CPU path, and its cupy host layer is absent here (its own kernels "

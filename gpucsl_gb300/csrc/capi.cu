@@ -188,6 +188,22 @@ SideStream *side_stream() {
     return &s;
 }
 
+// Joins the side stream back into the solve's stream on every return after the fork,
+// so no side-stream work of a failed call outlives the call unordered with the stream.
+struct SideJoin {
+    SideStream *ss;
+    cudaStream_t s;
+    bool armed = false;
+    cudaError_t join() {
+        if (!armed) return cudaSuccess;
+        armed = false;
+        cudaError_t e = cudaEventRecord(ss->join, ss->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ss->join, 0);
+        return e;
+    }
+    ~SideJoin() { join(); }
+};
+
 // Copy the device state into the public stats struct.
 int finish_stats(const DevState *d_st, gcsl_stats *stats, cudaStream_t s, bool discrete_edges, long long p) {
     DevState h;
@@ -236,10 +252,10 @@ HostCtl *host_ctl() {
 // level 1 alone, then up to 8 levels per host read of two pinned words (done flag, the
 // last level's maximum degree d).  Degrees only shrink, so level l can only run while
 // d - 1 >= l: a batch never extends past min(d - 1, ...) of the last read.
+// `words` are two host words for the control reads: the calling thread's pinned words,
+// or (allocation-free path) words on the caller's stack, read by a synchronous copy.
 template <typename EnqueueLevel>
-int run_levels(int max_level, DevState *d_st, cudaStream_t s, EnqueueLevel enqueue) {
-    HostCtl *hc = host_ctl();
-    if (!hc) return GCSL_ERR_DEVICE;
+int run_levels(int max_level, DevState *d_st, cudaStream_t s, int32_t *words, EnqueueLevel enqueue) {
     int level = 1;
     int bound = std::min(max_level, GCSL_MAX_LEVELS - 1);  // highest level that may still run
     int batch = 1;
@@ -250,23 +266,23 @@ int run_levels(int max_level, DevState *d_st, cudaStream_t s, EnqueueLevel enque
             if (e != cudaSuccess) return GCSL_ERR_DEVICE;
         }
         if (level > bound) break;
-        cudaError_t e = cudaMemcpyAsync(&hc->words[0], &d_st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaMemcpyAsync(&words[0], &d_st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(&hc->words[1], &d_st->max_degree[last], sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+            e = cudaMemcpyAsync(&words[1], &d_st->max_degree[last], sizeof(int32_t), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return GCSL_ERR_DEVICE;
-        if (hc->words[0]) break;
-        bound = std::min(bound, hc->words[1] - 1);
+        if (words[0]) break;
+        bound = std::min(bound, words[1] - 1);
         // after the first level, up to 8 levels per host read (a level enqueued past the end
         // costs four early-exit launches, about as much as a host read)
         batch = 8;
     }
     if (max_level >= GCSL_MAX_LEVELS && bound >= GCSL_MAX_LEVELS - 1) {
         // levels beyond the state arrays: only an error if the loop had not finished
-        if (cudaMemcpyAsync(&hc->words[0], &d_st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        if (cudaMemcpyAsync(&words[0], &d_st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
             return GCSL_ERR_DEVICE;
-        if (!hc->words[0]) return GCSL_ERR_UNSUPPORTED_LEVEL;
+        if (!words[0]) return GCSL_ERR_UNSUPPORTED_LEVEL;
     }
     return GCSL_OK;
 }
@@ -369,6 +385,110 @@ DiscWs carve_disc(void *ws, size_t cap, int p) {
 
 }  // namespace
 
+int gcsl::host::gauss_skeleton_run(const double *C, int p, long long n_obs, const double *thresholds,
+                                   int n_thresholds, int max_level, uint16_t *G, int *sepsets, int *rec_pool,
+                                   long long rec_cap, double *pmax, gcsl_stats *stats, void *workspace,
+                                   size_t workspace_bytes, void *stream, bool allocation_free) {
+    if (!C || !G || !pmax || p < 1 || n_obs < 4 || !thresholds || n_thresholds < 1 || max_level < 0)
+        return GCSL_ERR_INVALID_ARG;
+    if (p > GCSL_GAUSS_MAX_P) return GCSL_ERR_UNSUPPORTED;
+    if (rec_pool == nullptr) rec_cap = 0;
+    GaussWs w = carve_gauss(workspace, workspace_bytes, p);
+    if (!workspace || w.bytes > workspace_bytes) return GCSL_ERR_WORKSPACE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int sms = device_sms();
+    if (cudaMemsetAsync(w.st, 0, sizeof(DevState), s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    // r2min starts at 0x7f7f... = 1.4e306, above every rho^2 < 1 the levels can store
+    if (cudaMemsetAsync(w.r2min, 0x7f, sizeof(double) * (size_t)p * p, s) != cudaSuccess) return GCSL_ERR_DEVICE;
+    LevelTimer *lt = stats && !allocation_free ? level_timer() : nullptr;
+    int n_timed = 0;  // events recorded: ev[0 .. n_timed]
+    if (lt) cudaEventRecord(lt->ev[0], s);
+    const bool mixed = mixed_tests() && max_level >= 1;
+    if (host::launch_level0(C, p, thresholds[0], G, w.zmin, w.r2min, w.kept, w.st, mixed ? w.c32 : nullptr, s) !=
+        cudaSuccess)
+        return GCSL_ERR_DEVICE;
+    if (lt) {
+        cudaEventRecord(lt->ev[1], s);
+        n_timed = 1;
+    }
+    // pmax of the pairs removed at level 0 overlaps the level loop on the side stream (the
+    // allocation-free path has none: that work goes on `s` in order)
+    SideStream *ss = nullptr;
+    int32_t stack_words[2] = {0, 0};
+    int32_t *words = stack_words;
+    if (!allocation_free) {
+        ss = side_stream();
+        HostCtl *hc = host_ctl();
+        if (!ss || !hc) return GCSL_ERR_DEVICE;
+        words = hc->words;
+    }
+    SideJoin joiner{ss, s};
+    if (ss) {
+        if (cudaEventRecord(ss->fork, s) != cudaSuccess || cudaStreamWaitEvent(ss->stream, ss->fork, 0) != cudaSuccess)
+            return GCSL_ERR_DEVICE;
+        joiner.armed = true;  // from here every return joins the side stream back into s
+    }
+    cudaStream_t aux = ss ? ss->stream : s;
+    if (host::launch_sf_table(w.sftab, aux) != cudaSuccess ||
+        host::launch_pmax_level0(C, w.zmin, p, n_obs, w.sftab, pmax, sms, aux) != cudaSuccess)
+        return GCSL_ERR_DEVICE;
+    const long long region = cand_region_ints(w.cand_cap);
+    auto enqueue = [&](int level) -> cudaError_t {
+        // level 1 compacts the full matrix; later levels only shrink the previous lists;
+        // (re)compaction writes the level's edge list; the row prefix is only needed by
+        // the shared-memory kernel of levels above GCSL_GAUSS_REG_LEVELS
+        cudaError_t e = level == 1 ? host::launch_compact(G, p, w.adj, w.up, w.st, level, w.elist, s)
+                                   : host::launch_recompact(G, p, w.adj, w.up, w.st, level, w.elist, s);
+        if (e == cudaSuccess && level > GCSL_GAUSS_REG_LEVELS) e = host::launch_scan_int(w.up, p, w.prefix, w.st, s);
+        const bool tau_valid = level < n_thresholds;
+        const double tau = tau_valid ? thresholds[level] : 0.0;
+        const bool cand = mixed && level <= GCSL_GAUSS_REG_LEVELS;
+        int *qbuf = cand ? w.cand + (size_t)(level - 1) * region : nullptr;
+        // level 1 walks its edges whole: its edges are many and short, so the level kernel
+        // alone keeps every SM busy
+        ChunkBufs ck = w.ck;
+        if (level >= 2 && level <= GCSL_GAUSS_REG_LEVELS) ck.chunk_first += (size_t)(level - 1) * ck.heavy_cap;
+        else ck.heavy = nullptr;
+        if (chunking_off()) ck.heavy = nullptr;
+        if (e == cudaSuccess)
+            e = host::launch_gauss_level(level, C, p, w.adj, w.up, w.elist, w.prefix, tau, tau_valid, G, w.zmin,
+                                         w.r2min, sepsets, max_level, rec_pool, rec_cap, w.st, sms,
+                                         mixed ? w.c32 : nullptr, qbuf, region, ck, s);
+        // the level's FP64 z* candidates only feed pmax: they run on the low-priority side
+        // stream while the next levels proceed
+        if (e == cudaSuccess && cand) {
+            if (ss) {
+                e = cudaEventRecord(ss->level[level], s);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(ss->stream, ss->level[level], 0);
+            }
+            if (e == cudaSuccess)
+                e = host::launch_cand(level, C, p, tau, w.zmin, w.r2min, qbuf, region, w.st,
+                                      ck.heavy != nullptr ? ck.chunk_first : nullptr, sms, aux);
+        }
+        if (lt && level + 1 < GCSL_MAX_LEVELS + 2) {
+            cudaEventRecord(lt->ev[level + 1], s);
+            n_timed = level + 1;
+        }
+        return e;
+    };
+    const int rc = run_levels(max_level, w.st, s, words, enqueue);
+    if (joiner.join() != cudaSuccess) return GCSL_ERR_DEVICE;
+    if (rc != GCSL_OK) return rc;
+    if (host::launch_pmax(w.kept, w.st, w.zmin, w.r2min, p, n_obs, w.sftab, pmax, sms, s) != cudaSuccess)
+        return GCSL_ERR_DEVICE;
+    const int frc = finish_stats(w.st, stats, s, false, p);
+    if (lt) {
+        // level l spans events l .. l+1 (level 0 includes the state reset); levels that
+        // were enqueued but found the loop finished are reported as well
+        for (int l = 0; l < n_timed && l < GCSL_MAX_LEVELS; ++l) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, lt->ev[l], lt->ev[l + 1]) == cudaSuccess) stats->level_ms[l] = ms;
+        }
+        cudaGetLastError();  // a failed timing query must not surface in a later launch check
+    }
+    return frc;
+}
+
 extern "C" {
 
 int gcsl_version(void) { return GCSL_ABI_VERSION; }
@@ -448,90 +568,8 @@ size_t gcsl_gauss_workspace_bytes(int32_t p, int32_t max_level) {
 int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double *thresholds, int32_t n_thresholds,
                         int32_t max_level, uint16_t *G, int32_t *sepsets, int32_t *rec_pool, int64_t rec_cap,
                         double *pmax, gcsl_stats *stats, void *workspace, size_t workspace_bytes, void *stream) {
-    if (!C || !G || !pmax || p < 1 || n_obs < 4 || !thresholds || n_thresholds < 1 || max_level < 0)
-        return GCSL_ERR_INVALID_ARG;
-    if (p > GCSL_GAUSS_MAX_P) return GCSL_ERR_UNSUPPORTED;
-    if (rec_pool == nullptr) rec_cap = 0;
-    GaussWs w = carve_gauss(workspace, workspace_bytes, p);
-    if (!workspace || w.bytes > workspace_bytes) return GCSL_ERR_WORKSPACE;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const int sms = device_sms();
-    if (cudaMemsetAsync(w.st, 0, sizeof(DevState), s) != cudaSuccess) return GCSL_ERR_DEVICE;
-    // r2min starts at 0x7f7f... = 1.4e306, above every rho^2 < 1 the levels can store
-    if (cudaMemsetAsync(w.r2min, 0x7f, sizeof(double) * (size_t)p * p, s) != cudaSuccess) return GCSL_ERR_DEVICE;
-    LevelTimer *lt = stats ? level_timer() : nullptr;
-    int n_timed = 0;  // events recorded: ev[0 .. n_timed]
-    if (lt) cudaEventRecord(lt->ev[0], s);
-    const bool mixed = mixed_tests() && max_level >= 1;
-    if (host::launch_level0(C, p, thresholds[0], G, w.zmin, w.r2min, w.kept, w.st, mixed ? w.c32 : nullptr, s) !=
-        cudaSuccess)
-        return GCSL_ERR_DEVICE;
-    if (lt) {
-        cudaEventRecord(lt->ev[1], s);
-        n_timed = 1;
-    }
-    // pmax of the pairs removed at level 0 overlaps the level loop on the side stream
-    SideStream *ss = side_stream();
-    if (!ss) return GCSL_ERR_DEVICE;
-    if (cudaEventRecord(ss->fork, s) != cudaSuccess || cudaStreamWaitEvent(ss->stream, ss->fork, 0) != cudaSuccess)
-        return GCSL_ERR_DEVICE;
-    if (host::launch_sf_table(w.sftab, ss->stream) != cudaSuccess ||
-        host::launch_pmax_level0(C, w.zmin, p, n_obs, w.sftab, pmax, sms, ss->stream) != cudaSuccess)
-        return GCSL_ERR_DEVICE;
-    const long long region = cand_region_ints(w.cand_cap);
-    auto enqueue = [&](int level) -> cudaError_t {
-        // level 1 compacts the full matrix; later levels only shrink the previous lists;
-        // (re)compaction writes the level's edge list; the row prefix is only needed by
-        // the shared-memory kernel of levels above GCSL_GAUSS_REG_LEVELS
-        cudaError_t e = level == 1 ? host::launch_compact(G, p, w.adj, w.up, w.st, level, w.elist, s)
-                                   : host::launch_recompact(G, p, w.adj, w.up, w.st, level, w.elist, s);
-        if (e == cudaSuccess && level > GCSL_GAUSS_REG_LEVELS) e = host::launch_scan_int(w.up, p, w.prefix, w.st, s);
-        const bool tau_valid = level < n_thresholds;
-        const double tau = tau_valid ? thresholds[level] : 0.0;
-        const bool cand = mixed && level <= GCSL_GAUSS_REG_LEVELS;
-        int *qbuf = cand ? w.cand + (size_t)(level - 1) * region : nullptr;
-        // level 1 walks its edges whole: its edges are many and short, so the level kernel
-        // alone keeps every SM busy
-        ChunkBufs ck = w.ck;
-        if (level >= 2 && level <= GCSL_GAUSS_REG_LEVELS) ck.chunk_first += (size_t)(level - 1) * ck.heavy_cap;
-        else ck.heavy = nullptr;
-        if (chunking_off()) ck.heavy = nullptr;
-        if (e == cudaSuccess)
-            e = host::launch_gauss_level(level, C, p, w.adj, w.up, w.elist, w.prefix, tau, tau_valid, G, w.zmin,
-                                         w.r2min, sepsets, max_level, rec_pool, rec_cap, w.st, sms,
-                                         mixed ? w.c32 : nullptr, qbuf, region, ck, s);
-        // the level's FP64 z* candidates only feed pmax: they run on the low-priority side
-        // stream while the next levels proceed
-        if (e == cudaSuccess && cand) {
-            e = cudaEventRecord(ss->level[level], s);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(ss->stream, ss->level[level], 0);
-            if (e == cudaSuccess)
-                e = host::launch_cand(level, C, p, tau, w.zmin, w.r2min, qbuf, region, w.st,
-                                      ck.heavy != nullptr ? ck.chunk_first : nullptr, sms, ss->stream);
-        }
-        if (lt && level + 1 < GCSL_MAX_LEVELS + 2) {
-            cudaEventRecord(lt->ev[level + 1], s);
-            n_timed = level + 1;
-        }
-        return e;
-    };
-    const int rc = run_levels(max_level, w.st, s, enqueue);
-    if (cudaEventRecord(ss->join, ss->stream) != cudaSuccess || cudaStreamWaitEvent(s, ss->join, 0) != cudaSuccess)
-        return GCSL_ERR_DEVICE;
-    if (rc != GCSL_OK) return rc;
-    if (host::launch_pmax(w.kept, w.st, w.zmin, w.r2min, p, n_obs, w.sftab, pmax, sms, s) != cudaSuccess)
-        return GCSL_ERR_DEVICE;
-    const int frc = finish_stats(w.st, stats, s, false, p);
-    if (lt) {
-        // level l spans events l .. l+1 (level 0 includes the state reset); levels that
-        // were enqueued but found the loop finished are reported as well
-        for (int l = 0; l < n_timed && l < GCSL_MAX_LEVELS; ++l) {
-            float ms = 0.f;
-            if (cudaEventElapsedTime(&ms, lt->ev[l], lt->ev[l + 1]) == cudaSuccess) stats->level_ms[l] = ms;
-        }
-        cudaGetLastError();  // a failed timing query must not surface in a later launch check
-    }
-    return frc;
+    return host::gauss_skeleton_run(C, p, n_obs, thresholds, n_thresholds, max_level, G, sepsets, rec_pool, rec_cap,
+                                    pmax, stats, workspace, workspace_bytes, stream, false);
 }
 
 size_t gcsl_disc_workspace_bytes(int32_t p, int64_t n, int32_t max_level, int32_t max_dim) {
@@ -567,8 +605,9 @@ int gcsl_disc_skeleton(const uint8_t *data, int64_t ld, int64_t n, int32_t p, co
     // codes in range once per solve; the test kernels skip the per-sample checks then
     if (host::launch_disc_validate(data, ld, n, p, dims, w.st, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
     if (host::launch_disc_tests(A, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
-    int last_enqueued = 0;
-    int rc = run_levels(max_level, w.st, s, [&](int level) -> cudaError_t {
+    HostCtl *hc = host_ctl();
+    if (!hc) return GCSL_ERR_DEVICE;
+    int rc = run_levels(max_level, w.st, s, hc->words, [&](int level) -> cudaError_t {
         cudaError_t e2 = host::launch_compact(G, p, w.adj, nullptr, w.st, level, nullptr, s);
         if (e2 == cudaSuccess) e2 = host::launch_disc_weights(w.adj, p, level, w.weights, w.st, s);
         if (e2 == cudaSuccess) e2 = host::launch_scan_ll(w.weights, p, w.prefix, w.st, s);

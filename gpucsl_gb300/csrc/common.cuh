@@ -24,6 +24,13 @@ void note_launch(int kernels);
 // Records the first failing CUDA call of the calling thread's current entry point (kept
 // for gcsl_last_error) and returns e.
 cudaError_t note_error(const char *where, cudaError_t e);
+// The Gaussian skeleton solve behind gcsl_gauss_skeleton (capi.cu).  With
+// allocation_free set it creates nothing: no side stream, no event, no pinned host
+// word; all its work goes on `stream` and the level loop's control words are read
+// into the calling thread's stack.
+int gauss_skeleton_run(const double *C, int p, long long n_obs, const double *thresholds, int n_thresholds,
+                       int max_level, uint16_t *G, int *sepsets, int *rec_pool, long long rec_cap, double *pmax,
+                       gcsl_stats *stats, void *workspace, size_t workspace_bytes, void *stream, bool allocation_free);
 }  // namespace host
 
 // Level-0 decision bounds on the bit pattern of |r| (non-negative doubles order like

@@ -8,17 +8,23 @@
 // compacted adjacency, edge prefix, per-pair z*) lives in the file-scope device array
 // below instead of a caller-provided workspace.
 //
-// * The array holds GCSL_NOALLOC_SCRATCH_BYTES; problems with p > GCSL_NOALLOC_MAX_P
-//   are rejected with GCSL_ERR_UNSUPPORTED before any device work.
+// * The array holds GCSL_NOALLOC_SCRATCH_BYTES; p < 1 is an invalid argument, and
+//   problems with p > GCSL_NOALLOC_MAX_P are rejected with GCSL_ERR_UNSUPPORTED before
+//   any device work.
 // * Every GPU that loads this library holds the array until the process exits.
 // * The array's device address is looked up once per device, on the first call made
 //   with that device current (cudaGetSymbolAddress); make that first call before any
-//   stream capture begins.
+//   stream capture begins.  The cached address belongs to the device's context as it
+//   was at that first call: a cudaDeviceReset after it is not supported.
 // * All calls share the one array and it keeps the last call's contents: the solve
 //   clears its state block at the start and overwrites every other scratch word before
 //   reading it.  Calls whose device work overlaps (different streams, no ordering)
 //   race on the array; serialise them.
-// * No cudaMalloc, cudaFree or allocating library routine is called.
+// * Nothing is allocated or created, on the first call of a thread or any other: no
+//   cudaMalloc, cudaFree, cudaMallocHost or allocating library routine, no stream and no
+//   event.  Every kernel of the solve goes on the caller's stream in order, and the
+//   level loop's control words are read into the calling thread's stack by synchronous
+//   copies (the call synchronises the stream, as gcsl_gauss_skeleton does).
 #include <mutex>
 
 #include "common.cuh"
@@ -50,11 +56,13 @@ extern "C" int gcsl_gauss_skeleton_noalloc(const double *C, int32_t p, int64_t n
                                            int32_t n_thresholds, int32_t max_level, uint16_t *G, int32_t *sepsets,
                                            int32_t *rec_pool, int64_t rec_cap, double *pmax, gcsl_stats *stats,
                                            void *stream) {
-    if (p < 1 || p > GCSL_NOALLOC_MAX_P) return GCSL_ERR_UNSUPPORTED;
+    if (p < 1) return GCSL_ERR_INVALID_ARG;
+    if (p > GCSL_NOALLOC_MAX_P) return GCSL_ERR_UNSUPPORTED;
     if (gcsl_gauss_workspace_bytes(p, max_level) > sizeof(g_gauss_noalloc_scratch)) return GCSL_ERR_UNSUPPORTED;
     void *scratch = nullptr;
     const int rc = noalloc_scratch(&scratch);
     if (rc != GCSL_OK) return rc;
-    return gcsl_gauss_skeleton(C, p, n_obs, thresholds, n_thresholds, max_level, G, sepsets, rec_pool, rec_cap, pmax,
-                               stats, scratch, sizeof(g_gauss_noalloc_scratch), stream);
+    return gcsl::host::gauss_skeleton_run(C, p, n_obs, thresholds, n_thresholds, max_level, G, sepsets, rec_pool,
+                                          rec_cap, pmax, stats, scratch, sizeof(g_gauss_noalloc_scratch), stream,
+                                          true);
 }

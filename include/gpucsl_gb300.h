@@ -119,9 +119,13 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
  * all device memory after start-up.  Same arguments and results as gcsl_gauss_skeleton
  * minus the workspace: the scratch space is a static device array of
  * GCSL_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until exit.
- * p > GCSL_NOALLOC_MAX_P returns GCSL_ERR_UNSUPPORTED.  The first call on a device looks
- * up the array's address (make it before any stream capture); calls share the array,
- * so calls whose device work overlaps race and must be serialised. */
+ * p < 1 returns GCSL_ERR_INVALID_ARG, p > GCSL_NOALLOC_MAX_P GCSL_ERR_UNSUPPORTED.  The
+ * first call on a device looks up the array's address (make it before any stream
+ * capture; a cudaDeviceReset after it is not supported).  The call creates nothing, on
+ * a thread's first call or later: no device or pinned host allocation, no stream, no
+ * event.  All its kernels run in order on `stream`, and it synchronises `stream` to
+ * read the level loop's control words into the calling thread's stack.  Calls share
+ * the array, so calls whose device work overlaps race and must be serialised. */
 #define GCSL_NOALLOC_MAX_P 512
 #define GCSL_NOALLOC_SCRATCH_BYTES 16526336
 int gcsl_gauss_skeleton_noalloc(const double *C, int32_t p, int64_t n_obs, const double *thresholds,

@@ -36,7 +36,10 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_ROOT = Path(os.environ.get("GPUCSL_REFERENCE_ROOT", "/root/reference"))
+# The reference checkout: $GPUCSL_REFERENCE_ROOT, else a directory named `reference`
+# beside this repository's checkout.  Where neither exists the reference builds are
+# skipped (the GPU test box has no checkout; it uses the committed golden fixtures).
+REF_ROOT = Path(os.environ.get("GPUCSL_REFERENCE_ROOT") or HERE.parent.parent / "reference")
 REF_HELPERS = REF_ROOT / "gpucsl" / "pc" / "cuda" / "helpers"
 
 ORACLE_SO = HERE / "liboracle.so"

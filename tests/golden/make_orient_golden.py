@@ -4,7 +4,7 @@ orientation_rules.py, loaded by file path from the reference checkout so that th
 package's GPU imports are not triggered).  Run in a container that has the reference
 and networkx:
 
-    python tests/golden/make_orient_golden.py [/path/to/reference]
+    python tests/golden/make_orient_golden.py <reference checkout>
 
 Cases: random Erdos-Renyi skeletons (p 6..28) with random separating sets, including
 conflicting v-structures, and sepsets drawn so that some unshielded triples collide."""
@@ -49,7 +49,9 @@ def make_case(rng, p, dens, L, keep_common):
 def main():
     import networkx as nx
 
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit("usage: python tests/golden/make_orient_golden.py <reference checkout>")
+    ref = Path(sys.argv[1])
     vs = load(ref, "v_structures")
     rules = load(ref, "orientation_rules")
     rng = np.random.default_rng(2024)

@@ -92,3 +92,32 @@ def test_records_to_dense():
     assert out[0, 3].tolist() == [2, -1] and out[3, 0].tolist() == [2, -1]
     assert (out[2, 3] == -1).all()
     assert int((out >= 0).sum()) == 6
+
+
+def _dense_by_loop(rec, n_ints, p, max_level):
+    out = np.full((p, p, max_level), -1, np.int32)
+    k = 0
+    while k < n_ints:
+        lo, hi, lev = int(rec[k]), int(rec[k + 1]), int(rec[k + 2])
+        if lev <= max_level:
+            out[lo, hi, :lev] = rec[k + 3:k + 3 + lev]
+            out[hi, lo, :lev] = rec[k + 3:k + 3 + lev]
+        k += 3 + lev
+    return out
+
+
+def test_records_to_dense_matches_a_record_by_record_walk():
+    """The vectorised scatter (record offsets by pointer doubling) equals a walk over the
+    records one by one, on random pools of mixed levels, some above max_level."""
+    rng = np.random.default_rng(5)
+    for trial in range(20):
+        p, L = int(rng.integers(2, 60)), int(rng.integers(1, 6))
+        recs = []
+        pairs = [(a, b) for a in range(p) for b in range(a + 1, p)]
+        for k in rng.permutation(len(pairs))[:int(rng.integers(0, 300))]:  # one record per pair
+            lev = int(rng.integers(1, L + 3))
+            lo, hi = pairs[k]
+            recs += [lo, hi, lev] + rng.integers(0, p, lev).tolist()
+        rec = np.array(recs + [7, 7, 7], np.int32)  # trailing words past n_ints are ignored
+        n = len(recs)
+        assert np.array_equal(engine.records_to_dense(rec, n, p, L), _dense_by_loop(rec, n, p, L)), trial

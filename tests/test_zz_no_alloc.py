@@ -2,11 +2,14 @@
 
 It exists for callers that cannot call cudaMalloc (for example a host runtime whose
 allocator owns all device memory after start-up); its scratch space is a static device
-array inside the library.  This test calls it through the C ABI twice in a row (so the
-second call runs on the scratch contents the first one left) on two different problems,
-and compares every output with the workspace entry point gcsl_gauss_skeleton: skeleton
-and sepset records bit-exact, pmax within the 1e-9 relative tolerance of the parity
-tests.  The file is named to be collected last."""
+array inside the library, and the call creates no stream, event or pinned host buffer.
+This test calls it through the C ABI twice in a row (so the second call runs on the
+scratch contents the first one left) on two different problems, and on the largest
+supported problem (p = 512, the end of the array), and compares every output with the
+workspace entry point gcsl_gauss_skeleton: skeleton and sepset records bit-exact, pmax
+within the 1e-9 relative tolerance of the parity tests.  A first call from a new host
+thread must leave the device's free memory unchanged.  The file is named to be
+collected last."""
 import ctypes as ct
 
 import numpy as np
@@ -26,7 +29,7 @@ def _solve(torch, C_np, n, alpha, max_level, noalloc: bool):
     C = torch.from_numpy(np.ascontiguousarray(C_np)).cuda()
     G = torch.empty((p, p), dtype=torch.int16, device="cuda")
     pmax = torch.empty((p, p), dtype=torch.float64, device="cuda")
-    rec = torch.empty(p * 64, dtype=torch.int32, device="cuda")
+    rec = torch.empty(p * 256, dtype=torch.int32, device="cuda")
     thr_list = og.thresholds(n, alpha)
     thr = (ct.c_double * len(thr_list))(*thr_list)
     st = _lib.GcslStats()
@@ -71,6 +74,58 @@ def test_noalloc_matches_workspace_entry_point_twice(cuda):
     _compare(_solve(torch, C, 4000, 0.01, 8, noalloc=True), _solve(torch, C, 4000, 0.01, 8, noalloc=False))
 
 
+def test_noalloc_at_its_largest_size(cuda):
+    """p = GCSL_NOALLOC_MAX_P uses the scratch array up to its end."""
+    torch = cuda
+    w = gaussian_dag_data(512, 3000, 3, 43)
+    C = og.corrcoef(w.data)
+    for _ in range(2):
+        _compare(_solve(torch, C, 3000, 0.01, 6, noalloc=True), _solve(torch, C, 3000, 0.01, 6, noalloc=False))
+
+
+def test_noalloc_first_call_from_a_new_thread_allocates_nothing(cuda):
+    """The per-thread resources of the workspace entry point (side stream, events, pinned
+    control words) are not used here: a first call from a fresh host thread changes the
+    device's free memory by nothing."""
+    import threading
+
+    from gpucsl_gb300 import _lib
+
+    torch = cuda
+    L = _lib.lib()
+    w = gaussian_dag_data(200, 2000, 3, 44)
+    p, n = 200, 2000
+    C = torch.from_numpy(og.corrcoef(w.data)).cuda()
+    G = torch.empty((p, p), dtype=torch.int16, device="cuda")
+    pmax = torch.empty((p, p), dtype=torch.float64, device="cuda")
+    rec = torch.empty(p * 256, dtype=torch.int32, device="cuda")
+    thr_list = og.thresholds(n, 0.01)
+    thr = (ct.c_double * len(thr_list))(*thr_list)
+
+    def call(out):
+        st = _lib.GcslStats()
+        out["rc"] = L.gcsl_gauss_skeleton_noalloc(C.data_ptr(), p, n, thr, len(thr_list), 6, G.data_ptr(), None,
+                                                  rec.data_ptr(), rec.numel(), pmax.data_ptr(), ct.byref(st), None)
+
+    warm = {}
+    call(warm)  # module loading and the symbol lookup happen on this first call
+    torch.cuda.synchronize()
+    assert warm["rc"] == 0
+    free0, _ = torch.cuda.mem_get_info()
+    res = {}
+
+    def thread_body():
+        call(res)
+        res["sync"] = int(torch.cuda.synchronize() is None)
+
+    t = threading.Thread(target=thread_body)
+    t.start()
+    t.join()
+    free1, _ = torch.cuda.mem_get_info()
+    assert res["rc"] == 0 and res["sync"] == 1
+    assert free1 == free0, (free0, free1)
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch(cuda):
     torch = cuda
     from gpucsl_gb300 import _lib
@@ -84,3 +139,6 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(cuda):
     rc = L.gcsl_gauss_skeleton_noalloc(C.data_ptr(), p, 1000, thr, 50, 2, G.data_ptr(), None, None, 0,
                                        pmax.data_ptr(), None, _lib.stream_ptr())
     assert rc == _lib.GCSL_ERR_UNSUPPORTED
+    rc = L.gcsl_gauss_skeleton_noalloc(C.data_ptr(), 0, 1000, thr, 50, 2, G.data_ptr(), None, None, 0,
+                                       pmax.data_ptr(), None, _lib.stream_ptr())
+    assert rc == _lib.GCSL_ERR_INVALID_ARG
