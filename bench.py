@@ -392,11 +392,13 @@ def batched_leg(reps: int = 10) -> dict:
         for _ in range(2):
             b.graph.replay()
         ts = timed(b.graph.replay, reps)
-        L = engine._lib.lib()
-        t_corr = timed(lambda: engine._lib.check(L.gcsl_corr_tc_batch_run(ct.byref(b.corr_plan), engine._lib.stream_ptr()),
-                                                 "corr batch"), 3)
-        t_lv = timed(lambda: engine._lib.check(L.gcsl_gauss_batch_run(ct.byref(b.plan), engine._lib.stream_ptr()),
-                                               "gauss batch"), 3)
+        # the stages on their own: the correlation (split: five-digit product with its
+        # bound), then the level loop (split: first pass, exact correlation of the flagged
+        # instances, their re-solve), each after the one before it
+        t_corr, t_lv = [], []
+        for _ in range(3):
+            t_corr += timed(b.enqueue_correlation, 1)
+            t_lv += timed(b.enqueue_levels, 1)
         res = b.collect()
         tests = sum(r.tests for r in res)
         results[prec] = [b.to_host(k) for k in range(BATCH_COUNT)]
@@ -407,6 +409,12 @@ def batched_leg(reps: int = 10) -> dict:
                      "corr_ms": round(1e3 * statistics.median(t_corr), 3),
                      "levels_ms": round(1e3 * statistics.median(t_lv), 3),
                      "status_nonzero": sum(1 for r in res if r.status != 0)}
+        if prec == "split":
+            eps = b._cerr.cpu().numpy()
+            out[prec]["correlation"] = "five of seven integer digits (15 of 28 digit-pair products) on tcgen05"
+            out[prec]["c_err_max"] = float(eps.max())
+            out[prec]["c_err_median"] = float(np.median(eps))
+            out[prec]["exact_reruns"] = sum(r.exact_rerun for r in res)
         del b
         torch.cuda.empty_cache()
     # decisions and pmax of split against FP64

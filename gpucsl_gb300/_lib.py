@@ -39,6 +39,8 @@ EXPORTED = [
     "gcsl_gauss_batch_workspace_bytes", "gcsl_gauss_batch_prepare", "gcsl_gauss_batch_run",
     "gcsl_gauss_batch_collect", "gcsl_gauss_batch_set_lanes",
     "gcsl_corr_tc_batch_workspace_bytes", "gcsl_corr_tc_batch_prepare", "gcsl_corr_tc_batch_run",
+    "gcsl_corr_tc_batch_run_split", "gcsl_corr_tc_batch_run_flagged", "gcsl_gauss_batch_rerun",
+    "gcsl_gauss_batch_flags",
     "gcsl_orient_workspace_bytes", "gcsl_orient_edges", "gcsl_encode_workspace_bytes", "gcsl_ordinal_encode",
     "gcsl_set_test_precision",
 ]
@@ -91,11 +93,13 @@ class GaussInstance(ct.Structure):
         ("pmax", ct.c_void_p),
         ("rec_pool", ct.c_void_p),
         ("rec_cap", ct.c_int64),
+        ("c_err", ct.c_void_p),
         ("status", ct.c_int32),
         ("levels_run", ct.c_int32),
         ("n_records", ct.c_int64),
         ("tests", ct.c_int64),
         ("retests", ct.c_int64),
+        ("exact_rerun", ct.c_int32),
     ]
 
 
@@ -191,6 +195,14 @@ def lib() -> ct.CDLL:
                                              ct.POINTER(BatchPlan), _vp]
     L.gcsl_corr_tc_batch_run.restype = ct.c_int
     L.gcsl_corr_tc_batch_run.argtypes = [ct.POINTER(BatchPlan), _vp]
+    L.gcsl_corr_tc_batch_run_split.restype = ct.c_int
+    L.gcsl_corr_tc_batch_run_split.argtypes = [ct.POINTER(BatchPlan), _vp, _vp]
+    L.gcsl_corr_tc_batch_run_flagged.restype = ct.c_int
+    L.gcsl_corr_tc_batch_run_flagged.argtypes = [ct.POINTER(BatchPlan), _vp, _vp]
+    L.gcsl_gauss_batch_rerun.restype = ct.c_int
+    L.gcsl_gauss_batch_rerun.argtypes = [ct.POINTER(BatchPlan), _vp]
+    L.gcsl_gauss_batch_flags.restype = _vp
+    L.gcsl_gauss_batch_flags.argtypes = [ct.POINTER(BatchPlan)]
     L.gcsl_set_test_precision.restype = ct.c_int
     L.gcsl_set_test_precision.argtypes = [_i32]
     L.gcsl_encode_workspace_bytes.restype = _sz
@@ -201,7 +213,7 @@ def lib() -> ct.CDLL:
     L.gcsl_orient_workspace_bytes.argtypes = [_i32]
     L.gcsl_orient_edges.restype = ct.c_int
     L.gcsl_orient_edges.argtypes = [_vp, _i32, _vp, _i32, _vp, ct.POINTER(_i32), _vp, _sz, _vp]
-    if L.gcsl_version() != 1:
+    if L.gcsl_version() != 2:
         raise RuntimeError("libgpucsl_gb300.so ABI version mismatch")
     return L
 

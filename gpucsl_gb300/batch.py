@@ -8,8 +8,13 @@ that later solves replay.  The per-level lane-group width of the test kernel is 
 on the first solves (`autotune`).
 
 Precision "f64" gives, per instance, exactly the results of the single-problem path;
-"split" tests in FP32 with an FP64 re-test inside the guard band (skeleton and
-sepsets identical to "f64", pmax within the FP32 error of z*).
+"split" computes the correlation over five of the seven integer digits (15 of the 28
+digit-pair products, with a bound eps on its distance to the seven-digit result), tests
+in FP32 with an FP64 re-test inside the guard band, both carrying error bounds that
+include eps, and solves again with the exact correlation the few instances whose tests
+could not be decided on the split one: skeleton and sepsets identical to "f64", pmax
+within the FP32 error of z*.  After a split run, C of an instance holds the split
+correlation unless that instance was solved again (`InstanceResult.exact_rerun`).
 """
 from __future__ import annotations
 
@@ -29,6 +34,7 @@ class InstanceResult:
     n_records: int
     tests: int
     retests: int
+    exact_rerun: int = 0
 
 
 class GaussianBatch:
@@ -55,12 +61,15 @@ class GaussianBatch:
         self.split = precision == "split"
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         L = _lib.lib()
+        self.corr_plan = None
+        self.corr_ws = None
         # outputs and inputs of every instance live in a few flat buffers (views per instance)
         pp = [p * p for p in self.ps]
         off = np.concatenate([[0], np.cumsum(pp)]).astype(np.int64)
         tot = int(off[-1])
         self._C = torch.empty(tot, dtype=torch.float64, device=self.device)
         self._C32 = torch.empty(tot, dtype=torch.float32, device=self.device) if self.split else None
+        self._cerr = torch.zeros(self.count, dtype=torch.float64, device=self.device) if self.split else None
         self._G = torch.empty(tot, dtype=torch.int16, device=self.device)
         self._pmax = torch.empty(tot, dtype=torch.float64, device=self.device)
         self.C = [self._C[off[k]:off[k + 1]].view(p, p) for k, p in enumerate(self.ps)]
@@ -80,8 +89,6 @@ class GaussianBatch:
             raise ValueError("unsupported instance sizes")
         self.workspace = torch.empty(ws, dtype=torch.uint8, device=self.device)
         self.plan = _lib.BatchPlan()
-        self.corr_plan = None
-        self.corr_ws = None
         self.graph = None
         self.lanes = {l: 32 for l in range(1, self.max_level + 1)}
         self._prepare()
@@ -111,6 +118,9 @@ class GaussianBatch:
             I.pmax = self.pmax[k].data_ptr()
             I.rec_pool = self.rec[k].data_ptr()
             I.rec_cap = self.rec_caps[k]
+            # the split correlation's bound (set only while samples are bound: given
+            # correlations are taken as exact)
+            I.c_err = (self._cerr.data_ptr() + 8 * k) if (self.split and self.corr_plan is not None) else None
         return arr
 
     def _prepare(self):
@@ -153,6 +163,8 @@ class GaussianBatch:
                                                 n, p, ld, Cp, C32p, self.count, self.corr_ws.data_ptr(),
                                                 self.corr_ws.numel(), ct.byref(self.corr_plan), _lib.stream_ptr()),
                    "gcsl_corr_tc_batch_prepare")
+        if self.split:
+            self._prepare()  # the instances now carry the split correlation's bound
         self.graph = None
 
     def set_correlations(self, Cs):
@@ -163,17 +175,41 @@ class GaussianBatch:
             self.C[k].copy_(C)
             if self.split:
                 self.C32[k].copy_(C.to(self.C32[k].dtype))
+        had_samples = self.corr_plan is not None
         self.corr_plan = None
+        if self.split and had_samples:
+            self._prepare()  # given correlations are exact: no bound
         self.graph = None
 
     # ------------------------------------------------------------- runs
-    def enqueue(self):
-        """Enqueue correlation (when samples are bound) and the level loop, no sync."""
+    def enqueue_correlation(self):
+        """The correlation stage alone (split: the five-digit product with its bound)."""
         L = _lib.lib()
         s = _lib.stream_ptr()
-        if self.corr_plan is not None:
+        if self.corr_plan is None:
+            return
+        if self.split:
+            _lib.check(L.gcsl_corr_tc_batch_run_split(ct.byref(self.corr_plan), self._cerr.data_ptr(), s),
+                       "gcsl_corr_tc_batch_run_split")
+        else:
             _lib.check(L.gcsl_corr_tc_batch_run(ct.byref(self.corr_plan), s), "gcsl_corr_tc_batch_run")
+
+    def enqueue_levels(self):
+        """The level loop alone (split with samples: first pass, the exact correlation of
+        the flagged instances, their exact re-solve)."""
+        L = _lib.lib()
+        s = _lib.stream_ptr()
         _lib.check(L.gcsl_gauss_batch_run(ct.byref(self.plan), s), "gcsl_gauss_batch_run")
+        if self.split and self.corr_plan is not None:
+            flags = L.gcsl_gauss_batch_flags(ct.byref(self.plan))
+            _lib.check(L.gcsl_corr_tc_batch_run_flagged(ct.byref(self.corr_plan), flags, s),
+                       "gcsl_corr_tc_batch_run_flagged")
+            _lib.check(L.gcsl_gauss_batch_rerun(ct.byref(self.plan), s), "gcsl_gauss_batch_rerun")
+
+    def enqueue(self):
+        """Enqueue correlation (when samples are bound) and the level loop, no sync."""
+        self.enqueue_correlation()
+        self.enqueue_levels()
 
     def capture(self):
         """Capture `enqueue` into a CUDA graph replayed by `run(graph=True)`."""
@@ -217,8 +253,8 @@ class GaussianBatch:
     def collect(self) -> list[InstanceResult]:
         L = _lib.lib()
         rc = L.gcsl_gauss_batch_collect(ct.byref(self.plan), self._inst, self.count, _lib.stream_ptr())
-        res = [InstanceResult(int(I.status), int(I.levels_run), int(I.n_records), int(I.tests), int(I.retests))
-               for I in self._inst]
+        res = [InstanceResult(int(I.status), int(I.levels_run), int(I.n_records), int(I.tests), int(I.retests),
+                              int(I.exact_rerun)) for I in self._inst]
         if rc not in (_lib.GCSL_OK, _lib.GCSL_ERR_CAPACITY):
             _lib.check(rc, "gcsl_gauss_batch_collect")
         return res

@@ -81,7 +81,10 @@ size_t gauss_batch_workspace_bytes(const int *p, int count);
 int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level, int precision, void *ws,
                         size_t ws_bytes, long long *plan, int sms, cudaStream_t s);
 int gauss_batch_set_lanes(long long *plan, int level, int lanes);
-int gauss_batch_run(const long long *plan, cudaStream_t s);
+int gauss_batch_run(const long long *plan, cudaStream_t s, bool rerun);
+const int *gauss_batch_flags(const long long *plan);
+cudaError_t corr_tc_batch_run_mode(void *ws, int count, const long long *stage_totals, int dtype, int mode,
+                                   double *c_err, const int *active, cudaStream_t s);
 int gauss_batch_collect(const long long *plan, gcsl_gauss_instance *out, int count, cudaStream_t s);
 cudaError_t launch_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, float *D, int M, int N, int K, int *err,
                                 cudaStream_t s);
@@ -693,7 +696,19 @@ int gcsl_gauss_batch_prepare(const gcsl_gauss_instance *inst, int32_t count, int
 
 int gcsl_gauss_batch_run(const gcsl_batch_plan *plan, void *stream) {
     if (!plan) return GCSL_ERR_INVALID_ARG;
-    return host::gauss_batch_run(reinterpret_cast<const long long *>(plan->w), static_cast<cudaStream_t>(stream));
+    return host::gauss_batch_run(reinterpret_cast<const long long *>(plan->w), static_cast<cudaStream_t>(stream),
+                                 false);
+}
+
+int gcsl_gauss_batch_rerun(const gcsl_batch_plan *plan, void *stream) {
+    if (!plan) return GCSL_ERR_INVALID_ARG;
+    return host::gauss_batch_run(reinterpret_cast<const long long *>(plan->w), static_cast<cudaStream_t>(stream),
+                                 true);
+}
+
+const int32_t *gcsl_gauss_batch_flags(const gcsl_batch_plan *plan) {
+    if (!plan) return nullptr;
+    return host::gauss_batch_flags(reinterpret_cast<const long long *>(plan->w));
 }
 
 int gcsl_gauss_batch_collect(const gcsl_batch_plan *plan, gcsl_gauss_instance *inst, int32_t count, void *stream) {
@@ -756,6 +771,24 @@ int gcsl_corr_tc_batch_run(const gcsl_batch_plan *plan, void *stream) {
     if (w[0] != kCorrPlanMagic) return GCSL_ERR_INVALID_ARG;
     return map_cuda(host::corr_tc_batch_run(reinterpret_cast<void *>(static_cast<uintptr_t>(w[1])), (int)w[2], w + 4,
                                             (int)w[3], static_cast<cudaStream_t>(stream)));
+}
+
+int gcsl_corr_tc_batch_run_split(const gcsl_batch_plan *plan, double *c_err, void *stream) {
+    if (!plan || !c_err) return GCSL_ERR_INVALID_ARG;
+    const long long *w = reinterpret_cast<const long long *>(plan->w);
+    if (w[0] != kCorrPlanMagic) return GCSL_ERR_INVALID_ARG;
+    return map_cuda(host::corr_tc_batch_run_mode(reinterpret_cast<void *>(static_cast<uintptr_t>(w[1])), (int)w[2],
+                                                 w + 4, (int)w[3], host::CORR_BATCH_SPLIT, c_err, nullptr,
+                                                 static_cast<cudaStream_t>(stream)));
+}
+
+int gcsl_corr_tc_batch_run_flagged(const gcsl_batch_plan *plan, const int32_t *flags, void *stream) {
+    if (!plan || !flags) return GCSL_ERR_INVALID_ARG;
+    const long long *w = reinterpret_cast<const long long *>(plan->w);
+    if (w[0] != kCorrPlanMagic) return GCSL_ERR_INVALID_ARG;
+    return map_cuda(host::corr_tc_batch_run_mode(reinterpret_cast<void *>(static_cast<uintptr_t>(w[1])), (int)w[2],
+                                                 w + 4, (int)w[3], host::CORR_BATCH_FLAGGED, nullptr, flags,
+                                                 static_cast<cudaStream_t>(stream)));
 }
 
 

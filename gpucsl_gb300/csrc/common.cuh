@@ -24,6 +24,10 @@ void note_launch(int kernels);
 // Records the first failing CUDA call of the calling thread's current entry point (kept
 // for gcsl_last_error) and returns e.
 cudaError_t note_error(const char *where, cudaError_t e);
+// Modes of a batched correlation run (corr_tc.cu): every job with seven digits; every job
+// with five digits and an error bound; only flagged jobs, seven digits, on the digits of
+// a previous run.
+enum CorrBatchMode { CORR_BATCH_EXACT = 0, CORR_BATCH_SPLIT = 1, CORR_BATCH_FLAGGED = 2 };
 // The Gaussian skeleton solve behind gcsl_gauss_skeleton (capi.cu).  With
 // allocation_free set it creates nothing: no side stream, no event, no pinned host
 // word; all its work goes on `stream` and the level loop's control words are read

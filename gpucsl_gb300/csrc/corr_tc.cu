@@ -19,8 +19,16 @@
 //
 // Dropped pairs (k + l > 6) weigh at most 2^-48 of sum |x_i||x_j|, the same order as
 // the rounding of an FP64 GEMM.  Tile: 128 rows (i) x 64 columns (j), 7 accumulators
-// = 448 TMEM columns, K staged 32 samples at a time into two shared-memory buffers
-// (84 KB each) while the tensor core consumes the other.
+// = 448 TMEM columns, K staged 16 samples at a time into a ring of shared-memory stages
+// while the tensor core consumes the others.
+//
+// Split precision (batches): the same product over the five leading digits only, pairs
+// k + l <= 4 (15 of the 28 pair products, 5 accumulators), gives C' with
+//   |C' - C| <= eps = 2.5 * 2^-35 * (1.02 w + sqrt(w)),  w = n / min_i sum_t y_ti^2,
+// where C is the seven-digit result (derivation at split_eps below); the diagonal
+// kernel writes eps per instance.  Instances whose tests cannot be decided exactly with
+// C' are flagged by the level loop and get the seven-digit product afterwards (the
+// digit planes hold all seven digits either way).
 #include <type_traits>
 #include <vector>
 
@@ -29,16 +37,17 @@
 
 namespace gcsl {
 
-constexpr int OZ_S = 7;                 // digits per value
-constexpr int OZ_G = 7;                 // accumulator groups g = k + l <= 6
+constexpr int OZ_S = 7;                 // digits per value (all written by the digit split)
+constexpr int OZ_S_SPLIT = 5;           // digits of the split-precision product
 constexpr int OZ_TM = 128, OZ_TN = 64;  // output tile
 constexpr int OZ_KS = 32;               // sample padding granule
 constexpr int OZ_CHUNK_STEPS = 28;      // 448 samples (28 MMA K steps) between exact drains
 constexpr int OZ_NST = 4;               // shared-memory stages (one K step each)
 constexpr uint32_t OZ_TMEM_COLS = 512;
-constexpr int OZ_A_BYTES = OZ_S * OZ_TM * 16 * 2;  // 28672: 7 digits x 128 rows x 16 samples
-constexpr int OZ_B_BYTES = OZ_S * OZ_TN * 16 * 2;  // 14336: 7 digits x 64 rows x 16 samples
-constexpr int OZ_STAGE_BYTES = OZ_A_BYTES + OZ_B_BYTES;
+// shared-memory bytes of one K step for NS digits: NS x (128 A rows + 64 B rows) x 16
+// samples x 2 bytes (NS = 7: 28672 + 14336)
+constexpr int oz_a_bytes(int ns) { return ns * OZ_TM * 16 * 2; }
+constexpr int oz_stage_bytes(int ns) { return ns * (OZ_TM + OZ_TN) * 16 * 2; }
 constexpr unsigned long long OZ_WAIT_NS = 2000000000ull;
 
 struct OzDims {
@@ -58,6 +67,7 @@ struct OzJob {
     long long *phi, *plo;
     double *C;
     float *C32;  // optional FP32 copy of C
+    int index;   // position in its batch (0 for a single job)
 };
 
 // Kernel stages of a job; each has its own count of blocks per job.
@@ -66,21 +76,34 @@ enum OzStage { OZ_INIT = 0, OZ_STATS, OZ_MEAN, OZ_DIGITS, OZ_PRODUCT, OZ_DIAG, O
 // Where a kernel finds its job: one job passed by value (block b of the stage is block b
 // of the job), or a device table of jobs with each stage's exclusive block offsets
 // (block b belongs to the job k with off[k] <= b < off[k + 1]).
+//
+// A batch run may also carry, per job index: c_err, where the split-precision diagonal
+// kernel writes the bound eps of the job's C (null: exact product, no bound), and
+// active, the jobs to compute (null: all; a job whose flag is 0 is skipped by the
+// product, diagonal and finish kernels).
 struct OneJob {
     OzJob job;
     __device__ __forceinline__ OzJob get(long long b, long long &lb) const {
         lb = b;
         return job;
     }
+    __device__ __forceinline__ bool skip(int) const { return false; }
+    __device__ __forceinline__ double *err_slot(int) const { return nullptr; }
 };
 struct JobTable {
     const OzJob *jobs;
     const long long *off;
     int count;
+    double *c_err = nullptr;
+    const int *active = nullptr;
     __device__ __forceinline__ OzJob get(long long b, long long &lb) const {
         const int k = upper_row(off, count, b);
         lb = b - off[k];
         return jobs[k];
+    }
+    __device__ __forceinline__ bool skip(int index) const { return active != nullptr && active[index] == 0; }
+    __device__ __forceinline__ double *err_slot(int index) const {
+        return c_err != nullptr ? c_err + index : nullptr;
     }
 };
 
@@ -107,7 +130,11 @@ __global__ void colstats_init_kernel(Src src) {
     if (j < J.p) {
         J.kmin[j] = 0x7fffffffffffffffll;
         J.kmax[j] = (long long)0x8000000000000000ull;
-        if (j == 0) *J.err = 0;
+        if (j == 0) {
+            *J.err = 0;
+            double *slot = src.err_slot(J.index);
+            if (slot != nullptr) *slot = 0.0;
+        }
     }
 }
 
@@ -335,7 +362,7 @@ constexpr int OZ_THREADS = (OZ_DRAIN_WARPS + 2) * 32;    // + producer warp + MM
 // copies; warp 17 (lane 0) issues the tensor-core MMAs.  They synchronise only through
 // mbarriers: full (copy landed), empty (MMAs done reading a stage), chunk (MMAs of a
 // chunk done), drained (TMEM read, accumulators may be overwritten).
-template <class Src>
+template <class Src, int NS>
 __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t full_bar[OZ_NST], empty_bar[OZ_NST], chunk_bar, drained_bar;
@@ -354,6 +381,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
         s_lb = lb0;
     }
     __syncthreads();
+    if (src.skip(s_job.index)) return;  // not selected in this run (uniform over the block)
     const long long lb = s_lb;
     const OzDims &D = s_job.D;
     int I, J;
@@ -392,11 +420,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
                     break;
                 }
                 if (*(volatile int *)&s_fail) break;
-                uint8_t *sA = smem + (size_t)b * OZ_STAGE_BYTES;
-                uint8_t *sB = sA + OZ_A_BYTES;
-                mbar_expect_tx(&full_bar[b], (uint32_t)OZ_STAGE_BYTES);
+                uint8_t *sA = smem + (size_t)b * oz_stage_bytes(NS);
+                uint8_t *sB = sA + oz_a_bytes(NS);
+                mbar_expect_tx(&full_bar[b], (uint32_t)oz_stage_bytes(NS));
                 const long long q = q0 + st;
-                for (int k = 0; k < OZ_S; ++k) {
+                for (int k = 0; k < NS; ++k) {
                     bulk_g2s(sA + k * 4096, dig + (((size_t)k * nI + I) * nq + q) * 4096, 4096u, &full_bar[b]);
                     bulk_g2s(sB + k * 2048,
                              dig + (((size_t)k * nI + (J >> 1)) * nq + q) * 4096 + (size_t)(J & 1) * 2048, 2048u,
@@ -422,16 +450,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
                         break;
                     }
                     tc::fence_after_sync();
-                    uint8_t *sA = smem + (size_t)b * OZ_STAGE_BYTES;
-                    uint8_t *sB = sA + OZ_A_BYTES;
-                    // Digit k of A against digits l = 0 .. 6-k of B: the B digits are
+                    uint8_t *sA = smem + (size_t)b * oz_stage_bytes(NS);
+                    uint8_t *sB = sA + oz_a_bytes(NS);
+                    // Digit k of A against digits l = 0 .. NS-1-k of B: the B digits are
                     // consecutive 64-row operands in shared memory and the products land in
                     // consecutive accumulator groups g = k + l (TMEM columns 64 g ..), so up
                     // to four pairs form one MMA with N = 64 x (number of pairs).
 #pragma unroll
-                    for (int k = 0; k < OZ_S; ++k) {
+                    for (int k = 0; k < NS; ++k) {
                         const uint64_t ad = tc::sdesc(tc::smem_u32(sA + k * 4096), 128, 256);
-                        const int pairs = OZ_S - k;
+                        const int pairs = NS - k;
                         const uint32_t acc = (st == c0 && k == 0) ? 0u : 1u;  // k = 0 writes every group first
 #pragma unroll
                         for (int l0 = 0; l0 < pairs; l0 += 4) {
@@ -463,9 +491,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
                 break;
             }
             tc::fence_after_sync();
-            // groups 0..2 -> hi with weights 2^14, 2^7, 1; groups 3..6 -> lo with 2^21, 2^14, 2^7, 1
+            // groups 0..2 -> hi with weights 2^14, 2^7, 1; groups 3..NS-1 -> lo with 2^21, 2^14, 2^7, 1
 #pragma unroll
-            for (int g = 0; g < OZ_G; ++g) {
+            for (int g = 0; g < NS; ++g) {
                 float v[16];
                 tc::tmem_ld16(tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(g * OZ_TN + cq * 16), v);
                 const long long wgt = 1ll << (7 * ((g < 3 ? 2 : 6) - g));
@@ -563,15 +591,49 @@ __device__ __forceinline__ double oz_cov(const long long *__restrict__ part_hi, 
     return scale_pow2(val, expo[i] + expo[j] - 56) * scale;
 }
 
+// Bound of |C' - C| for the five-digit product C' against the seven-digit C, from the
+// column of i (the bound of a job is the maximum over its columns).
+//
+// With I = round(y 2^49) = sum_{k<5} d_k 2^(42-7k) + r (|r| <= 2^13; |d_0| <= 2^7 and
+// |d_k| <= 2^6 after it), the kept pairs k + l <= 4 miss from I_i I_j the pairs
+// k + l >= 5 (at most 1.01 * 2^63) and the terms with r (at most 2^13 (|I_i| + |I_j|)
+// + 3 * 2^26); the seven-digit product itself misses at most 2^50 (pairs k + l >= 7).
+// In units of y (divide by 2^98) a sample contributes at most 1.02 * 2^-35 +
+// 2^-36 (|y_ti| + |y_tj|), and by Cauchy-Schwarz sum_t |y_ti| <= sqrt(n S_i) with
+// S_i = sum_t y_ti^2.  Relative to sqrt(S_i S_j) the covariance error is then at most
+// f(w) = 1.02 * 2^-35 w + 2^-35 sqrt(w) with w = n / min(S_i, S_j), and the
+// normalisation by the (equally perturbed) variances at most doubles it to first
+// order; the factor 2.5 covers that, the higher-order terms and the roundings.
+template <class Src>
+__device__ __forceinline__ double split_eps(const OzJob &J, int i) {
+    long long H = 0, Lo = 0;
+    for (int s = 0; s < J.D.splits; ++s) {
+        const size_t ix = ((size_t)s * J.D.p_pad + i) * J.D.p_pad + i;
+        H += J.phi[ix];
+        Lo += J.plo[ix];
+    }
+    const double S = scale_pow2(exact_sum_to_f64(H, Lo), -56);  // sum_t y_ti^2
+    if (!(S > 0.0)) return __longlong_as_double(0x7ff0000000000000ll);
+    const double w = (double)J.n / S;
+    return 2.5 * 0x1p-35 * (1.02 * w + sqrt(w));
+}
+
 template <class Src>
 __global__ void ozaki_diag_kernel(Src src) {
     pdl_wait();
     pdl_trigger();
     long long lb;
     const OzJob &J = src.get(blockIdx.x, lb);
+    if (src.skip(J.index)) return;
     const int i = (int)lb * blockDim.x + threadIdx.x;
     const double scale = 1.0 / (double)(J.n - 1);
-    if (i < J.p) J.inv_sd[i] = 1.0 / sqrt(oz_cov(J.phi, J.plo, J.D, J.expo, scale, i, i));
+    if (i < J.p) {
+        J.inv_sd[i] = 1.0 / sqrt(oz_cov(J.phi, J.plo, J.D, J.expo, scale, i, i));
+        double *slot = src.err_slot(J.index);
+        if (slot != nullptr)  // non-negative doubles order like their bit patterns
+            atomicMax(reinterpret_cast<unsigned long long *>(slot),
+                      (unsigned long long)__double_as_longlong(split_eps<Src>(J, i)));
+    }
 }
 
 // C_ij = clip(cov_ij / s_i / s_j, -1, 1) (the normalisation of numpy's corrcoef, with
@@ -585,6 +647,7 @@ __global__ void ozaki_finish_kernel(Src src) {
     pdl_trigger();
     long long lb;
     const OzJob &J = src.get(blockIdx.x, lb);
+    if (src.skip(J.index)) return;
     const int p = J.p;
     const int nb = (p + 31) / 32;
     int rem = (int)lb, bi = 0;
@@ -680,6 +743,7 @@ static size_t oz_job(OzJob &J, void *ws, const void *X, long long n, int p, long
     J.plo = J.phi ? J.phi + (size_t)D.splits * D.p_pad * (size_t)D.p_pad : nullptr;
     J.C = nullptr;
     J.C32 = nullptr;
+    J.index = 0;
     return off;
 }
 
@@ -700,12 +764,12 @@ size_t corr_tc_workspace_bytes(long long n, int p, int num_sms) {
     return oz_job(J, nullptr, nullptr, n, p, p, num_sms, 0);
 }
 
-template <class Src>
+template <class Src, int NS>
 static cudaError_t set_ozaki_smem() {
     static std::atomic<bool> done{false};  // per instantiation; the value set is the same for every caller
     if (done.load()) return cudaSuccess;
-    const cudaError_t e = cudaFuncSetAttribute(corr_ozaki_kernel<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               OZ_NST * OZ_STAGE_BYTES);
+    const cudaError_t e = cudaFuncSetAttribute(corr_ozaki_kernel<Src, NS>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_NST * oz_stage_bytes(NS));
     if (e == cudaSuccess) done.store(true);
     return e;
 }
@@ -744,13 +808,13 @@ static cudaError_t launch_digits(const Src &src, const long long *nb, int dtype,
                : launch_stage(digit_split_kernel<float, Src>, nb[OZ_DIGITS], 256, 0, src, s, "digit_split_kernel launch");
 }
 
-template <class Src>
+template <class Src, int NS = OZ_S>
 static cudaError_t launch_product(const Src &src, const long long *nb, cudaStream_t s) {
     note_launch(3);
-    cudaError_t e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<Src>());
+    cudaError_t e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<Src, NS>());
     if (e != cudaSuccess) return e;
-    e = launch_stage(corr_ozaki_kernel<Src>, nb[OZ_PRODUCT], OZ_THREADS, (size_t)OZ_NST * OZ_STAGE_BYTES, src, s,
-                     "corr_ozaki_kernel launch");
+    e = launch_stage(corr_ozaki_kernel<Src, NS>, nb[OZ_PRODUCT], OZ_THREADS, (size_t)OZ_NST * oz_stage_bytes(NS), src,
+                     s, "corr_ozaki_kernel launch");
     if (e != cudaSuccess) return e;
     e = launch_stage(ozaki_diag_kernel<Src>, nb[OZ_DIAG], 256, 0, src, s, "ozaki_diag_kernel launch");
     if (e != cudaSuccess) return e;
@@ -821,6 +885,7 @@ cudaError_t corr_tc_batch_prepare(const void *const *X, const long long *n, cons
         cur += oz_job(J, base + cur, X[k], n[k], p[k], ldx[k], 1, 1);
         J.C = C[k];
         J.C32 = C32 ? C32[k] : nullptr;
+        J.index = k;
         long long nb[OZ_NSTAGES];
         oz_stage_blocks(J, nb);
         for (int st = 0; st < OZ_NSTAGES; ++st)
@@ -835,7 +900,11 @@ cudaError_t corr_tc_batch_prepare(const void *const *X, const long long *n, cons
     return e;
 }
 
-cudaError_t corr_tc_batch_run(void *ws, int count, const long long *stage_totals, int dtype, cudaStream_t s) {
+// Modes of a batch run: every job exactly (seven digits); every job in split precision
+// (five digits, bound per job into c_err); or only the jobs whose flag is set, exactly,
+// reusing the digits of a previous run (product, diagonal and finish only).
+cudaError_t corr_tc_batch_run_mode(void *ws, int count, const long long *stage_totals, int dtype, int mode,
+                                   double *c_err, const int *active, cudaStream_t s) {
     char *base = static_cast<char *>(ws);
     const size_t a = ((size_t)count * sizeof(OzJob) + 255) / 256 * 256;
     const OzJob *jobs = reinterpret_cast<const OzJob *>(base);
@@ -848,27 +917,47 @@ cudaError_t corr_tc_batch_run(void *ws, int count, const long long *stage_totals
     // one JobTable per stage (the offsets differ); the stage launchers take the table of
     // their first kernel, so launch stage by stage
     JobTable t[OZ_NSTAGES];
-    for (int st = 0; st < OZ_NSTAGES; ++st) t[st] = JobTable{jobs, off + (size_t)st * (count + 1), count};
-    note_launch(7);
+    for (int st = 0; st < OZ_NSTAGES; ++st) {
+        t[st] = JobTable{jobs, off + (size_t)st * (count + 1), count};
+        t[st].c_err = mode == CORR_BATCH_SPLIT ? c_err : nullptr;
+        t[st].active = mode == CORR_BATCH_FLAGGED ? active : nullptr;
+    }
     cudaError_t e;
-    colstats_init_kernel<JobTable><<<(unsigned)nb[OZ_INIT], 256, 0, s>>>(t[OZ_INIT]);
-    if ((e = note_error("colstats_init_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
-    if (dtype == GCSL_DTYPE_F64) colstats_kernel<double, JobTable><<<(unsigned)nb[OZ_STATS], 256, 0, s>>>(t[OZ_STATS]);
-    else colstats_kernel<float, JobTable><<<(unsigned)nb[OZ_STATS], 256, 0, s>>>(t[OZ_STATS]);
-    if ((e = note_error("colstats_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
-    col_mean_exp_kernel<JobTable><<<(unsigned)nb[OZ_MEAN], 256, 0, s>>>(t[OZ_MEAN]);
-    if ((e = note_error("col_mean_exp_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
-    if (dtype == GCSL_DTYPE_F64)
-        digit_split_kernel<double, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
-    else digit_split_kernel<float, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
-    if ((e = note_error("digit_split_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
-    if ((e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<JobTable>())) != cudaSuccess) return e;
-    corr_ozaki_kernel<JobTable><<<(unsigned)nb[OZ_PRODUCT], OZ_THREADS, OZ_NST * OZ_STAGE_BYTES, s>>>(t[OZ_PRODUCT]);
+    if (mode != CORR_BATCH_FLAGGED) {
+        note_launch(4);
+        colstats_init_kernel<JobTable><<<(unsigned)nb[OZ_INIT], 256, 0, s>>>(t[OZ_INIT]);
+        if ((e = note_error("colstats_init_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+        if (dtype == GCSL_DTYPE_F64)
+            colstats_kernel<double, JobTable><<<(unsigned)nb[OZ_STATS], 256, 0, s>>>(t[OZ_STATS]);
+        else colstats_kernel<float, JobTable><<<(unsigned)nb[OZ_STATS], 256, 0, s>>>(t[OZ_STATS]);
+        if ((e = note_error("colstats_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+        col_mean_exp_kernel<JobTable><<<(unsigned)nb[OZ_MEAN], 256, 0, s>>>(t[OZ_MEAN]);
+        if ((e = note_error("col_mean_exp_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+        if (dtype == GCSL_DTYPE_F64)
+            digit_split_kernel<double, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
+        else digit_split_kernel<float, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
+        if ((e = note_error("digit_split_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    }
+    note_launch(3);
+    if (mode == CORR_BATCH_SPLIT) {
+        if ((e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<JobTable, OZ_S_SPLIT>())) != cudaSuccess)
+            return e;
+        corr_ozaki_kernel<JobTable, OZ_S_SPLIT>
+            <<<(unsigned)nb[OZ_PRODUCT], OZ_THREADS, OZ_NST * oz_stage_bytes(OZ_S_SPLIT), s>>>(t[OZ_PRODUCT]);
+    } else {
+        if ((e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<JobTable, OZ_S>())) != cudaSuccess) return e;
+        corr_ozaki_kernel<JobTable, OZ_S>
+            <<<(unsigned)nb[OZ_PRODUCT], OZ_THREADS, OZ_NST * oz_stage_bytes(OZ_S), s>>>(t[OZ_PRODUCT]);
+    }
     if ((e = note_error("corr_ozaki_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
     ozaki_diag_kernel<JobTable><<<(unsigned)nb[OZ_DIAG], 256, 0, s>>>(t[OZ_DIAG]);
     if ((e = note_error("ozaki_diag_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
     ozaki_finish_kernel<JobTable><<<(unsigned)nb[OZ_FINISH], 256, 0, s>>>(t[OZ_FINISH]);
     return note_error("ozaki_finish_kernel launch", cudaGetLastError());
+}
+
+cudaError_t corr_tc_batch_run(void *ws, int count, const long long *stage_totals, int dtype, cudaStream_t s) {
+    return corr_tc_batch_run_mode(ws, count, stage_totals, dtype, CORR_BATCH_EXACT, nullptr, nullptr, s);
 }
 
 }  // namespace host

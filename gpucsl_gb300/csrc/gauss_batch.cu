@@ -13,9 +13,18 @@
 // Precision GCSL_PREC_F64 runs the FP64 tests of the single-instance path.  Precision
 // GCSL_PREC_SPLIT first tests in FP32 on an FP32 copy of C and decides there when the
 // FP32 rho^2 is outside the guard band (tanh^2 of the thresholds at 1.1 alpha and
-// 0.9 alpha, i.e. the test's p-value is not within 10 % of alpha) and every pivot of the
-// elimination is at least 1e-3; otherwise the test is repeated in FP64 from C.  The
-// skeleton and sepsets then equal the FP64 ones; z* (and pmax) carry the FP32 error.
+// 0.9 alpha, i.e. the test's p-value is not within 10 % of alpha); otherwise the test is
+// repeated in FP64 from C.  The skeleton and sepsets then equal the FP64 ones; z* (and
+// pmax) carry the FP32 error.
+//
+// When an instance's C comes from the split-precision correlation (c_err: a bound eps on
+// |C - C_exact|), every decision carries a first-order error bound that includes eps:
+// the FP32 test decides outside the band only when its whole interval is, the FP64
+// re-test decides when its interval clears the FP64 path's knife edge, and a test that
+// neither can decide sets the instance's flag (level 0 likewise when |r| lies within
+// eps of tanh(tau_0)).  Flagged instances are solved again (gauss_batch_rerun) after the
+// seven-digit correlation, with the exact C; the others keep their results, which then
+// equal the exact-C results.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -32,6 +41,8 @@ constexpr float SPLIT_MIN_PIVOT = 1e-3f;
 struct BInst {
     const double *C;
     const float *C32;
+    const double *c_err;  // bound on |C - C_exact| (split-precision correlation), or null when C is exact
+    int *flag;            // set when a decision needs the exact C
     uint16_t *G;
     double *pmax;
     int *rec;
@@ -100,6 +111,108 @@ __device__ __forceinline__ bool gauss_test_f32(const float *__restrict__ C32, in
     return minpiv >= SPLIT_MIN_PIVOT && rho2 < 0.99f;  // NaN fails both
 }
 
+// ------------------------------------------------- tests on an approximate C
+// The elimination of gauss_test_f32_at (gauss_dev.cuh) in T = float or double, with a
+// first-order bound of the distance of every entry to its value for the exact C: the
+// inputs start at u|c| + in_err (in_err bounds |C - C_exact| entrywise; the unit
+// diagonal of xi and xj is exact in both), and each reciprocal, product and fma adds u
+// times its result plus the propagated bounds of its operands.
+template <typename T>
+struct BoundArith;
+template <>
+struct BoundArith<float> {
+    static constexpr float u = 5.9604645e-08f;  // 2^-24
+    static __device__ __forceinline__ float fma_(float a, float b, float c) { return fmaf(a, b, c); }
+};
+template <>
+struct BoundArith<double> {
+    static constexpr double u = 1.1102230246251565e-16;  // 2^-53
+    static __device__ __forceinline__ double fma_(double a, double b, double c) { return fma(a, b, c); }
+};
+
+struct C32Acc {
+    const float *__restrict__ C32;
+    int p;
+    __device__ __forceinline__ float operator()(int a, int b) const { return __ldg(C32 + (size_t)a * p + b); }
+};
+struct C64Acc {
+    const double *__restrict__ C;
+    int p;
+    __device__ __forceinline__ double operator()(int a, int b) const { return __ldg(C + (size_t)a * p + b); }
+};
+
+template <typename T>
+__device__ __forceinline__ bool rho2_bound_t(T h00, T e00, T h01, T e01, T h11, T e11, T &rho2, T &err) {
+    const T u = BoundArith<T>::u;
+    const T lo00 = h00 - e00, lo11 = h11 - e11;
+    rho2 = (h01 * h01) / (h00 * h11);
+    const T ah = fabs(h01);
+    err = T(2) * ((T(2) * ah * e01 + e01 * e01) / (lo00 * lo11) + rho2 * (e00 / lo00 + e11 / lo11) +
+                  T(4) * u * rho2);
+    return e00 < T(0.25) * h00 && e11 < T(0.25) * h11 && rho2 + err < T(0.98);  // NaN fails
+}
+
+template <int L, typename T, class Acc>
+__device__ __forceinline__ bool gauss_test_bound(const Acc &at, int xi, int xj, const int *X, T in_err, T &rho2,
+                                                 T &err) {
+    const T u = BoundArith<T>::u;
+    constexpr int D = L + 2;
+    T A[D * (D + 1) / 2], E[D * (D + 1) / 2];
+#pragma unroll
+    for (int r = 0; r < L; ++r) {
+#pragma unroll
+        for (int c = 0; c <= r; ++c) A[r * (r + 1) / 2 + c] = at(X[r], X[c]);
+        A[L * (L + 1) / 2 + r] = at(xi, X[r]);
+        A[(L + 1) * (L + 2) / 2 + r] = at(xj, X[r]);
+    }
+    A[L * (L + 1) / 2 + L] = T(1);
+    A[(L + 1) * (L + 2) / 2 + L] = at(xi, xj);
+    A[(L + 1) * (L + 2) / 2 + L + 1] = T(1);
+#pragma unroll
+    for (int k = 0; k < D * (D + 1) / 2; ++k) E[k] = u * fabs(A[k]) + in_err;
+    E[L * (L + 1) / 2 + L] = T(0);
+    E[(L + 1) * (L + 2) / 2 + L + 1] = T(0);
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+        const T piv = A[j * (j + 1) / 2 + j], ep = E[j * (j + 1) / 2 + j];
+        ok = ok && ep < T(0.25) * piv;
+        const T inv = T(1) / piv;
+        const T einv = ep * inv * inv * T(1.5) + u * fabs(inv);  // 1/(p - e) <= (1 + 1.5 e/p)/p for e < p/4
+#pragma unroll
+        for (int i = j + 1; i < D; ++i) {
+            const T aij = A[i * (i + 1) / 2 + j];
+            const T t = aij * inv;
+            const T et = fabs(aij) * einv + fabs(inv) * E[i * (i + 1) / 2 + j] + u * fabs(t);
+#pragma unroll
+            for (int k = j + 1; k <= i; ++k) {
+                const T akj = A[k * (k + 1) / 2 + j];
+                const T v = BoundArith<T>::fma_(-t, akj, A[i * (i + 1) / 2 + k]);
+                E[i * (i + 1) / 2 + k] += fabs(t) * E[k * (k + 1) / 2 + j] + fabs(akj) * et + u * fabs(v);
+                A[i * (i + 1) / 2 + k] = v;
+            }
+        }
+    }
+    const int i00 = L * (L + 1) / 2 + L, i01 = (L + 1) * (L + 2) / 2 + L, i11 = (L + 1) * (L + 2) / 2 + L + 1;
+    return rho2_bound_t<T>(A[i00], E[i00], A[i01], E[i01], A[i11], E[i11], rho2, err) && ok;
+}
+
+// The FP64 re-test of a key whose FP32 interval touches the guard band, on the
+// approximate C with its bound: decided when the interval clears the FP64 path's knife
+// edge [t2 (1 - 1e-12), t2 (1 + 1e-12)] (then its decision is the exact C's); otherwise
+// the instance is flagged for the exact re-solve and the FP64 result stands in.
+template <int L>
+__device__ __noinline__ TestOut split_retest_call(const double *__restrict__ C, int p, int vi, int vj, const int *S,
+                                                  double tau, double t2, double eps, int *flag) {
+    double r, e;
+    const bool ok = gauss_test_bound<L, double>(C64Acc{C, p}, vi, vj, S, eps * 1.001, r, e);
+    const bool decided = ok && (r + e < t2 * (1.0 - 1e-12) || r - e > t2 * (1.0 + 1e-12));
+    if (!decided) *(volatile int *)flag = 1;
+    TestOut o = gauss_test_reg<L>(C, p, vi, vj, S, tau, t2);
+    if (decided) o.remove = r + e < t2 * (1.0 - 1e-12);
+    return o;
+}
+
 template <int L>
 struct SplitTest {
     static constexpr bool kMixed = false;
@@ -109,18 +222,33 @@ struct SplitTest {
     double tau, t2;
     float t2lo, t2hi;
     unsigned long long *retests;
+    double eps;  // bound on |C - C_exact|, or a negative value when C is exact
+    int *flag;
     __device__ __forceinline__ TestOut operator()(int vi, int vj, const int *S) const {
-        float r2;
-        const bool ok = gauss_test_f32<L>(C32, p, vi, vj, S, r2);
-        if (ok && (r2 < t2lo || r2 > t2hi)) {
+        if (eps < 0.0) {
+            float r2;
+            const bool ok = gauss_test_f32<L>(C32, p, vi, vj, S, r2);
+            if (ok && (r2 < t2lo || r2 > t2hi)) {
+                TestOut o;
+                o.rho2 = (double)r2;
+                o.zexact = __longlong_as_double(0x7ff0000000000000ll);
+                o.remove = r2 < t2lo;
+                return o;
+            }
+            ++*retests;
+            return gauss_test_reg<L>(C, p, vi, vj, S, tau, t2);
+        }
+        float r, e;
+        const bool ok = gauss_test_bound<L, float>(C32Acc{C32, p}, vi, vj, S, (float)(eps * 1.001), r, e);
+        if (ok && (__fadd_ru(r, e) < t2lo || __fsub_rd(r, e) > t2hi)) {
             TestOut o;
-            o.rho2 = (double)r2;
+            o.rho2 = (double)r;
             o.zexact = __longlong_as_double(0x7ff0000000000000ll);
-            o.remove = r2 < t2lo;
+            o.remove = __fadd_ru(r, e) < t2lo;
             return o;
         }
         ++*retests;
-        return gauss_test_reg<L>(C, p, vi, vj, S, tau, t2);
+        return split_retest_call<L>(C, p, vi, vj, S, tau, t2, eps, flag);
     }
 };
 
@@ -132,13 +260,19 @@ __device__ __forceinline__ int inst_of(const long long *__restrict__ off, int co
     return k;
 }
 
+// A kernel of the exact re-solve (rerun) skips every instance whose flag is not set.
+__device__ __forceinline__ bool skip_inst(const BInst &I, bool rerun) { return rerun && *(volatile int *)I.flag == 0; }
+
 // Per p^2 chunk: r2min = 1.4e306 (above every stored rho^2); chunk 0 also clears the
-// instance's DevState; block 0 builds the erfc table of the pmax kernels.
+// instance's DevState (and, on the first pass, its flag); block 0 builds the erfc
+// table of the pmax kernels.
 __global__ void batch_init_kernel(const BInst *__restrict__ inst, const long long *__restrict__ off_p2, int count,
-                                  double *__restrict__ sftab) {
-    if (blockIdx.x == 0) sf_table_build(reinterpret_cast<double (*)[SF_TERMS]>(sftab));  // erfc table for pmax
+                                  double *__restrict__ sftab, bool rerun) {
+    if (blockIdx.x == 0 && !rerun) sf_table_build(reinterpret_cast<double (*)[SF_TERMS]>(sftab));  // erfc table for pmax
     long long lb;
     const BInst &I = inst[inst_of(off_p2, count, blockIdx.x, lb)];
+    if (skip_inst(I, rerun)) return;
+    if (lb == 0 && !rerun && threadIdx.x == 0) *I.flag = 0;
     const long long total = (long long)I.p * I.p;
     const long long k0 = lb * BATCH_P2_CHUNK, k1 = min(total, k0 + BATCH_P2_CHUNK);
     const double big = __longlong_as_double(0x7f7f7f7f7f7f7f7fll);
@@ -149,23 +283,43 @@ __global__ void batch_init_kernel(const BInst *__restrict__ inst, const long lon
     }
 }
 
+// Level 0.  On an approximate C (first pass, c_err set) a pair whose |r| lies within the
+// bound of tanh(tau_0) cannot be decided: the instance is flagged.
 __global__ void batch_level0_kernel(const BInst *__restrict__ inst, const long long *__restrict__ off_tiles,
-                                    int count) {
+                                    int count, bool rerun) {
     long long lb;
     const BInst &I = inst[inst_of(off_tiles, count, blockIdx.x, lb)];
+    if (skip_inst(I, rerun)) return;
+    if (!rerun && I.c_err != nullptr) {
+        const double eps = *I.c_err * 1.001 + 1e-15;
+        const double t0 = sqrt(I.t2[0]);
+        const int nb = (I.p + 31) / 32;
+        int rem = (int)lb, bi = 0;
+        while (rem >= nb - bi) {
+            rem -= nb - bi;
+            ++bi;
+        }
+        const int bj = bi + rem;
+        bool unsure = false;
+        for (int r = threadIdx.x >> 5; r < 32; r += blockDim.x >> 5) {
+            const int i = bi * 32 + r, j = bj * 32 + (threadIdx.x & 31);
+            if (i < I.p && j < I.p && i < j) unsure |= !(fabs(fabs(I.C[(size_t)i * I.p + j]) - t0) > eps);
+        }
+        if (__syncthreads_or(unsure) && threadIdx.x == 0) *(volatile int *)I.flag = 1;
+    }
     level0_tile(I.C, I.p, I.tau[0], I.l0, I.G, I.zmin, I.r2min, I.kept, I.st, (int)lb);
 }
 
 // Warp per (instance, row); level 1 compacts G, later levels refilter the lists.
 __global__ void batch_compact_kernel(const BInst *__restrict__ inst, const long long *__restrict__ off_rows,
-                                     int count, int level) {
+                                     int count, int level, bool rerun) {
     const int lane = threadIdx.x & 31;
     const long long rows = off_rows[count];
     const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < rows; g += warps) {
         long long r;
         const BInst &I = inst[inst_of(off_rows, count, g, r)];
-        if (I.st->done) continue;
+        if (skip_inst(I, rerun) || I.st->done) continue;
         const int deg = (level == 1) ? compact_row(I.G, I.p, I.adj, I.up, (int)r, lane)
                                      : recompact_row(I.G, I.p, I.adj, I.up, (int)r, lane);
         if (lane == 0) atomicMax(&I.st->max_degree[level], deg);
@@ -176,8 +330,12 @@ __global__ void batch_compact_kernel(const BInst *__restrict__ inst, const long 
 // rule max degree - 1 < level, and the level cap), scan its rows into the edge prefix
 // and publish its edge count.
 __global__ void batch_scan_kernel(const BInst *__restrict__ inst, int count, int level, int max_level,
-                                  long long *__restrict__ edges) {
+                                  long long *__restrict__ edges, bool rerun) {
     const BInst &I = inst[blockIdx.x];
+    if (skip_inst(I, rerun)) {
+        if (threadIdx.x == 0) edges[blockIdx.x] = 0;
+        return;
+    }
     DevState *st = I.st;
     __shared__ int s_run;
     if (threadIdx.x == 0) {
@@ -212,7 +370,8 @@ __global__ void batch_edge_offsets_kernel(const long long *__restrict__ edges, i
 
 template <int L, int G, bool SPLIT>
 __global__ void __launch_bounds__(256) batch_level_kernel(const BInst *__restrict__ inst,
-                                                         const long long *__restrict__ edge_off, int count) {
+                                                         const long long *__restrict__ edge_off, int count,
+                                                         bool rerun) {
     constexpr int GPW = 32 / G;
     const int lane = threadIdx.x & 31, gl = lane & (G - 1), gw = lane / G;
     const unsigned gshift = (unsigned)(gw * G);
@@ -237,9 +396,13 @@ __global__ void __launch_bounds__(256) batch_level_kernel(const BInst *__restric
         bool removed = false;
         unsigned long long n_tests = 0, retests = 0;
         if constexpr (SPLIT) {
+            // the rerun has the exact C: no bound
+            const double eps = (has && !rerun && I.c_err != nullptr) ? *I.c_err : -1.0;
             walk_edge<L, G>(J, has, I.adj, I.p, gl, gshift, gbits,
-                            SplitTest<L>{I.C, I.C32, I.p, I.tau[L], I.t2[L], I.t2lo[L], I.t2hi[L], &retests}, I.G,
-                            nullptr, BATCH_MAX_LEVEL, I.rec, I.rec_cap, I.st, r2min, zmin_exact, removed, n_tests);
+                            SplitTest<L>{I.C, I.C32, I.p, I.tau[L], I.t2[L], I.t2lo[L], I.t2hi[L], &retests, eps,
+                                         I.flag},
+                            I.G, nullptr, BATCH_MAX_LEVEL, I.rec, I.rec_cap, I.st, r2min, zmin_exact, removed,
+                            n_tests);
         } else {
             walk_edge<L, G>(J, has, I.adj, I.p, gl, gshift, gbits, F64Test<L>{I.C, I.p, I.tau[L], I.t2[L]}, I.G,
                             nullptr, BATCH_MAX_LEVEL, I.rec, I.rec_cap, I.st, r2min, zmin_exact, removed, n_tests);
@@ -258,12 +421,13 @@ __global__ void __launch_bounds__(256) batch_level_kernel(const BInst *__restric
 
 // pmax of the pairs removed at level 0 and the -1 fill, per p^2 chunk.
 __global__ void batch_pmax_removed_kernel(const BInst *__restrict__ inst, const long long *__restrict__ off_p2,
-                                          int count, const double *__restrict__ sftab) {
+                                          int count, const double *__restrict__ sftab, bool rerun) {
     __shared__ double tab[SF_CENTRES][SF_TERMS];
-    sf_table_load(tab, sftab);
-    __syncthreads();
     long long lb;
     const BInst &I = inst[inst_of(off_p2, count, blockIdx.x, lb)];
+    if (skip_inst(I, rerun)) return;  // uniform over the block
+    sf_table_load(tab, sftab);
+    __syncthreads();
     const unsigned p = (unsigned)I.p;
     const unsigned total = p * p;
     const unsigned k0 = (unsigned)lb * BATCH_P2_CHUNK, k1 = min(total, k0 + (unsigned)BATCH_P2_CHUNK);
@@ -275,11 +439,12 @@ __global__ void batch_pmax_removed_kernel(const BInst *__restrict__ inst, const 
 }
 
 // pmax of the pairs kept at level 0, block per instance.
-__global__ void batch_pmax_kept_kernel(const BInst *__restrict__ inst, const double *__restrict__ sftab) {
+__global__ void batch_pmax_kept_kernel(const BInst *__restrict__ inst, const double *__restrict__ sftab, bool rerun) {
     __shared__ double tab[SF_CENTRES][SF_TERMS];
+    const BInst &I = inst[blockIdx.x];
+    if (skip_inst(I, rerun)) return;  // uniform over the block
     sf_table_load(tab, sftab);
     __syncthreads();
-    const BInst &I = inst[blockIdx.x];
     const int n = I.st->n_kept;
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
         const int k = I.kept[t];
@@ -296,7 +461,7 @@ namespace host {
 namespace {
 
 struct BatchLayout {
-    size_t table, off_tiles, off_rows, off_p2, edges, edge_off, sftab, slices, total;
+    size_t table, off_tiles, off_rows, off_p2, edges, edge_off, sftab, flags, slices, total;
 };
 
 size_t al(size_t x) { return (x + 255) / 256 * 256; }
@@ -325,6 +490,8 @@ BatchLayout layout(const int *p, int count) {
     off += al(((size_t)count + 1) * sizeof(long long));
     L.sftab = off;
     off += al((size_t)SF_CENTRES * SF_TERMS * sizeof(double));
+    L.flags = off;
+    off += al((size_t)count * sizeof(int));
     L.slices = off;
     for (int k = 0; k < count; ++k) off += slice_bytes(p[k]);
     L.total = off;
@@ -333,26 +500,28 @@ BatchLayout layout(const int *p, int count) {
 
 // plan words
 enum {
-    PW_MAGIC = 0, PW_WS, PW_COUNT, PW_MAXL, PW_PREC, PW_TILES, PW_ROWS, PW_P2, PW_SMS, PW_LANES  // PW_LANES + level
+    PW_MAGIC = 0, PW_WS, PW_COUNT, PW_MAXL, PW_PREC, PW_TILES, PW_ROWS, PW_P2, PW_SMS, PW_FLAGS,
+    PW_LANES  // PW_LANES + level, up to PW_LANES + BATCH_MAX_LEVEL (< 48 plan words)
 };
+static_assert(PW_LANES + BATCH_MAX_LEVEL < 48, "plan words");
 constexpr long long PLAN_MAGIC = 0x4743534c42415443ll;  // "GCSLBATC"
 
 template <int L, int G, bool SPLIT>
-void launch_level_t(const BInst *inst, const long long *eoff, int count, int sms, cudaStream_t s) {
+void launch_level_t(const BInst *inst, const long long *eoff, int count, int sms, bool rerun, cudaStream_t s) {
     const int threads = L >= 4 ? 128 : 256;
     const int blocks = sms * (L >= 4 ? 12 : 8);
-    batch_level_kernel<L, G, SPLIT><<<blocks, threads, 0, s>>>(inst, eoff, count);
+    batch_level_kernel<L, G, SPLIT><<<blocks, threads, 0, s>>>(inst, eoff, count, rerun);
 }
 
 template <bool SPLIT>
-cudaError_t launch_level(int L, int lanes, const BInst *inst, const long long *eoff, int count, int sms,
+cudaError_t launch_level(int L, int lanes, const BInst *inst, const long long *eoff, int count, int sms, bool rerun,
                          cudaStream_t s) {
     const bool g8 = lanes == 8 && L <= 4;
     switch (L) {
 #define GCSL_BL(K)                                                                 \
     case K:                                                                        \
-        if (g8 && K <= 4) launch_level_t<K, (K <= 4 ? 8 : 32), SPLIT>(inst, eoff, count, sms, s); \
-        else launch_level_t<K, 32, SPLIT>(inst, eoff, count, sms, s);             \
+        if (g8 && K <= 4) launch_level_t<K, (K <= 4 ? 8 : 32), SPLIT>(inst, eoff, count, sms, rerun, s); \
+        else launch_level_t<K, 32, SPLIT>(inst, eoff, count, sms, rerun, s);      \
         break;
         GCSL_BL(1) GCSL_BL(2) GCSL_BL(3) GCSL_BL(4) GCSL_BL(5) GCSL_BL(6)
         GCSL_BL(7) GCSL_BL(8) GCSL_BL(9) GCSL_BL(10) GCSL_BL(11) GCSL_BL(12)
@@ -388,6 +557,8 @@ int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level,
         const size_t pp = (size_t)p * p;
         I.C = X.C;
         I.C32 = X.C32;
+        I.c_err = precision == GCSL_PREC_SPLIT ? X.c_err : nullptr;
+        I.flag = reinterpret_cast<int *>(base + Ly.flags) + k;
         I.G = X.G;
         I.pmax = X.pmax;
         I.rec = X.rec_pool;
@@ -439,6 +610,7 @@ int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level,
                             s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(base + Ly.off_p2, op2.data(), op2.size() * sizeof(long long), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(base + Ly.flags, 0, (size_t)count * sizeof(int), s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host vectors die with this call
     if (e != cudaSuccess) return GCSL_ERR_DEVICE;
     std::memset(plan, 0, sizeof(long long) * 48);
@@ -452,10 +624,16 @@ int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level,
     plan[PW_P2] = op2[(size_t)count];
     plan[PW_SMS] = sms;
     for (int l = 0; l <= BATCH_MAX_LEVEL; ++l) plan[PW_LANES + l] = 32;
+    plan[PW_FLAGS] = (long long)reinterpret_cast<uintptr_t>(base + Ly.flags);
     return GCSL_OK;
 }
 
+
 bool gauss_batch_plan_ok(const long long *plan) { return plan && plan[PW_MAGIC] == PLAN_MAGIC; }
+
+const int *gauss_batch_flags(const long long *plan) {
+    return gauss_batch_plan_ok(plan) ? reinterpret_cast<const int *>(static_cast<uintptr_t>(plan[PW_FLAGS])) : nullptr;
+}
 
 int gauss_batch_set_lanes(long long *plan, int level, int lanes) {
     if (!gauss_batch_plan_ok(plan) || level < 1 || level > BATCH_MAX_LEVEL || (lanes != 32 && lanes != 8))
@@ -465,8 +643,9 @@ int gauss_batch_set_lanes(long long *plan, int level, int lanes) {
 }
 
 // Enqueues the whole batch: init, level 0, levels 1..max_level, pmax.  No host reads:
-// the sequence can be captured into a CUDA graph.
-int gauss_batch_run(const long long *plan, cudaStream_t s) {
+// the sequence can be captured into a CUDA graph.  With rerun set only the flagged
+// instances are solved (again), with the test of an exact C.
+int gauss_batch_run(const long long *plan, cudaStream_t s, bool rerun) {
     if (!gauss_batch_plan_ok(plan)) return GCSL_ERR_INVALID_ARG;
     char *base = reinterpret_cast<char *>(static_cast<uintptr_t>(plan[PW_WS]));
     const int count = (int)plan[PW_COUNT], max_level = (int)plan[PW_MAXL], sms = (int)plan[PW_SMS];
@@ -487,23 +666,23 @@ int gauss_batch_run(const long long *plan, cudaStream_t s) {
     long long *eoff = reinterpret_cast<long long *>(base + Ly.edge_off);
     double *sftab = reinterpret_cast<double *>(base + Ly.sftab);
 
-    batch_init_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count, sftab);
-    batch_level0_kernel<<<(unsigned)plan[PW_TILES], 256, 0, s>>>(inst, ot, count);
+    batch_init_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count, sftab, rerun);
+    batch_level0_kernel<<<(unsigned)plan[PW_TILES], 256, 0, s>>>(inst, ot, count, rerun);
     note_launch(2);
     const long long rows = plan[PW_ROWS];
     const int cblocks = (int)std::min<long long>((rows + 7) / 8, (long long)sms * 16);
     for (int level = 1; level <= max_level; ++level) {
-        batch_compact_kernel<<<cblocks, 256, 0, s>>>(inst, orow, count, level);
-        batch_scan_kernel<<<count, 256, 0, s>>>(inst, count, level, max_level, edges);
+        batch_compact_kernel<<<cblocks, 256, 0, s>>>(inst, orow, count, level, rerun);
+        batch_scan_kernel<<<count, 256, 0, s>>>(inst, count, level, max_level, edges, rerun);
         batch_edge_offsets_kernel<<<1, 1024, 0, s>>>(edges, count, eoff);
         note_launch(3);
         const int lanes = (int)plan[PW_LANES + level];
-        const cudaError_t e = split ? launch_level<true>(level, lanes, inst, eoff, count, sms, s)
-                                    : launch_level<false>(level, lanes, inst, eoff, count, sms, s);
+        const cudaError_t e = split ? launch_level<true>(level, lanes, inst, eoff, count, sms, rerun, s)
+                                    : launch_level<false>(level, lanes, inst, eoff, count, sms, rerun, s);
         if (e != cudaSuccess) return GCSL_ERR_DEVICE;
     }
-    batch_pmax_removed_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count, sftab);
-    batch_pmax_kept_kernel<<<count, 256, 0, s>>>(inst, sftab);
+    batch_pmax_removed_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count, sftab, rerun);
+    batch_pmax_kept_kernel<<<count, 256, 0, s>>>(inst, sftab, rerun);
     note_launch(2);
     return cudaGetLastError() == cudaSuccess ? GCSL_OK : GCSL_ERR_DEVICE;
 }
@@ -515,6 +694,10 @@ int gauss_batch_collect(const long long *plan, gcsl_gauss_instance *out, int cou
     std::vector<BInst> tab((size_t)count);
     if (cudaMemcpyAsync(tab.data(), base, tab.size() * sizeof(BInst), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
+        return GCSL_ERR_DEVICE;
+    std::vector<int> flags((size_t)count, 0);
+    if (cudaMemcpyAsync(flags.data(), gauss_batch_flags(plan), (size_t)count * sizeof(int), cudaMemcpyDeviceToHost,
+                        s) != cudaSuccess)
         return GCSL_ERR_DEVICE;
     std::vector<DevState> st((size_t)count);
     for (int k = 0; k < count; ++k)
@@ -533,6 +716,7 @@ int gauss_batch_collect(const long long *plan, gcsl_gauss_instance *out, int cou
         for (int l = 1; l <= BATCH_MAX_LEVEL; ++l) tests += (long long)h.tests[l];
         o.tests = tests;
         o.retests = (int64_t)h.retests;
+        o.exact_rerun = flags[(size_t)k] != 0 ? 1 : 0;
         if (first == GCSL_OK && h.status != GCSL_OK) first = h.status;
     }
     return first;

@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define GCSL_ABI_VERSION 1
+#define GCSL_ABI_VERSION 2
 
 #define GCSL_OK 0
 #define GCSL_ERR_INVALID_ARG 1
@@ -178,6 +178,14 @@ int gcsl_orient_edges(const uint16_t *G, int32_t p, const int32_t *sepsets, int3
  * tests whose p-value lies within 10 % of alpha (thresholds band_lo at 1.1 alpha and
  * band_hi at 0.9 alpha) or whose elimination meets a pivot below 1e-3: skeleton and
  * sepsets equal the FP64 ones, pmax carries the FP32 error of z*.
+ * With c_err set (device double: a bound on |C - C_exact|, as written by
+ * gcsl_corr_tc_batch_run_split), every split decision carries an error bound that
+ * includes it; an instance with a test neither FP32 nor FP64 can decide on that C is
+ * flagged (exact_rerun).  The full split sequence is
+ *   gcsl_corr_tc_batch_run_split -> gcsl_gauss_batch_run ->
+ *   gcsl_corr_tc_batch_run_flagged (with gcsl_gauss_batch_flags) -> gcsl_gauss_batch_rerun,
+ * after which every instance's skeleton and sepsets equal those of the FP64 path on the
+ * exact (seven-digit) correlation.
  * max_level <= GCSL_BATCH_MAX_LEVEL; the instances of a plan must not overlap in time
  * with another run of the same workspace. */
 #define GCSL_PREC_F64 0
@@ -197,11 +205,13 @@ typedef struct gcsl_gauss_instance {
     double *pmax;             /* device p x p pmax out */
     int32_t *rec_pool;        /* device sepset record pool ([lo, hi, level, S...]), or NULL */
     int64_t rec_cap;
+    const double *c_err;      /* device bound on |C - C_exact| (GCSL_PREC_SPLIT on a split correlation), or NULL */
     int32_t status;           /* out (collect): device status of this instance */
     int32_t levels_run;       /* out (collect) */
     int64_t n_records;        /* out (collect): ints used in rec_pool (may exceed rec_cap) */
     int64_t tests;            /* out (collect): canonical executed tests, level 0 included */
     int64_t retests;          /* out (collect): FP64 re-tests of GCSL_PREC_SPLIT */
+    int32_t exact_rerun;      /* out (collect): 1 when the instance needed the exact correlation */
 } gcsl_gauss_instance;
 
 typedef struct gcsl_batch_plan {
@@ -212,6 +222,11 @@ size_t gcsl_gauss_batch_workspace_bytes(const int32_t *p, int32_t count);
 int gcsl_gauss_batch_prepare(const gcsl_gauss_instance *inst, int32_t count, int32_t max_level, int32_t precision,
                              void *workspace, size_t workspace_bytes, gcsl_batch_plan *plan, void *stream);
 int gcsl_gauss_batch_run(const gcsl_batch_plan *plan, void *stream);
+/* Solves again, with the exact test, the instances flagged by the last run (after their
+ * exact correlation); the other instances are left as they are.  Enqueues only. */
+int gcsl_gauss_batch_rerun(const gcsl_batch_plan *plan, void *stream);
+/* Device array of the plan's per-instance exact_rerun flags (count int32), or NULL. */
+const int32_t *gcsl_gauss_batch_flags(const gcsl_batch_plan *plan);
 int gcsl_gauss_batch_collect(const gcsl_batch_plan *plan, gcsl_gauss_instance *inst, int32_t count, void *stream);
 /* Autotuner hook: lanes per edge (32 or 8; 8 only for levels <= 4) of a level's test
  * kernel.  Results do not depend on it. */
@@ -226,6 +241,16 @@ int gcsl_corr_tc_batch_prepare(const void *const *X, int32_t dtype, const int64_
                                const int64_t *ldx, double *const *C, float *const *C32, int32_t count,
                                void *workspace, size_t workspace_bytes, gcsl_batch_plan *plan, void *stream);
 int gcsl_corr_tc_batch_run(const gcsl_batch_plan *plan, void *stream);
+/* Split precision (replaces np.corrcoef, gpucsl/pc/helpers.py:58-59, for the batched
+ * split path): the product over the five leading digits only (15 of the 28 digit-pair
+ * products); c_err (device, count doubles) receives per instance a bound eps on the
+ * distance of each entry of C to the seven-digit result, eps = 2.5 * 2^-35 (1.02 w +
+ * sqrt(w)) with w = n / min_i sum_t y_ti^2 (y: centred, power-of-two-scaled samples).
+ * The digit planes keep all seven digits. */
+int gcsl_corr_tc_batch_run_split(const gcsl_batch_plan *plan, double *c_err, void *stream);
+/* The seven-digit product, diagonal and normalisation for the instances whose device
+ * flag (count int32) is non-zero, on the digits of the preceding run of the plan. */
+int gcsl_corr_tc_batch_run_flagged(const gcsl_batch_plan *plan, const int32_t *flags, void *stream);
 
 /* ----------------------------------------------------- discrete skeleton (d,e) */
 /* Replaces the level loop of gpucsl/pc/discover_skeleton_discrete.py:80-112 with the

@@ -42,7 +42,7 @@ def test_abi_version_and_status_strings(built_lib):
     from gpucsl_gb300 import _lib
 
     L = _lib.lib()
-    assert L.gcsl_version() == 1
+    assert L.gcsl_version() == 2
     assert L.gcsl_status_string(0) == b"ok"
     assert b"record pool" in L.gcsl_status_string(_lib.GCSL_ERR_CAPACITY)
     # argument validation happens on the host, before any device call

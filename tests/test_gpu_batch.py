@@ -73,20 +73,28 @@ def test_f64_batch_equals_single_path_and_oracle(cuda, workloads):
 
 
 def test_split_precision_keeps_every_decision(cuda, workloads):
+    """Split: the five-digit correlation lies within its stated bound of the exact one
+    (instances solved again hold the exact one), and every decision equals FP64's."""
     torch = cuda
     b64, _ = make_batch(torch, workloads, "f64")
     r64 = b64.run()
     b32, _ = make_batch(torch, workloads, "split")
     r32 = b32.run()
+    eps = b32._cerr.cpu().numpy()
     worst = 0.0
     for k in range(len(workloads)):
         G, sep, pmax = b64.to_host(k)
         G2, sep2, pmax2 = b32.to_host(k)
         assert (G == G2).all() and (sep == sep2).all(), k
         assert r32[k].tests == r64[k].tests, k
-        assert np.array_equal(b32.C[k].cpu().numpy(), b64.C[k].cpu().numpy())
+        dC = float((b32.C[k] - b64.C[k]).abs().max())
+        if r32[k].exact_rerun:
+            assert dC == 0.0, k
+        else:
+            assert dC <= eps[k], (k, dC, eps[k])
         worst = max(worst, float(np.abs(pmax - pmax2).max()))
     assert worst < 1e-4, worst
+    assert (eps[[k for k, w in enumerate(workloads) if w.data.shape[1] > 1]] < 1e-6).all(), eps
 
 
 def test_instance_alone_equals_instance_in_the_mix(cuda, workloads):
