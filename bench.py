@@ -97,6 +97,28 @@ def max_over_ranks(x: float, world: int) -> float:
     return float(t.item())
 
 
+def sum_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def gather_lists(x: list, world: int) -> list:
+    """Concatenation of every rank's list (rank order)."""
+    if world == 1:
+        return list(x)
+    import torch.distributed as dist
+
+    parts = [None] * world
+    dist.all_gather_object(parts, list(x))
+    return [v for part in parts for v in part]
+
+
 # -------------------------------------------------------------------- clocks
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -349,21 +371,25 @@ def e2e_api_leg(data, solver, E: int, levels_run: int, reps: int = 10) -> dict:
 BATCH_COUNT, BATCH_ALPHA, BATCH_L = 512, 0.01, 4
 
 
-def batched_leg(reps: int = 10) -> dict:
+def batched_leg(reps: int = 10, world: int = 1, rank: int = 0) -> dict:
     """512 uneven Gaussian instances (p ~ U{50..400}, n ~ U{500..20000}, degree ~ U[2, 4],
     seeds 1000 + k, alpha 0.01, levels <= 4): batched tensor-core correlation + batched
     level loop replayed as one CUDA graph, split precision (FP32 tests, FP64 re-test in
-    the guard band) and FP64; against the plain per-instance path on the same samples."""
-    import ctypes as ct
-
+    the guard band) and FP64; against the plain per-instance path on the same samples.
+    Under N ranks each rank solves its footprint-balanced share of the 512 instances
+    (replicas, no collective on the data path); times are the slowest rank's."""
     import numpy as np
     import torch
 
     from gpucsl_gb300 import engine
     from gpucsl_gb300.batch import GaussianBatch
+    from gpucsl_gb300.shard import gaussian_cost, my_shard
     from gpucsl_gb300.synthetic import batch_instance_sizes, gaussian_dag_data_device
 
-    sizes = batch_instance_sizes(BATCH_COUNT)
+    all_sizes = batch_instance_sizes(BATCH_COUNT)
+    mine = my_shard([gaussian_cost(p, n) for (p, n, _, _) in all_sizes], world, rank)
+    sizes = [all_sizes[k] for k in mine]
+    count = len(sizes)
     ps, ns = [s[0] for s in sizes], [s[1] for s in sizes]
     Xs = [gaussian_dag_data_device(p, n, d, seed) for (p, n, d, seed) in sizes]
     torch.cuda.synchronize()
@@ -379,9 +405,13 @@ def batched_leg(reps: int = 10) -> dict:
             ts.append(a.elapsed_time(b) / 1e3)
         return ts
 
+    def slowest(t: float) -> float:
+        return max_over_ranks(t, world)
+
     out = {"workload": f"gaussian_batch_{BATCH_COUNT}_p50-400_n500-20000_deg2-4_alpha{BATCH_ALPHA}_L{BATCH_L}",
            "unit": "skeletons/s", "data": "synthetic (DAG from numpy seed 1000+k, noise from torch on the device)",
-           "sample_bytes": int(sum(p * n * 8 for p, n in zip(ps, ns)))}
+           "sample_bytes": int(sum(p * n * 8 for (p, n, _, _) in all_sizes)),
+           "ranks": world, "instances_per_rank": f"{count} on rank {rank} (footprint-balanced split)"}
     results = {}
     for prec in ("split", "f64"):
         b = GaussianBatch(ps, ns, BATCH_ALPHA, BATCH_L, prec)
@@ -391,6 +421,7 @@ def batched_leg(reps: int = 10) -> dict:
         b.capture()
         for _ in range(2):
             b.graph.replay()
+        barrier(world)
         ts = timed(b.graph.replay, reps)
         # the stages on their own: the correlation (split: five-digit product with its
         # bound), then the level loop (split: first pass, exact correlation of the flagged
@@ -400,27 +431,27 @@ def batched_leg(reps: int = 10) -> dict:
             t_corr += timed(b.enqueue_correlation, 1)
             t_lv += timed(b.enqueue_levels, 1)
         res = b.collect()
-        tests = sum(r.tests for r in res)
-        results[prec] = [b.to_host(k) for k in range(BATCH_COUNT)]
-        out[prec] = {"value": round(BATCH_COUNT / statistics.median(ts), 2), "ms_per_batch":
-                     round(1e3 * statistics.median(ts), 3), "tests_per_batch": tests,
-                     "tests_per_s": round(tests / statistics.median(ts), 1),
-                     "retests": sum(r.retests for r in res), "lanes_per_level": lanes,
-                     "corr_ms": round(1e3 * statistics.median(t_corr), 3),
-                     "levels_ms": round(1e3 * statistics.median(t_lv), 3),
-                     "status_nonzero": sum(1 for r in res if r.status != 0)}
+        tests = int(sum_over_ranks(sum(r.tests for r in res), world))
+        results[prec] = [b.to_host(k) for k in range(count)]
+        t_batch = slowest(statistics.median(ts))
+        out[prec] = {"value": round(BATCH_COUNT / t_batch, 2), "ms_per_batch": round(1e3 * t_batch, 3),
+                     "tests_per_batch": tests, "tests_per_s": round(tests / t_batch, 1),
+                     "retests": int(sum_over_ranks(sum(r.retests for r in res), world)), "lanes_per_level": lanes,
+                     "corr_ms": round(1e3 * slowest(statistics.median(t_corr)), 3),
+                     "levels_ms": round(1e3 * slowest(statistics.median(t_lv)), 3),
+                     "status_nonzero": int(sum_over_ranks(sum(1 for r in res if r.status != 0), world))}
         if prec == "split":
             eps = b._cerr.cpu().numpy()
             out[prec]["correlation"] = "five of seven integer digits (15 of 28 digit-pair products) on tcgen05"
-            out[prec]["c_err_max"] = float(eps.max())
-            out[prec]["c_err_median"] = float(np.median(eps))
-            out[prec]["exact_reruns"] = sum(r.exact_rerun for r in res)
+            out[prec]["c_err_max"] = max_over_ranks(float(eps.max()), world)
+            out[prec]["c_err_median_rank0"] = float(np.median(eps))
+            out[prec]["exact_reruns"] = int(sum_over_ranks(sum(r.exact_rerun for r in res), world))
         del b
         torch.cuda.empty_cache()
     # decisions and pmax of split against FP64
     mism_g = mism_s = 0
     max_abs = max_rel = 0.0
-    for (G1, S1, P1), (G2, S2, P2) in zip(results["split"], results["f64"]):
+    for (G1, S1, P1), (G2, S2, P2) in zip(results["split"], results["f64"]):  # this rank's instances
         mism_g += int((G1 != G2).sum())
         mism_s += int((S1 != S2).any(axis=2).sum())
         iu = np.triu_indices(G1.shape[0], 1)
@@ -428,8 +459,10 @@ def batched_leg(reps: int = 10) -> dict:
             d = np.abs(P1[iu] - P2[iu])
             max_abs = max(max_abs, float(d.max()))
             max_rel = max(max_rel, float((d / np.maximum(np.abs(P2[iu]), 1e-300)).max()))
-    out["split_vs_f64"] = {"skeleton_mismatches": mism_g, "sepset_mismatches": mism_s,
-                           "pmax_max_abs_err": max_abs, "pmax_max_rel_err": max_rel}
+    out["split_vs_f64"] = {"skeleton_mismatches": int(sum_over_ranks(mism_g, world)),
+                           "sepset_mismatches": int(sum_over_ranks(mism_s, world)),
+                           "pmax_max_abs_err": max_over_ranks(max_abs, world),
+                           "pmax_max_rel_err": max_over_ranks(max_rel, world)}
     # plain per-instance path (single-problem API, no host sync inside the loop)
     solvers = [engine.GaussianSolver(p, BATCH_L, record_cap=4 * p * p) for p in ps]  # no pool growth
     Cs = [torch.empty((p, p), dtype=torch.float64, device="cuda") for p in ps]
@@ -438,14 +471,14 @@ def batched_leg(reps: int = 10) -> dict:
     thr = [engine.gaussian_thresholds(n, BATCH_ALPHA) for n in ns]
 
     def plain():
-        for k in range(BATCH_COUNT):
+        for k in range(count):
             engine.correlation(Xs[k], out=Cs[k], workspace=corr_ws)
             solvers[k].run(Cs[k], ns[k], thr[k], sync=False)
 
     plain()
-    tp = timed(plain, 3)
-    out["plain_f64"] = {"value": round(BATCH_COUNT / statistics.median(tp), 2),
-                        "ms_per_batch": round(1e3 * statistics.median(tp), 3)}
+    barrier(world)
+    tp = slowest(statistics.median(timed(plain, 3)))
+    out["plain_f64"] = {"value": round(BATCH_COUNT / tp, 2), "ms_per_batch": round(1e3 * tp, 3)}
     out["speedup_split_vs_plain"] = round(out["split"]["value"] / out["plain_f64"]["value"], 2)
     return out
 

@@ -191,6 +191,122 @@ SideStream *side_stream() {
     return &s;
 }
 
+// Level batches replayed from CUDA graphs.  A solve enqueues its levels in batches
+// (level 1, then up to 8 levels per host read of the termination state); each batch
+// costs about four launches per level, which on the upper levels (little work each) is
+// more host time than device time.  When the same batch recurs -- the same workspace,
+// matrix, outputs, thresholds and level range, as in repeated solves of one solver --
+// it is captured once into a CUDA graph (its side-stream candidate kernels joined back
+// at the end of the batch) and replayed by one launch.  A batch seen once, the level
+// timers and the allocation-free path launch directly.
+struct LevelGraphKey {
+    const void *ws;
+    const double *C;
+    const void *G, *sep, *rec;
+    long long rec_cap;
+    int p, max_level, a, b, n_thr, mixed, chunked, sms;
+    unsigned long long thr_hash;
+};
+
+struct LevelGraph {
+    LevelGraphKey key;
+    cudaGraphExec_t exec = nullptr;
+    bool failed = false;  // capture not possible: always launch directly
+    long long kernels = 0;
+};
+
+struct LevelGraphCache {
+    static constexpr int kEntries = 16;
+    LevelGraph e[kEntries];
+    int used = 0, next = 0;
+    cudaStream_t cap = nullptr;   // private stream the batches are captured on
+    cudaEvent_t cap_join = nullptr;
+};
+
+LevelGraphCache *level_graph_cache() {
+    static thread_local LevelGraphCache caches[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return nullptr;
+    LevelGraphCache &c = caches[dev];
+    if (!c.cap) {
+        if (cudaStreamCreateWithFlags(&c.cap, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+        if (cudaEventCreateWithFlags(&c.cap_join, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+    }
+    return &c;
+}
+
+bool graphs_off() {
+    static const bool off = [] {
+        const char *e = getenv("GCSL_LEVEL_GRAPHS");
+        return e && e[0] == '0';
+    }();
+    return off;
+}
+
+// Launches levels key.a..key.b on s: from the cached graph when the batch recurs (captured
+// on its second occurrence), else directly.  enqueue_on(level, stream) enqueues a level;
+// side is the solve's side stream, joined back into the capture before it ends.
+template <typename EnqueueOn>
+cudaError_t launch_level_batch(const LevelGraphKey &key, cudaStream_t s, cudaStream_t side, EnqueueOn enqueue_on) {
+    auto direct = [&]() -> cudaError_t {
+        for (int l = key.a; l <= key.b; ++l) {
+            const cudaError_t e = enqueue_on(l, s);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    };
+    LevelGraphCache *c = graphs_off() ? nullptr : level_graph_cache();
+    if (!c) return direct();
+    LevelGraph *g = nullptr;
+    for (int i = 0; i < c->used; ++i)
+        if (std::memcmp(&c->e[i].key, &key, sizeof(key)) == 0) g = &c->e[i];
+    if (!g) {  // first occurrence: remember it, launch directly
+        LevelGraph &slot = c->e[c->used < LevelGraphCache::kEntries ? c->used++ : c->next];
+        if (c->used == LevelGraphCache::kEntries) c->next = (c->next + 1) % LevelGraphCache::kEntries;
+        if (slot.exec) cudaGraphExecDestroy(slot.exec);
+        slot = LevelGraph{};
+        slot.key = key;
+        return direct();
+    }
+    if (g->failed) return direct();
+    if (!g->exec) {
+        const long long k0 = g_kernel_launches.load(std::memory_order_relaxed);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(c->cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            for (int l = key.a; l <= key.b && e == cudaSuccess; ++l) e = enqueue_on(l, c->cap);
+            if (e == cudaSuccess && side) {
+                e = cudaEventRecord(c->cap_join, side);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(c->cap, c->cap_join, 0);
+            }
+            const cudaError_t ee = cudaStreamEndCapture(c->cap, &graph);
+            if (e == cudaSuccess) e = ee;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            cudaGetLastError();  // capture errors are not sticky: clear and launch directly from now on
+            g->exec = nullptr;
+            g->failed = true;
+            g_last_error[0] = '\0';
+            return direct();
+        }
+        g->kernels = g_kernel_launches.load(std::memory_order_relaxed) - k0;
+        g_kernel_launches.fetch_sub(g->kernels, std::memory_order_relaxed);  // counted when replayed
+    }
+    const cudaError_t e = cudaGraphLaunch(g->exec, s);
+    if (e == cudaSuccess) host::note_launch((int)g->kernels);
+    return host::note_error("level batch graph launch", e);
+}
+
+unsigned long long fnv1a(const void *data, size_t bytes) {
+    const unsigned char *b = static_cast<const unsigned char *>(data);
+    unsigned long long h = 1469598103934665603ull;
+    for (size_t i = 0; i < bytes; ++i) h = (h ^ b[i]) * 1099511628211ull;
+    return h;
+}
+
 // Joins the side stream back into the solve's stream on every return after the fork,
 // so no side-stream work of a failed call outlives the call unordered with the stream.
 struct SideJoin {
@@ -257,17 +373,16 @@ HostCtl *host_ctl() {
 // d - 1 >= l: a batch never extends past min(d - 1, ...) of the last read.
 // `words` are two host words for the control reads: the calling thread's pinned words,
 // or (allocation-free path) words on the caller's stack, read by a synchronous copy.
-template <typename EnqueueLevel>
-int run_levels(int max_level, DevState *d_st, cudaStream_t s, int32_t *words, EnqueueLevel enqueue) {
+// enqueue_range(a, b) enqueues levels a..b on `s`.
+template <typename EnqueueRange>
+int run_levels(int max_level, DevState *d_st, cudaStream_t s, int32_t *words, EnqueueRange enqueue_range) {
     int level = 1;
     int bound = std::min(max_level, GCSL_MAX_LEVELS - 1);  // highest level that may still run
     int batch = 1;
     while (level <= bound) {
         const int last = std::min(bound, level + batch - 1);
-        for (; level <= last; ++level) {
-            cudaError_t e = enqueue(level);
-            if (e != cudaSuccess) return GCSL_ERR_DEVICE;
-        }
+        if (enqueue_range(level, last) != cudaSuccess) return GCSL_ERR_DEVICE;
+        level = last + 1;
         if (level > bound) break;
         cudaError_t e = cudaMemcpyAsync(&words[0], &d_st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess)
@@ -436,7 +551,7 @@ int gcsl::host::gauss_skeleton_run(const double *C, int p, long long n_obs, cons
         host::launch_pmax_level0(C, w.zmin, p, n_obs, w.sftab, pmax, sms, aux) != cudaSuccess)
         return GCSL_ERR_DEVICE;
     const long long region = cand_region_ints(w.cand_cap);
-    auto enqueue = [&](int level) -> cudaError_t {
+    auto enqueue_on = [&](int level, cudaStream_t s) -> cudaError_t {
         // level 1 compacts the full matrix; later levels only shrink the previous lists;
         // (re)compaction writes the level's edge list; the row prefix is only needed by
         // the shared-memory kernel of levels above GCSL_GAUSS_REG_LEVELS
@@ -474,7 +589,35 @@ int gcsl::host::gauss_skeleton_run(const double *C, int p, long long n_obs, cons
         }
         return e;
     };
-    const int rc = run_levels(max_level, w.st, s, words, enqueue);
+    auto enqueue_range = [&](int a, int b) -> cudaError_t {
+        if (lt || allocation_free) {  // timed levels or nothing to create: direct launches
+            for (int l = a; l <= b; ++l) {
+                const cudaError_t e = enqueue_on(l, s);
+                if (e != cudaSuccess) return e;
+            }
+            return cudaSuccess;
+        }
+        LevelGraphKey key;
+        std::memset(&key, 0, sizeof(key));
+        key.ws = workspace;
+        key.C = C;
+        key.G = G;
+        key.sep = sepsets;
+        key.rec = rec_pool;
+        key.rec_cap = rec_cap;
+        key.p = p;
+        key.max_level = max_level;
+        key.a = a;
+        key.b = b;
+        key.n_thr = n_thresholds;
+        key.mixed = mixed;
+        key.chunked = !chunking_off();
+        key.sms = sms;
+        const int t_end = std::min(b + 1, n_thresholds);
+        key.thr_hash = a < t_end ? fnv1a(thresholds + a, sizeof(double) * (size_t)(t_end - a)) : 0ull;
+        return launch_level_batch(key, s, ss ? ss->stream : nullptr, enqueue_on);
+    };
+    const int rc = run_levels(max_level, w.st, s, words, enqueue_range);
     if (joiner.join() != cudaSuccess) return GCSL_ERR_DEVICE;
     if (rc != GCSL_OK) return rc;
     if (host::launch_pmax(w.kept, w.st, w.zmin, w.r2min, p, n_obs, w.sftab, pmax, sms, s) != cudaSuccess)
@@ -610,7 +753,7 @@ int gcsl_disc_skeleton(const uint8_t *data, int64_t ld, int64_t n, int32_t p, co
     if (host::launch_disc_tests(A, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;
     HostCtl *hc = host_ctl();
     if (!hc) return GCSL_ERR_DEVICE;
-    int rc = run_levels(max_level, w.st, s, hc->words, [&](int level) -> cudaError_t {
+    auto disc_level = [&](int level) -> cudaError_t {
         cudaError_t e2 = host::launch_compact(G, p, w.adj, nullptr, w.st, level, nullptr, s);
         if (e2 == cudaSuccess) e2 = host::launch_disc_weights(w.adj, p, level, w.weights, w.st, s);
         if (e2 == cudaSuccess) e2 = host::launch_scan_ll(w.weights, p, w.prefix, w.st, s);
@@ -623,6 +766,13 @@ int gcsl_disc_skeleton(const uint8_t *data, int64_t ld, int64_t n, int32_t p, co
             e2 = host::launch_disc_finalize(w.adj, p, level, G, w.win, sepsets, max_level, rec_pool, rec_cap, w.st,
                                             sms, s);
         return e2;
+    };
+    int rc = run_levels(max_level, w.st, s, hc->words, [&](int a, int b) -> cudaError_t {
+        for (int level = a; level <= b; ++level) {
+            const cudaError_t e2 = disc_level(level);
+            if (e2 != cudaSuccess) return e2;
+        }
+        return cudaSuccess;
     });
     if (rc != GCSL_OK) return rc;
     if (host::launch_pmax_finish(pmax, p, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;

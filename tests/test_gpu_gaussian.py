@@ -114,6 +114,31 @@ def test_determinism_repeat(cuda):
         assert np.array_equal(o[2], outs[0][2])
 
 
+def test_repeated_solves_replay_level_graphs(cuda):
+    """Repeated solves of one solver: the first launches its level batches directly, the
+    second captures them into CUDA graphs, later ones replay the graphs.  Every solve
+    gives the oracle's skeleton, sepsets, test counts and pmax, and a replayed solve
+    launches the same kernels as a direct one (counted per graph replay)."""
+    from gpucsl_gb300 import _lib, engine
+
+    torch = cuda
+    w = gaussian_dag_data(400, 5000, 4, 37)
+    C = og.corrcoef(w.data)
+    ref = og.skeleton(C, 5000, 0.01, 398)
+    Cg = torch.from_numpy(C).cuda()
+    thr = og.thresholds(5000, 0.01)
+    s = engine.GaussianSolver(400, 398)
+    L = _lib.lib()
+    counts = []
+    for _ in range(4):
+        k0 = int(L.gcsl_kernel_launches())
+        st = s.run(Cg, 5000, thr)
+        counts.append(int(L.gcsl_kernel_launches()) - k0)
+        G, sep, pmax = s.to_host()
+        assert_parity(G, sep, pmax, st, ref)
+    assert counts[2] == counts[0] and counts[3] == counts[0], counts
+
+
 def test_edge_cases(cuda):
     # two variables, max_level 0 (sepsets of shape (p, p, 0))
     w = gaussian_dag_data(2, 100, 1, 3)
