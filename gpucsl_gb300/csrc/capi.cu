@@ -198,7 +198,8 @@ SideStream *side_stream() {
 // matrix, outputs, thresholds and level range, as in repeated solves of one solver --
 // it is captured once into a CUDA graph (its side-stream candidate kernels joined back
 // at the end of the batch) and replayed by one launch.  A batch seen once, the level
-// timers and the allocation-free path launch directly.
+// timers and the allocation-free path launch directly; so does everything unless
+// GCSL_LEVEL_GRAPHS=1 (see graphs_off).
 struct LevelGraphKey {
     const void *ws;
     const double *C;
@@ -236,10 +237,13 @@ LevelGraphCache *level_graph_cache() {
     return &c;
 }
 
+// Level-batch graphs are used with GCSL_LEVEL_GRAPHS=1 (measured on the p = 1000,
+// n = 10000 solve: the replayed batches were no faster than the programmatic-dependent
+// launches, whose prologues overlap the previous kernel).
 bool graphs_off() {
     static const bool off = [] {
         const char *e = getenv("GCSL_LEVEL_GRAPHS");
-        return e && e[0] == '0';
+        return !(e && e[0] == '1');
     }();
     return off;
 }

@@ -79,9 +79,20 @@ __global__ void row_scan_kernel(const T *__restrict__ cnt, int p, long long *__r
 
 // Level kernel of level L (1 <= L <= GCSL_GAUSS_REG_LEVELS): the edge phase over one
 // resident wave of warps.  The unit kernel follows it when edges are chunked.
+//
+// Edges only shrink from level to level, so the previous level's edge count bounds this
+// one's.  It was written by the (re)compaction of level L - 1, three or more kernels
+// before this one: every kernel of the loop waits for its predecessor before it lets its
+// successor start, so that compaction has completed when this kernel starts and the
+// count can be read before the wait.  Blocks beyond the bound leave before loading the
+// binomial rows (the upper levels keep a few hundred edges, and the grid is sized for
+// the thousands of level 1); block 0 always stays, it records the end of the loop.
 template <int L, bool MIXED>
 __global__ void __launch_bounds__(256) gauss_level_reg_kernel(LevelCtx x) {
     __shared__ BinomRows sb;
+    if (L >= 2 && blockIdx.x > 0 &&
+        (long long)blockIdx.x * (blockDim.x >> 5) >= (long long)__ldcg(&x.st->edges[L - 1]))
+        return;
     if (L >= 2) binom_rows_load(sb);  // constant table: before the wait on the previous kernel
     pdl_wait();
     pdl_trigger();
@@ -93,17 +104,23 @@ __global__ void __launch_bounds__(256) gauss_level_reg_kernel(LevelCtx x) {
                                ((long long)gridDim.x * blockDim.x) >> 5);
 }
 
+//
+// The units of a level are known only when the level kernel has finished, and most levels
+// chunk few edges or none: blocks check their share after the wait and only blocks with
+// units load the binomial rows (block 0 always stays, as in the level kernel).
 template <int L, bool MIXED>
 __global__ void __launch_bounds__(256) gauss_level_units_kernel(LevelCtx x) {
     __shared__ BinomRows sb;
-    if (L >= 2) binom_rows_load(sb);  // constant table: before the wait on the level kernel
     pdl_wait();
     pdl_trigger();
-    if (L >= 2) __syncthreads();
     if (!level_active(x.st, L, x.tau_valid)) return;
     const long long reserved = (long long)x.st->units[L];
     const long long nu = reserved < x.ck.unit_cap ? reserved : x.ck.unit_cap;
     if ((long long)blockIdx.x * (blockDim.x >> 5) >= nu) return;
+    if (L >= 2) {
+        binom_rows_load(sb);
+        __syncthreads();
+    }
     level_unit_phase<L, MIXED>(x, L >= 2 ? &sb : nullptr, ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
                                ((long long)gridDim.x * blockDim.x) >> 5);
 }

@@ -115,10 +115,11 @@ def test_determinism_repeat(cuda):
 
 
 def test_repeated_solves_replay_level_graphs(cuda):
-    """Repeated solves of one solver: the first launches its level batches directly, the
-    second captures them into CUDA graphs, later ones replay the graphs.  Every solve
-    gives the oracle's skeleton, sepsets, test counts and pmax, and a replayed solve
-    launches the same kernels as a direct one (counted per graph replay)."""
+    """Repeated solves of one solver.  With GCSL_LEVEL_GRAPHS=1 the first launches its
+    level batches directly, the second captures them into CUDA graphs and later ones
+    replay the graphs (run by test_level_graphs_in_a_subprocess); without it every solve
+    launches directly.  Every solve gives the oracle's skeleton, sepsets, test counts and
+    pmax, and launches the same number of kernels (graph replays counted per kernel)."""
     from gpucsl_gb300 import _lib, engine
 
     torch = cuda
@@ -127,7 +128,7 @@ def test_repeated_solves_replay_level_graphs(cuda):
     ref = og.skeleton(C, 5000, 0.01, 398)
     Cg = torch.from_numpy(C).cuda()
     thr = og.thresholds(5000, 0.01)
-    s = engine.GaussianSolver(400, 398)
+    s = engine.GaussianSolver(400, 398, record_cap=400 * 400 * 4)  # no pool growth between solves
     L = _lib.lib()
     counts = []
     for _ in range(4):
@@ -137,6 +138,22 @@ def test_repeated_solves_replay_level_graphs(cuda):
         G, sep, pmax = s.to_host()
         assert_parity(G, sep, pmax, st, ref)
     assert counts[2] == counts[0] and counts[3] == counts[0], counts
+
+
+def test_level_graphs_in_a_subprocess(cuda):
+    """The repeated-solve test above with level-batch graphs switched on (the switch is
+    read once per process)."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    here = Path(__file__).resolve()
+    env = dict(os.environ, GCSL_LEVEL_GRAPHS="1")
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-p", "no:cacheprovider", "-m", "gpu",
+                        f"{here}::test_repeated_solves_replay_level_graphs"], capture_output=True, text=True,
+                       env=env, cwd=here.parents[1], timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
 
 
 def test_edge_cases(cuda):
