@@ -484,33 +484,54 @@ def batched_leg(reps: int = 10, world: int = 1, rank: int = 0) -> dict:
 
 
 # ------------------------------------------------------------ serving leg
-SERVE_COUNT, SERVE_RATES = 64, (10.0, 40.0, 160.0, 320.0, 640.0, 1280.0)
+SERVE_COUNT, SERVE_RATES = 256, (20.0, 80.0, 320.0, 640.0, 1280.0)
 
 
-def serving_leg() -> dict:
+def serving_leg(world: int = 1, rank: int = 0) -> dict:
     """Poisson arrivals of a 70 % Gaussian (p log-uniform 20..2000, n 1000..50000, FP32
     samples, alpha 0.01) / 30 % discrete (p 20..300, n 10000..100000, cardinality 2..6,
-    alpha 0.05) request mix, levels <= 3, 120 GB admission budget: latency from arrival
-    to results on the host through the continuous-batching server and through the plain
-    one-request-at-a-time path, on the same trace, rate swept until the server saturates."""
-    from gpucsl_gb300.serve import SkeletonServer, latency_summary, serve_plain
-    from gpucsl_gb300.synthetic import poisson_arrivals, serving_requests
+    alpha 0.05) request mix, levels <= 3, 120 GB admission budget, 256 requests per rate:
+    latency from arrival to results on the host through the continuous-batching server
+    and through the plain one-request-at-a-time path, on the same trace, rate swept until
+    the server saturates.  Under N ranks each rank serves its footprint-balanced share of
+    the trace (arrival times kept); latencies are pooled over ranks and throughput is all
+    responses over the longest span."""
+    from gpucsl_gb300.serve import Response, SkeletonServer, latency_summary, serve_plain
+    from gpucsl_gb300.shard import discrete_cost, gaussian_cost, my_shard
+    from gpucsl_gb300.synthetic import poisson_arrivals, serving_requests, serving_sizes
 
-    reqs = serving_requests(SERVE_COUNT, seed=7)
-    warm = poisson_arrivals(reqs[:6], rate=1e9)
+    sizes = serving_sizes(SERVE_COUNT, seed=7)
+    costs = [gaussian_cost(p, n) if kind == "gaussian" else discrete_cost(p, n) for kind, p, n in sizes]
+    mine = my_shard(costs, world, rank)
+    t0 = time.perf_counter()
+    reqs = serving_requests(SERVE_COUNT, seed=7, only=mine)
+    gen_s = time.perf_counter() - t0
+    warm = poisson_arrivals(reqs[:8], rate=1e9, count=SERVE_COUNT)
     SkeletonServer(120e9).serve(warm)
     serve_plain(warm)
+
+    def pooled(resp):
+        # (kind, arrival, done, batch) of every rank's responses; done / arrival share a clock
+        # per rank, so latencies and spans stay per rank and only the lists are pooled
+        rows = gather_lists([(r.kind, r.arrival, r.done, r.batch) for r in resp], world)
+        fake = [Response(0, k, None, None, None, a, a, d, b) for k, a, d, b in rows]
+        return latency_summary(fake)
+
     rows = []
     for rate in SERVE_RATES:
-        tr = poisson_arrivals(reqs, rate=rate, seed=11)
-        srv = latency_summary(SkeletonServer(120e9).serve(tr))
-        pln = latency_summary(serve_plain(tr))
+        tr = poisson_arrivals(reqs, rate=rate, seed=11, count=SERVE_COUNT)
+        barrier(world)
+        srv = pooled(SkeletonServer(120e9).serve(tr))
+        barrier(world)
+        pln = pooled(serve_plain(tr))
         rows.append({"rate_per_s": rate, "server": srv, "plain": pln})
         if srv["skeletons_per_s"] is not None and srv["skeletons_per_s"] < 0.6 * rate:
             break  # saturated
-    n_g = sum(1 for r in reqs if r.kind == "gaussian")
+    n_g = sum(1 for kind, _, _ in sizes if kind == "gaussian")
     return {"workload": f"serving_{SERVE_COUNT}_requests_gauss{n_g}_disc{SERVE_COUNT - n_g}_L3_budget120GB",
-            "unit": "ms (latency), skeletons/s", "data": "synthetic (seeded per request)", "sweep": rows}
+            "unit": "ms (latency), skeletons/s", "data": "synthetic (seeded per request; discrete samples drawn "
+            "and ordinal-encoded on the device)", "ranks": world, "requests_per_rank": len(mine),
+            "payload_generation_s_rank0": round(gen_s, 2), "sweep": rows}
 
 
 # ------------------------------------------------------------------ our arm
@@ -691,13 +712,15 @@ def run_ours(args, world, rank, local):
     if not args.no_extras and rank == 0:
         out["e2e_api"] = e2e_api_leg(w.data, solver, E, levels_run)
 
-    # ---- batched instances (split precision and FP64) against the plain per-instance path
-    if not args.no_extras and rank == 0:
-        out["batched"] = batched_leg()
+    # ---- batched instances (split precision and FP64) against the plain per-instance path;
+    # under N ranks every rank solves its share of the instances (replicas)
+    if not args.no_extras:
+        out["batched"] = batched_leg(world=world, rank=rank)
 
-    # ---- serving: continuous batching under Poisson arrivals against the plain path
-    if not args.no_extras and rank == 0:
-        out["serving"] = serving_leg()
+    # ---- serving: continuous batching under Poisson arrivals against the plain path; every
+    # rank serves its share of the trace
+    if not args.no_extras:
+        out["serving"] = serving_leg(world=world, rank=rank)
 
     # ---- edge orientation of this workload's skeleton on the GPU; the CPU-baseline leg
     # below checks its CPDAG against the reference's sequential algorithm (the oracle)
@@ -893,8 +916,9 @@ def main():
 
         gbuild.build()
         torch.cuda.set_device(local)
-        leg = batched_leg() if args.batched_only else serving_leg()
-        print(json.dumps({"batched" if args.batched_only else "serving": leg}), flush=True)
+        leg = batched_leg(world=world, rank=rank) if args.batched_only else serving_leg(world=world, rank=rank)
+        if rank == 0:
+            print(json.dumps({"batched" if args.batched_only else "serving": leg}), flush=True)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

@@ -40,7 +40,8 @@ EXPORTED = [
     "gcsl_gauss_batch_collect", "gcsl_gauss_batch_set_lanes",
     "gcsl_corr_tc_batch_workspace_bytes", "gcsl_corr_tc_batch_prepare", "gcsl_corr_tc_batch_run",
     "gcsl_corr_tc_batch_run_split", "gcsl_corr_tc_batch_run_flagged", "gcsl_gauss_batch_rerun",
-    "gcsl_gauss_batch_flags",
+    "gcsl_gauss_batch_flags", "gcsl_gauss_state_bytes", "gcsl_gauss_batch_table_bytes",
+    "gcsl_gauss_batch_prepare_staged", "gcsl_gauss_batch_step", "gcsl_records_to_dense",
     "gcsl_orient_workspace_bytes", "gcsl_orient_edges", "gcsl_encode_workspace_bytes", "gcsl_ordinal_encode",
     "gcsl_set_test_precision",
 ]
@@ -94,6 +95,7 @@ class GaussInstance(ct.Structure):
         ("rec_pool", ct.c_void_p),
         ("rec_cap", ct.c_int64),
         ("c_err", ct.c_void_p),
+        ("state", ct.c_void_p),
         ("status", ct.c_int32),
         ("levels_run", ct.c_int32),
         ("n_records", ct.c_int64),
@@ -203,6 +205,17 @@ def lib() -> ct.CDLL:
     L.gcsl_gauss_batch_rerun.argtypes = [ct.POINTER(BatchPlan), _vp]
     L.gcsl_gauss_batch_flags.restype = _vp
     L.gcsl_gauss_batch_flags.argtypes = [ct.POINTER(BatchPlan)]
+    L.gcsl_gauss_state_bytes.restype = _sz
+    L.gcsl_gauss_state_bytes.argtypes = [_i32]
+    L.gcsl_gauss_batch_table_bytes.restype = _sz
+    L.gcsl_gauss_batch_table_bytes.argtypes = [_i32]
+    L.gcsl_gauss_batch_prepare_staged.restype = ct.c_int
+    L.gcsl_gauss_batch_prepare_staged.argtypes = [ct.POINTER(GaussInstance), _i32, _i32, _i32, _vp, _sz, _vp, _sz,
+                                                  ct.POINTER(BatchPlan), _vp]
+    L.gcsl_gauss_batch_step.restype = ct.c_int
+    L.gcsl_gauss_batch_step.argtypes = [ct.POINTER(BatchPlan), _i32, _i32, _i32, _vp, _vp]
+    L.gcsl_records_to_dense.restype = ct.c_int
+    L.gcsl_records_to_dense.argtypes = [_vp, _i64, _i32, _i32, _vp]
     L.gcsl_set_test_precision.restype = ct.c_int
     L.gcsl_set_test_precision.argtypes = [_i32]
     L.gcsl_encode_workspace_bytes.restype = _sz

@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -82,6 +83,13 @@ int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level,
                         size_t ws_bytes, long long *plan, int sms, cudaStream_t s);
 int gauss_batch_set_lanes(long long *plan, int level, int lanes);
 int gauss_batch_run(const long long *plan, cudaStream_t s, bool rerun);
+int gauss_batch_step(const long long *plan, int first, int last, bool finish, bool rerun, int32_t *host_status,
+                     cudaStream_t s);
+int gauss_batch_prepare_staged(const gcsl_gauss_instance *in, int count, int max_level, int precision, void *ws,
+                               size_t ws_bytes, void *stage, size_t stage_bytes, long long *plan, int sms,
+                               cudaStream_t s);
+size_t gauss_state_bytes(int p);
+size_t gauss_batch_table_bytes(int count);
 const int *gauss_batch_flags(const long long *plan);
 cudaError_t corr_tc_batch_run_mode(void *ws, int count, const long long *stage_totals, int dtype, int mode,
                                    double *c_err, const int *active, cudaStream_t s);
@@ -852,6 +860,78 @@ int gcsl_gauss_batch_run(const gcsl_batch_plan *plan, void *stream) {
     if (!plan) return GCSL_ERR_INVALID_ARG;
     return host::gauss_batch_run(reinterpret_cast<const long long *>(plan->w), static_cast<cudaStream_t>(stream),
                                  false);
+}
+
+size_t gcsl_gauss_state_bytes(int32_t p) { return (p < 1 || p > GCSL_GAUSS_MAX_P) ? 0 : host::gauss_state_bytes(p); }
+
+size_t gcsl_gauss_batch_table_bytes(int32_t count) { return count < 1 ? 0 : host::gauss_batch_table_bytes(count); }
+
+static int check_instances(const gcsl_gauss_instance *inst, int32_t count, int32_t max_level, int32_t precision) {
+    if (!inst || count < 1 || max_level < 0 || max_level > GCSL_BATCH_MAX_LEVEL ||
+        (precision != GCSL_PREC_F64 && precision != GCSL_PREC_SPLIT))
+        return GCSL_ERR_INVALID_ARG;
+    for (int k = 0; k < count; ++k) {
+        const gcsl_gauss_instance &I = inst[k];
+        if (!I.C || !I.G || !I.pmax || I.p < 1 || I.n_obs < 4 || !I.thresholds || I.n_thresholds < 1)
+            return GCSL_ERR_INVALID_ARG;
+        if (I.p > GCSL_GAUSS_MAX_P) return GCSL_ERR_UNSUPPORTED;
+        if (precision == GCSL_PREC_SPLIT && (!I.C32 || !I.band_lo || !I.band_hi)) return GCSL_ERR_INVALID_ARG;
+        if (I.state != nullptr && reinterpret_cast<uintptr_t>(I.state) % 256 != 0) return GCSL_ERR_INVALID_ARG;
+    }
+    return GCSL_OK;
+}
+
+int gcsl_gauss_batch_prepare_staged(const gcsl_gauss_instance *inst, int32_t count, int32_t max_level,
+                                    int32_t precision, void *workspace, size_t workspace_bytes, void *stage,
+                                    size_t stage_bytes, gcsl_batch_plan *plan, void *stream) {
+    if (!plan || !workspace || !stage) return GCSL_ERR_INVALID_ARG;
+    const int rc = check_instances(inst, count, max_level, precision);
+    if (rc != GCSL_OK) return rc;
+    return host::gauss_batch_prepare_staged(inst, count, max_level, precision, workspace, workspace_bytes, stage,
+                                            stage_bytes, reinterpret_cast<long long *>(plan->w), device_sms(),
+                                            static_cast<cudaStream_t>(stream));
+}
+
+int gcsl_gauss_batch_step(const gcsl_batch_plan *plan, int32_t first_level, int32_t last_level, int32_t finish,
+                          int32_t *host_status, void *stream) {
+    if (!plan || first_level < 0 || last_level > GCSL_BATCH_MAX_LEVEL) return GCSL_ERR_INVALID_ARG;
+    return host::gauss_batch_step(reinterpret_cast<const long long *>(plan->w), first_level, last_level, finish != 0,
+                                  false, host_status, static_cast<cudaStream_t>(stream));
+}
+
+int gcsl_records_to_dense(const int32_t *rec, int64_t n_ints, int32_t p, int32_t max_level, int32_t *out) {
+    if (n_ints < 0 || p < 1 || max_level < 0 || (!rec && n_ints > 0) || (!out && max_level > 0))
+        return GCSL_ERR_INVALID_ARG;
+    const size_t total = (size_t)p * p * (size_t)max_level;
+    if (total == 0) return GCSL_OK;
+    // the -1 fill is the bulk of the work for large p: split it over a few threads
+    const size_t chunk = (size_t)1 << 22;
+    const int nt = (int)std::min<size_t>(8, (total + chunk - 1) / chunk);
+    if (nt > 1) {
+        std::vector<std::thread> th;
+        const size_t per = (total + nt - 1) / nt;
+        for (int t = 0; t < nt; ++t)
+            th.emplace_back([=] {
+                const size_t a = (size_t)t * per, b = std::min(total, a + per);
+                if (a < b) std::fill(out + a, out + b, -1);
+            });
+        for (auto &x : th) x.join();
+    } else {
+        std::fill(out, out + total, -1);
+    }
+    int64_t k = 0;
+    while (k < n_ints) {
+        if (k + 3 > n_ints) return GCSL_ERR_INVALID_ARG;
+        const int lo = rec[k], hi = rec[k + 1], lev = rec[k + 2];
+        if (lev < 0 || k + 3 + lev > n_ints || lo < 0 || lo >= p || hi < 0 || hi >= p) return GCSL_ERR_INVALID_ARG;
+        if (lev <= max_level) {
+            int32_t *a = out + ((size_t)lo * p + hi) * max_level;
+            int32_t *b = out + ((size_t)hi * p + lo) * max_level;
+            for (int c = 0; c < lev; ++c) a[c] = b[c] = rec[k + 3 + c];
+        }
+        k += 3 + lev;
+    }
+    return GCSL_OK;
 }
 
 int gcsl_gauss_batch_rerun(const gcsl_batch_plan *plan, void *stream) {

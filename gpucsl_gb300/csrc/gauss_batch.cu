@@ -455,13 +455,29 @@ __global__ void batch_pmax_kept_kernel(const BInst *__restrict__ inst, const dou
     }
 }
 
+// The erfc table of the pmax kernels (a plan whose step finishes without its own init).
+__global__ void batch_sftab_kernel(double *__restrict__ sftab) {
+    sf_table_build(reinterpret_cast<double (*)[SF_TERMS]>(sftab));
+}
+
+// [done, last level run, status, record ints] per instance.
+__global__ void batch_status_kernel(const BInst *__restrict__ inst, int count, int *__restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const DevState *st = inst[k].st;
+    out[4 * k] = *(volatile const int *)&st->done;
+    out[4 * k + 1] = *(volatile const int *)&st->last_level;
+    out[4 * k + 2] = *(volatile const int *)&st->status;
+    out[4 * k + 3] = (int)*(volatile const unsigned long long *)&st->n_rec_ints;
+}
+
 // ---------------------------------------------------------------------- host
 namespace host {
 
 namespace {
 
 struct BatchLayout {
-    size_t table, off_tiles, off_rows, off_p2, edges, edge_off, sftab, flags, slices, total;
+    size_t table, off_tiles, off_rows, off_p2, edges, edge_off, sftab, flags, status, slices, total;
 };
 
 size_t al(size_t x) { return (x + 255) / 256 * 256; }
@@ -492,15 +508,18 @@ BatchLayout layout(const int *p, int count) {
     off += al((size_t)SF_CENTRES * SF_TERMS * sizeof(double));
     L.flags = off;
     off += al((size_t)count * sizeof(int));
+    L.status = off;
+    off += al((size_t)count * 4 * sizeof(int));
     L.slices = off;
-    for (int k = 0; k < count; ++k) off += slice_bytes(p[k]);
+    if (p)  // p == nullptr: every instance brings its own state slice
+        for (int k = 0; k < count; ++k) off += slice_bytes(p[k]);
     L.total = off;
     return L;
 }
 
 // plan words
 enum {
-    PW_MAGIC = 0, PW_WS, PW_COUNT, PW_MAXL, PW_PREC, PW_TILES, PW_ROWS, PW_P2, PW_SMS, PW_FLAGS,
+    PW_MAGIC = 0, PW_WS, PW_COUNT, PW_MAXL, PW_PREC, PW_TILES, PW_ROWS, PW_P2, PW_SMS, PW_FLAGS, PW_STATUS,
     PW_LANES  // PW_LANES + level, up to PW_LANES + BATCH_MAX_LEVEL (< 48 plan words)
 };
 static_assert(PW_LANES + BATCH_MAX_LEVEL < 48, "plan words");
@@ -533,25 +552,21 @@ cudaError_t launch_level(int L, int lanes, const BInst *inst, const long long *e
     return cudaGetLastError();
 }
 
-}  // namespace
-
-size_t gauss_batch_workspace_bytes(const int *p, int count) { return layout(p, count).total; }
-
-// Builds the instance table on the host and uploads it with the offset arrays
-// (synchronous: outside any stream capture).  thresholds / band arrays are host arrays.
-int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level, int precision, void *ws,
-                        size_t ws_bytes, long long *plan, int sms, cudaStream_t s) {
-    std::vector<int> ps((size_t)count);
-    for (int k = 0; k < count; ++k) ps[(size_t)k] = in[k].p;
-    const BatchLayout Ly = layout(ps.data(), count);
-    if (ws_bytes < Ly.total) return GCSL_ERR_WORKSPACE;
-    char *base = static_cast<char *>(ws);
-    std::vector<BInst> tab((size_t)count);
-    std::vector<long long> ot((size_t)count + 1, 0), orow((size_t)count + 1, 0), op2((size_t)count + 1, 0);
+// Builds the instance table and offset arrays in host memory laid out as the device
+// header [table | tiles | rows | p^2 chunks] (at `hdr`, Ly.edges bytes).  Instances with
+// a state pointer keep their solve state there (it persists across plans and calls);
+// the others get a slice of the workspace.  Returns the totals through the plan words.
+int build_header(const gcsl_gauss_instance *in, int count, int max_level, int precision, char *base,
+                 const BatchLayout &Ly, char *hdr, long long *plan, int sms) {
+    BInst *tab = reinterpret_cast<BInst *>(hdr + Ly.table);
+    long long *ot = reinterpret_cast<long long *>(hdr + Ly.off_tiles);
+    long long *orow = reinterpret_cast<long long *>(hdr + Ly.off_rows);
+    long long *op2 = reinterpret_cast<long long *>(hdr + Ly.off_p2);
+    ot[0] = orow[0] = op2[0] = 0;
     size_t cur = Ly.slices;
     for (int k = 0; k < count; ++k) {
         const gcsl_gauss_instance &X = in[k];
-        BInst &I = tab[(size_t)k];
+        BInst &I = tab[k];
         std::memset(&I, 0, sizeof(I));
         const int p = X.p;
         const size_t pp = (size_t)p * p;
@@ -567,7 +582,8 @@ int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level,
         I.p = p;
         I.n_thr = X.n_thresholds;
         I.sqrt_nm3 = std::sqrt((double)(X.n_obs - 3));
-        char *c = base + cur;
+        char *c = X.state != nullptr ? static_cast<char *>(X.state) : base + cur;
+        if (X.state == nullptr) cur += slice_bytes(p);
         I.st = reinterpret_cast<DevState *>(c);
         c += al(sizeof(DevState));
         I.adj = reinterpret_cast<int *>(c);
@@ -581,7 +597,6 @@ int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level,
         I.r2min = reinterpret_cast<double *>(c);
         c += al(pp * sizeof(double));
         I.kept = reinterpret_cast<int *>(c);
-        cur += slice_bytes(p);
         for (int l = 0; l <= BATCH_MAX_LEVEL; ++l) {
             const double tau = l < X.n_thresholds ? X.thresholds[l] : 0.0;
             const double t = std::tanh(tau);
@@ -597,37 +612,83 @@ int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level,
             }
         }
         const long long nb = (p + 31) / 32;
-        ot[(size_t)k + 1] = ot[(size_t)k] + nb * (nb + 1) / 2;
-        orow[(size_t)k + 1] = orow[(size_t)k] + p;
-        op2[(size_t)k + 1] = op2[(size_t)k] + ((long long)pp + BATCH_P2_CHUNK - 1) / BATCH_P2_CHUNK;
+        ot[k + 1] = ot[k] + nb * (nb + 1) / 2;
+        orow[k + 1] = orow[k] + p;
+        op2[k + 1] = op2[k] + ((long long)pp + BATCH_P2_CHUNK - 1) / BATCH_P2_CHUNK;
     }
-    if (ot[(size_t)count] > 0x7fffffffll || op2[(size_t)count] > 0x7fffffffll) return GCSL_ERR_UNSUPPORTED;
-    cudaError_t e = cudaMemcpyAsync(base + Ly.table, tab.data(), tab.size() * sizeof(BInst), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(base + Ly.off_tiles, ot.data(), ot.size() * sizeof(long long), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(base + Ly.off_rows, orow.data(), orow.size() * sizeof(long long), cudaMemcpyHostToDevice,
-                            s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(base + Ly.off_p2, op2.data(), op2.size() * sizeof(long long), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(base + Ly.flags, 0, (size_t)count * sizeof(int), s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host vectors die with this call
-    if (e != cudaSuccess) return GCSL_ERR_DEVICE;
+    if (ot[count] > 0x7fffffffll || op2[count] > 0x7fffffffll) return GCSL_ERR_UNSUPPORTED;
     std::memset(plan, 0, sizeof(long long) * 48);
     plan[PW_MAGIC] = PLAN_MAGIC;
-    plan[PW_WS] = (long long)reinterpret_cast<uintptr_t>(ws);
+    plan[PW_WS] = (long long)reinterpret_cast<uintptr_t>(base);
     plan[PW_COUNT] = count;
     plan[PW_MAXL] = max_level;
     plan[PW_PREC] = precision;
-    plan[PW_TILES] = ot[(size_t)count];
-    plan[PW_ROWS] = orow[(size_t)count];
-    plan[PW_P2] = op2[(size_t)count];
+    plan[PW_TILES] = ot[count];
+    plan[PW_ROWS] = orow[count];
+    plan[PW_P2] = op2[count];
     plan[PW_SMS] = sms;
     for (int l = 0; l <= BATCH_MAX_LEVEL; ++l) plan[PW_LANES + l] = 32;
     plan[PW_FLAGS] = (long long)reinterpret_cast<uintptr_t>(base + Ly.flags);
+    plan[PW_STATUS] = (long long)reinterpret_cast<uintptr_t>(base + Ly.status);
     return GCSL_OK;
 }
 
+BatchLayout layout_for(const gcsl_gauss_instance *in, int count) {
+    std::vector<int> ps;
+    for (int k = 0; k < count; ++k)
+        if (in[k].state == nullptr) ps.push_back(in[k].p);
+    BatchLayout Ly = layout(nullptr, count);
+    for (int p : ps) Ly.total += slice_bytes(p);
+    return Ly;
+}
+
+}  // namespace
+
+size_t gauss_batch_workspace_bytes(const int *p, int count) { return layout(p, count).total; }
+
+size_t gauss_state_bytes(int p) { return slice_bytes(p); }
+
+size_t gauss_batch_table_bytes(int count) { return layout(nullptr, count).total; }
+
+// Builds the instance table on the host and uploads it with the offset arrays
+// (synchronous: outside any stream capture).  thresholds / band arrays are host arrays.
+int gauss_batch_prepare(const gcsl_gauss_instance *in, int count, int max_level, int precision, void *ws,
+                        size_t ws_bytes, long long *plan, int sms, cudaStream_t s) {
+    const BatchLayout Ly = layout_for(in, count);
+    if (ws_bytes < Ly.total) return GCSL_ERR_WORKSPACE;
+    char *base = static_cast<char *>(ws);
+    std::vector<char> hdr(Ly.edges);
+    const int rc = build_header(in, count, max_level, precision, base, Ly, hdr.data(), plan, sms);
+    if (rc != GCSL_OK) return rc;
+    cudaError_t e = cudaMemcpyAsync(base, hdr.data(), hdr.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(base + Ly.flags, 0, (size_t)count * sizeof(int), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host vector dies with this call
+    if (e != cudaSuccess) {
+        plan[PW_MAGIC] = 0;
+        return GCSL_ERR_DEVICE;
+    }
+    return GCSL_OK;
+}
+
+// The same without a synchronisation: the header is built in the caller's host buffer
+// `stage` (pinned, gcsl_gauss_batch_table_bytes(count) bytes), which must stay untouched
+// until the stream has passed the copy enqueued here.
+int gauss_batch_prepare_staged(const gcsl_gauss_instance *in, int count, int max_level, int precision, void *ws,
+                               size_t ws_bytes, void *stage, size_t stage_bytes, long long *plan, int sms,
+                               cudaStream_t s) {
+    const BatchLayout Ly = layout_for(in, count);
+    if (ws_bytes < Ly.total || stage_bytes < Ly.edges) return GCSL_ERR_WORKSPACE;
+    char *base = static_cast<char *>(ws);
+    const int rc = build_header(in, count, max_level, precision, base, Ly, static_cast<char *>(stage), plan, sms);
+    if (rc != GCSL_OK) return rc;
+    cudaError_t e = cudaMemcpyAsync(base, stage, Ly.edges, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(base + Ly.flags, 0, (size_t)count * sizeof(int), s);
+    if (e != cudaSuccess) {
+        plan[PW_MAGIC] = 0;
+        return GCSL_ERR_DEVICE;
+    }
+    return GCSL_OK;
+}
 
 bool gauss_batch_plan_ok(const long long *plan) { return plan && plan[PW_MAGIC] == PLAN_MAGIC; }
 
@@ -642,22 +703,18 @@ int gauss_batch_set_lanes(long long *plan, int level, int lanes) {
     return GCSL_OK;
 }
 
-// Enqueues the whole batch: init, level 0, levels 1..max_level, pmax.  No host reads:
-// the sequence can be captured into a CUDA graph.  With rerun set only the flagged
-// instances are solved (again), with the test of an exact C.
-int gauss_batch_run(const long long *plan, cudaStream_t s, bool rerun) {
+// Enqueues levels first..last (first == 0: the state reset and level 0 as well) of every
+// instance of the plan, then, with finish, the pmax write-back.  Levels run in order per
+// instance across calls (its state lives in its slice); an instance whose loop has ended
+// skips the rest on the device.  host_status (pinned, 4 ints per instance) receives
+// [done, last level run, status, sepset record ints] of every instance after the step.
+int gauss_batch_step(const long long *plan, int first, int last, bool finish, bool rerun, int32_t *host_status,
+                     cudaStream_t s) {
     if (!gauss_batch_plan_ok(plan)) return GCSL_ERR_INVALID_ARG;
     char *base = reinterpret_cast<char *>(static_cast<uintptr_t>(plan[PW_WS]));
     const int count = (int)plan[PW_COUNT], max_level = (int)plan[PW_MAXL], sms = (int)plan[PW_SMS];
     const bool split = plan[PW_PREC] == GCSL_PREC_SPLIT;
-    BatchLayout Ly;
-    Ly.table = 0;
-    Ly.off_tiles = al((size_t)count * sizeof(BInst));
-    Ly.off_rows = Ly.off_tiles + al(((size_t)count + 1) * sizeof(long long));
-    Ly.off_p2 = Ly.off_rows + al(((size_t)count + 1) * sizeof(long long));
-    Ly.edges = Ly.off_p2 + al(((size_t)count + 1) * sizeof(long long));
-    Ly.edge_off = Ly.edges + al((size_t)count * sizeof(long long));
-    Ly.sftab = Ly.edge_off + al(((size_t)count + 1) * sizeof(long long));
+    const BatchLayout Ly = layout(nullptr, count);
     const BInst *inst = reinterpret_cast<const BInst *>(base + Ly.table);
     const long long *ot = reinterpret_cast<const long long *>(base + Ly.off_tiles);
     const long long *orow = reinterpret_cast<const long long *>(base + Ly.off_rows);
@@ -666,12 +723,14 @@ int gauss_batch_run(const long long *plan, cudaStream_t s, bool rerun) {
     long long *eoff = reinterpret_cast<long long *>(base + Ly.edge_off);
     double *sftab = reinterpret_cast<double *>(base + Ly.sftab);
 
-    batch_init_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count, sftab, rerun);
-    batch_level0_kernel<<<(unsigned)plan[PW_TILES], 256, 0, s>>>(inst, ot, count, rerun);
-    note_launch(2);
+    if (first == 0) {
+        batch_init_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count, sftab, rerun);
+        batch_level0_kernel<<<(unsigned)plan[PW_TILES], 256, 0, s>>>(inst, ot, count, rerun);
+        note_launch(2);
+    }
     const long long rows = plan[PW_ROWS];
     const int cblocks = (int)std::min<long long>((rows + 7) / 8, (long long)sms * 16);
-    for (int level = 1; level <= max_level; ++level) {
+    for (int level = std::max(first, 1); level <= std::min(last, max_level); ++level) {
         batch_compact_kernel<<<cblocks, 256, 0, s>>>(inst, orow, count, level, rerun);
         batch_scan_kernel<<<count, 256, 0, s>>>(inst, count, level, max_level, edges, rerun);
         batch_edge_offsets_kernel<<<1, 1024, 0, s>>>(edges, count, eoff);
@@ -681,10 +740,32 @@ int gauss_batch_run(const long long *plan, cudaStream_t s, bool rerun) {
                                     : launch_level<false>(level, lanes, inst, eoff, count, sms, rerun, s);
         if (e != cudaSuccess) return GCSL_ERR_DEVICE;
     }
-    batch_pmax_removed_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count, sftab, rerun);
-    batch_pmax_kept_kernel<<<count, 256, 0, s>>>(inst, sftab, rerun);
-    note_launch(2);
+    if (finish) {
+        if (first != 0) {  // the erfc table of this plan's header is built by its init kernel
+            batch_sftab_kernel<<<1, 32, 0, s>>>(sftab);
+            note_launch(1);
+        }
+        batch_pmax_removed_kernel<<<(unsigned)plan[PW_P2], 256, 0, s>>>(inst, op2, count, sftab, rerun);
+        batch_pmax_kept_kernel<<<count, 256, 0, s>>>(inst, sftab, rerun);
+        note_launch(2);
+    }
+    if (host_status != nullptr) {
+        int *dev_status = reinterpret_cast<int *>(static_cast<uintptr_t>(plan[PW_STATUS]));
+        batch_status_kernel<<<(count + 127) / 128, 128, 0, s>>>(inst, count, dev_status);
+        note_launch(1);
+        if (cudaMemcpyAsync(host_status, dev_status, (size_t)count * 4 * sizeof(int), cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess)
+            return GCSL_ERR_DEVICE;
+    }
     return cudaGetLastError() == cudaSuccess ? GCSL_OK : GCSL_ERR_DEVICE;
+}
+
+// Enqueues the whole batch: init, level 0, levels 1..max_level, pmax.  No host reads:
+// the sequence can be captured into a CUDA graph.  With rerun set only the flagged
+// instances are solved (again), with the test of an exact C.
+int gauss_batch_run(const long long *plan, cudaStream_t s, bool rerun) {
+    if (!gauss_batch_plan_ok(plan)) return GCSL_ERR_INVALID_ARG;
+    return gauss_batch_step(plan, 0, (int)plan[PW_MAXL], true, rerun, nullptr, s);
 }
 
 // Synchronises the stream and copies every instance's state back into the outputs.

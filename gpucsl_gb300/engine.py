@@ -19,47 +19,15 @@ def _torch():
     return _lib.require_cuda()
 
 
-def record_starts(rec: np.ndarray) -> np.ndarray:
-    """Offsets of the records [lo, hi, level, S...] packed back to back in `rec`.
-
-    A record's successor starts at start + 3 + level; the chain from offset 0 is followed
-    by pointer doubling (log2(len) vectorised rounds) rather than record by record."""
-    n = int(rec.size)
-    if n == 0:
-        return np.zeros(0, np.int64)
-    idx = np.arange(n, dtype=np.int64)
-    lev = np.zeros(n, np.int64)
-    if n > 2:
-        lev[:n - 2] = np.maximum(rec[2:].astype(np.int64), 0)
-    nxt = np.append(np.minimum(idx + 3 + lev, n), n)  # n is the end (a fixed point)
-    reach = np.zeros(n + 1, bool)
-    reach[0] = True
-    span = 1
-    while span < n + 1:
-        reach[nxt[reach]] = True  # every start reached in < 2 * span steps
-        nxt = nxt[nxt]
-        span *= 2
-    return np.nonzero(reach[:n])[0]
-
-
 def records_to_dense(rec: np.ndarray, n_ints: int, p: int, max_level: int) -> np.ndarray:
     """Scatter the int32 sepset records [lo, hi, level, S...] into the reference's dense
-    (p, p, max_level) layout filled with -1 (discover_skeleton_gaussian.py:166-168)."""
-    out = np.full((p, p, max_level), -1, np.int32)
-    rec = np.asarray(rec[:n_ints])
-    starts = record_starts(rec)
-    if starts.size == 0:
-        return out
-    lo, hi, lev = rec[starts], rec[starts + 1], rec[starts + 2]
-    for l in np.unique(lev):
-        l = int(l)
-        if l < 1 or l > max_level:
-            continue
-        sel = starts[lev == l]
-        S = rec[sel[:, None] + 3 + np.arange(l)]
-        a, b = rec[sel], rec[sel + 1]
-        out[a, b, :l] = S
-        out[b, a, :l] = S
+    (p, p, max_level) layout filled with -1 (discover_skeleton_gaussian.py:166-168), by
+    the library's host routine (gcsl_records_to_dense: multi-threaded fill, no GIL)."""
+    out = np.empty((p, p, max_level), np.int32)
+    rec = np.ascontiguousarray(np.asarray(rec[:n_ints], dtype=np.int32))
+    _lib.check(_lib.lib().gcsl_records_to_dense(rec.ctypes.data if n_ints else None, int(n_ints), int(p),
+                                                int(max_level), out.ctypes.data if out.size else None),
+               "gcsl_records_to_dense")
     return out
 
 

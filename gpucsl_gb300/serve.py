@@ -1,25 +1,35 @@
-"""Serving skeleton requests with continuous batching and memory-budget admission.
+"""Serving skeleton requests with continuous batching at level granularity.
 
 Requests (Gaussian: FP32 samples; discrete: ordinal codes and cardinalities) arrive at
 arbitrary times.  A request is admitted once the device memory it needs fits in the
 budget next to the requests in flight (first come, first served: a large request at
-the head waits rather than being overtaken).  Workers own one CUDA stream each:
+the head waits rather than being overtaken).
 
-* the Gaussian workers (two by default) each take every admitted Gaussian request that
-  is waiting when they become free and solve them as one `GaussianBatch` (batched
-  tensor-core correlation + batched level loop), so requests that arrive while a batch
-  runs join the next one; one or two waiting requests go through the single-problem
-  path instead, whose solve is shorter than a batch's setup;
-* the discrete workers (three by default) each take the next admitted discrete request
-  and solve it through `DiscreteSolver`, so discrete solves overlap on the device.
+* Gaussian requests go to one engine thread that owns two CUDA streams.  On the
+  correlation stream an admitted request's samples are copied in and its correlation is
+  computed at once.  On the level stream the engine advances, tick by tick, every
+  request in flight by one level: requests whose correlation is done start (state
+  reset, level 0 and level 1), the others run their next level, and those past their
+  last level get the pmax write-back and their results copied into pinned host memory.
+  The requests due for the same levels form one batched plan per tick
+  (gcsl_gauss_batch_prepare_staged / gcsl_gauss_batch_step); each request keeps its
+  solve state in its own device slice across ticks, so a request that arrives while
+  others are in flight joins at the next tick and a finished one leaves at once.  No
+  host read happens between the levels of a request.
+* Discrete requests go to worker threads, one stream each, which solve them
+  concurrently through the single-problem path.
+* Finished requests are turned into the reference's output arrays (dense sepsets by the
+  library's host routine, outside the GIL) by a pool of finishing threads.
 
 Latency is measured from a request's arrival to the moment its results are on the
 host.  `serve_plain` serves the same trace one request at a time through the plain
 single-problem API, for comparison.  Results of a request do not depend on what it was
-batched with (each instance of a batch keeps its own state).
+batched with (each instance keeps its own state).
 """
 from __future__ import annotations
 
+import concurrent.futures as cf
+import ctypes as ct
 import threading
 import time
 from collections import deque
@@ -28,7 +38,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from .engine import DiscreteSolver, GaussianSolver, correlation, gaussian_thresholds
+from .engine import DiscreteSolver, GaussianSolver, correlation, gaussian_thresholds, records_to_dense
 
 
 @dataclass
@@ -106,22 +116,34 @@ class _Admission:
             self.used -= nbytes
 
 
-class SkeletonServer:
-    """Continuous-batching server for one device."""
+class _Tick:
+    """One tick of the Gaussian engine in flight: its completion event and what must
+    stay alive until the stream has passed it."""
+    __slots__ = ("event", "keep", "finishing")
 
-    def __init__(self, budget_bytes: float = 120e9, max_batch: int = 256, precision: str = "f64",
-                 discrete_workers: int = 3, gaussian_workers: int = 2, solo_max: int = 2):
+    def __init__(self, event, keep, finishing):
+        self.event, self.keep, self.finishing = event, keep, finishing
+
+
+class _GaussJob:
+    """A Gaussian request in the engine: its device buffers and where it stands."""
+    __slots__ = ("r", "adm_t", "nbytes", "X", "cws", "C", "G", "pmax", "rec", "state", "thr", "inst", "corr_ev",
+                 "next_level", "status", "host", "batch")
+
+
+class SkeletonServer:
+    """Continuous-batching server for one device (see the module docstring)."""
+
+    MAX_LEVEL = 12  # the batched level kernels' range; deeper requests take the single-problem path
+
+    def __init__(self, budget_bytes: float = 120e9, discrete_workers: int = 3, finishing_threads: int = 4,
+                 max_inflight_ticks: int = 2):
         self.budget = int(budget_bytes)
-        self.max_batch = int(max_batch)
-        self.precision = precision
-        # Gaussian workers: each takes every waiting request it can batch; up to solo_max
-        # requests are solved one by one through the single-problem path (its solve is
-        # shorter than a batch's setup), more form one GaussianBatch
-        self.gaussian_workers = max(1, int(gaussian_workers))
-        self.solo_max = int(solo_max)
         # discrete solves of different requests overlap on the device: each worker owns a
         # stream, and one solve's host reads between levels leave the GPU to the others
         self.discrete_workers = max(1, int(discrete_workers))
+        self.finishing_threads = max(1, int(finishing_threads))
+        self.max_inflight = max(1, int(max_inflight_ticks))
 
     # ----------------------------------------------------------- workers
     def _guard(self, fn, errors, stop, *args):
@@ -131,10 +153,155 @@ class SkeletonServer:
             errors.append(e)
             stop[0] = True
 
-    def _gaussian_worker(self, q, cv, stop, adm, out, t0, clock):
-        torch = _lib.require_cuda()
-        from .batch import GaussianBatch
+    # -- Gaussian engine -------------------------------------------------
+    def _start(self, item, torch, corr_stream):
+        """Allocate a request's buffers and enqueue its samples and correlation."""
+        L = _lib.lib()
+        r, adm_t, nbytes = item
+        j = _GaussJob()
+        j.r, j.adm_t, j.nbytes = r, adm_t, nbytes
+        p, n = r.p, r.n
+        with torch.cuda.stream(corr_stream):
+            j.X = r.samples.to("cuda", non_blocking=True)
+            j.cws = torch.empty(int(L.gcsl_corr_tc_workspace_bytes(n, p)), dtype=torch.uint8, device="cuda")
+            j.C = torch.empty((p, p), dtype=torch.float64, device="cuda")
+            _lib.check(L.gcsl_corr_f64_tc(j.X.data_ptr(), _lib.GCSL_DTYPE_F32, n, p, p, j.C.data_ptr(),
+                                          j.cws.data_ptr(), j.cws.numel(), _lib.stream_ptr(corr_stream)),
+                       "gcsl_corr_f64_tc")
+            j.corr_ev = torch.cuda.Event()
+            j.corr_ev.record(corr_stream)
+            j.G = torch.empty((p, p), dtype=torch.int16, device="cuda")
+            j.pmax = torch.empty((p, p), dtype=torch.float64, device="cuda")
+            j.rec = torch.empty(max(1024, 64 * p), dtype=torch.int32, device="cuda")
+            j.state = torch.empty(int(L.gcsl_gauss_state_bytes(p)), dtype=torch.uint8, device="cuda")
+        j.thr = (ct.c_double * 50)(*gaussian_thresholds(n, r.alpha))
+        I = _lib.GaussInstance()
+        I.C, I.p, I.n_obs = j.C.data_ptr(), p, n
+        I.thresholds, I.n_thresholds = j.thr, 50
+        I.G, I.pmax = j.G.data_ptr(), j.pmax.data_ptr()
+        I.rec_pool, I.rec_cap = j.rec.data_ptr(), j.rec.numel()
+        I.state = j.state.data_ptr()
+        j.inst = I
+        j.next_level = 0
+        return j
 
+    def _enqueue_group(self, torch, jobs, first, last, finish, stream, keep):
+        """One batched plan over `jobs` (all due for levels first..last), stepped on
+        `stream`; returns the pinned status array [done, last level, status, records]."""
+        L = _lib.lib()
+        k = len(jobs)
+        arr = (_lib.GaussInstance * k)(*[j.inst for j in jobs])
+        tb = int(L.gcsl_gauss_batch_table_bytes(k))
+        ws = torch.empty(tb, dtype=torch.uint8, device="cuda")
+        stage = torch.empty(tb, dtype=torch.uint8, pin_memory=True)
+        status = torch.zeros(4 * k, dtype=torch.int32, pin_memory=True)
+        plan = _lib.BatchPlan()
+        sp = _lib.stream_ptr(stream)
+        _lib.check(L.gcsl_gauss_batch_prepare_staged(arr, k, max(j.r.max_level for j in jobs), _lib.GCSL_PREC_F64,
+                                                     ws.data_ptr(), tb, stage.data_ptr(), tb, ct.byref(plan), sp),
+                   "gcsl_gauss_batch_prepare_staged")
+        _lib.check(L.gcsl_gauss_batch_step(ct.byref(plan), first, last, 1 if finish else 0, status.data_ptr(), sp),
+                   "gcsl_gauss_batch_step")
+        keep += [arr, ws, stage, status, plan]
+        return status
+
+    def _gaussian_engine(self, q, cv, stop, adm, out, t0, clock, finisher, solo_q, solo_cv):
+        torch = _lib.require_cuda()
+        corr_stream = torch.cuda.Stream()
+        level_stream = torch.cuda.Stream()
+        starting: list[_GaussJob] = []    # correlation enqueued, levels not started
+        active: list[_GaussJob] = []      # levels in progress
+        inflight: deque[_Tick] = deque()
+        while True:
+            with cv:
+                while not q and not starting and not active and not inflight and not stop[0]:
+                    cv.wait(0.001)
+                if stop[0] and not (q or starting or active or inflight):
+                    return
+                new = list(q)
+                q.clear()
+            for item in new:
+                if item[0].max_level > self.MAX_LEVEL:
+                    with solo_cv:
+                        solo_q.append(item)
+                        solo_cv.notify()
+                    continue
+                starting.append(self._start(item, torch, corr_stream))
+            ready = [j for j in starting if j.corr_ev.query()]
+            starting = [j for j in starting if j not in ready]
+            # a plan's instances share their level cap: groups by (next level, cap)
+            groups, starts = {}, {}
+            for j in active:
+                groups.setdefault((j.next_level, j.r.max_level), []).append(j)
+            for j in ready:
+                starts.setdefault(j.r.max_level, []).append(j)
+            keep, finishing = [], []
+            if ready or active:
+                for j in ready:
+                    level_stream.wait_event(j.corr_ev)  # completed already: orders the stream after it
+                for cap, js in starts.items():  # start: state reset, level 0 and level 1
+                    self._enqueue_group(torch, js, 0, min(1, cap), False, level_stream, keep)
+                    for j in js:
+                        j.next_level, j.batch = 2, len(js)
+                        j.cws = j.X = None  # the correlation is done with them
+                for lv, cap in sorted(groups):
+                    js = groups[(lv, cap)]
+                    if lv > cap:  # past the last level: pmax and results
+                        st = self._enqueue_group(torch, js, lv, lv - 1, True, level_stream, keep)
+                        with torch.cuda.stream(level_stream):
+                            for i, j in enumerate(js):
+                                j.status = (st, i)
+                                j.host = (torch.empty(j.G.shape, dtype=torch.int16, pin_memory=True),
+                                          torch.empty(j.pmax.shape, dtype=torch.float64, pin_memory=True),
+                                          torch.empty(j.rec.shape, dtype=torch.int32, pin_memory=True))
+                                j.host[0].copy_(j.G, non_blocking=True)
+                                j.host[1].copy_(j.pmax, non_blocking=True)
+                                j.host[2].copy_(j.rec, non_blocking=True)
+                        finishing += js
+                    else:
+                        self._enqueue_group(torch, js, lv, lv, False, level_stream, keep)
+                        for j in js:
+                            j.next_level = lv + 1
+                active = [j for j in active if j not in finishing] + ready
+                ev = torch.cuda.Event()
+                ev.record(level_stream)
+                inflight.append(_Tick(ev, keep, finishing))
+            # retire ticks: when too many are in flight, or when nothing else can progress
+            idle = not active and not ready
+            while inflight and (len(inflight) > self.max_inflight or inflight[0].event.query() or
+                                (idle and not starting and not q)):
+                t = inflight.popleft()
+                t.event.synchronize()
+                for j in t.finishing:
+                    finisher.submit(self._finish_gaussian, j, out, adm, t0, clock)
+            if not ready and not active and starting:
+                time.sleep(0.0002)  # correlations running: nothing to step yet
+
+    def _finish_gaussian(self, j, out, adm, t0, clock):
+        st, i = j.status
+        done, last, status, n_rec = (int(x) for x in st[4 * i:4 * i + 4].tolist())
+        r = j.r
+        if status != _lib.GCSL_OK or n_rec > j.rec.numel():
+            # record pool too small (or an error): solve this request alone through the
+            # single-problem path, which grows its pool
+            G, sep, pm = self._solve_alone(r, j.C)
+        else:
+            Gh, Ph, Rh = j.host
+            G = Gh.numpy().view(np.uint16)
+            pm = Ph.numpy()
+            sep = records_to_dense(Rh.numpy(), n_rec, r.p, r.max_level)
+        out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, j.adm_t, clock() - t0, j.batch))
+        adm.release(j.nbytes)
+
+    @staticmethod
+    def _solve_alone(r, C):
+        s = GaussianSolver(r.p, r.max_level)
+        s.run(C, r.n, gaussian_thresholds(r.n, r.alpha))
+        return s.to_host()
+
+    def _solo_worker(self, q, cv, stop, adm, out, t0, clock):
+        """Gaussian requests beyond the batched kernels' level range, one at a time."""
+        torch = _lib.require_cuda()
         stream = torch.cuda.Stream()
         while True:
             with cv:
@@ -142,40 +309,12 @@ class SkeletonServer:
                     cv.wait(0.001)
                 if not q and stop[0]:
                     return
-                # the head request and every waiting request with its alpha and level cap
-                key = (q[0][0].alpha, q[0][0].max_level)
-                batch, rest = [], deque()
-                while q:
-                    item = q.popleft()
-                    if (item[0].alpha, item[0].max_level) == key and len(batch) < self.max_batch:
-                        batch.append(item)
-                    else:
-                        rest.append(item)
-                q.extend(rest)
-            if len(batch) <= self.solo_max:
-                for r, adm_t, nbytes in batch:
-                    with torch.cuda.stream(stream):
-                        X = r.samples.to("cuda", non_blocking=True)
-                        s = GaussianSolver(r.p, r.max_level)
-                        s.run(correlation(X), r.n, gaussian_thresholds(r.n, r.alpha))
-                        G, sep, pm = s.to_host()
-                    out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, adm_t, clock() - t0, 1))
-                    adm.release(nbytes)
-                    del s, X
-                continue
+                r, adm_t, nbytes = q.popleft()
             with torch.cuda.stream(stream):
-                Xs = [r.samples.to("cuda", non_blocking=True) for r, _, _ in batch]
-                b = GaussianBatch([r.p for r, _, _ in batch], [r.n for r, _, _ in batch], key[0], key[1],
-                                  self.precision)
-                b.bind_samples(Xs)
-                b.run(graph=False)
-                res = [b.to_host(k) for k in range(len(batch))]
-            done = clock() - t0
-            for k, (r, adm_t, nbytes) in enumerate(batch):
-                G, sep, pm = res[k]
-                out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, adm_t, done, len(batch)))
-                adm.release(nbytes)
-            del b, Xs
+                X = r.samples.to("cuda", non_blocking=True)
+                G, sep, pm = self._solve_alone(r, correlation(X))
+            out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, adm_t, clock() - t0))
+            adm.release(nbytes)
 
     def _discrete_worker(self, q, cv, stop, adm, out, t0, clock):
         torch = _lib.require_cuda()
@@ -203,19 +342,33 @@ class SkeletonServer:
         """Serve `trace` (arrival times relative to the call) and return one response per
         request, in completion order."""
         adm = _Admission(self.budget)
-        qg, qd = deque(), deque()
-        cvg, cvd = threading.Condition(), threading.Condition()
+        qg, qd, qs = deque(), deque(), deque()
+        cvg, cvd, cvs = threading.Condition(), threading.Condition(), threading.Condition()
         stop = [False]
         errors: list[BaseException] = []
         out: list[Response] = []
+        finisher = cf.ThreadPoolExecutor(max_workers=self.finishing_threads)
         t0 = clock()
-        wgs = [threading.Thread(target=self._guard, args=(self._gaussian_worker, errors, stop, qg, cvg, stop, adm,
-                                                          out, t0, clock), daemon=True)
-               for _ in range(self.gaussian_workers)]
+
+        def fin_guard(fn, *a):
+            try:
+                fn(*a)
+            except BaseException as e:  # surfaced by serve()
+                errors.append(e)
+                stop[0] = True
+
+        class _Fin:
+            def submit(self_, fn, *a):
+                return finisher.submit(fin_guard, fn, *a)
+
+        wg = threading.Thread(target=self._guard, args=(self._gaussian_engine, errors, stop, qg, cvg, stop, adm, out,
+                                                        t0, clock, _Fin(), qs, cvs), daemon=True)
+        ws = threading.Thread(target=self._guard, args=(self._solo_worker, errors, stop, qs, cvs, stop, adm, out, t0,
+                                                        clock), daemon=True)
         wds = [threading.Thread(target=self._guard, args=(self._discrete_worker, errors, stop, qd, cvd, stop, adm,
                                                           out, t0, clock), daemon=True)
                for _ in range(self.discrete_workers)]
-        for w in wgs + wds:
+        for w in [wg, ws] + wds:
             w.start()
         pending = deque(sorted(trace, key=lambda r: r.arrival))
         waiting: deque = deque()  # arrived, not admitted (FIFO)
@@ -233,26 +386,22 @@ class SkeletonServer:
                         break
                     waiting.popleft()
                     item = (r, clock() - t0, nbytes)
-                    if r.kind == "gaussian":
-                        with cvg:
-                            qg.append(item)
-                            cvg.notify()
-                    else:
-                        with cvd:
-                            qd.append(item)
-                            cvd.notify()
+                    q, cv = (qg, cvg) if r.kind == "gaussian" else (qd, cvd)
+                    with cv:
+                        q.append(item)
+                        cv.notify()
                 if pending and not waiting:
                     time.sleep(max(0.0, min(0.0005, pending[0].arrival - (clock() - t0))))
                 elif waiting:
                     time.sleep(0.0002)
         finally:
             stop[0] = True
-            with cvg:
-                cvg.notify_all()
-            with cvd:
-                cvd.notify_all()
-            for w in wgs + wds:
+            for cv in (cvg, cvd, cvs):
+                with cv:
+                    cv.notify_all()
+            for w in [wg, ws] + wds:
                 w.join()
+            finisher.shutdown(wait=True)
         if errors:
             raise errors[0]
         return out
@@ -286,10 +435,19 @@ def serve_plain(trace: list[Request], clock=time.perf_counter) -> list[Response]
 
 
 def latency_summary(resp: list[Response]) -> dict:
-    lat = np.array([r.latency for r in resp])
-    span = max(r.done for r in resp) - min(r.arrival for r in resp)
-    return {"p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
-            "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3),
-            "mean_ms": round(1e3 * float(lat.mean()), 3),
-            "skeletons_per_s": round(len(resp) / span, 2) if span > 0 else None,
-            "mean_batch": round(float(np.mean([r.batch for r in resp])), 2)}
+    """p50 / p99 / mean latency and throughput of a set of responses, overall and per kind."""
+    def summ(rs):
+        lat = np.array([r.latency for r in rs])
+        span = max(r.done for r in rs) - min(r.arrival for r in rs)
+        return {"count": len(rs), "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
+                "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3),
+                "mean_ms": round(1e3 * float(lat.mean()), 3),
+                "skeletons_per_s": round(len(rs) / span, 2) if span > 0 else None,
+                "mean_batch": round(float(np.mean([r.batch for r in rs])), 2)}
+
+    out = summ(resp)
+    for kind in ("gaussian", "discrete"):
+        rs = [r for r in resp if r.kind == kind]
+        if rs:
+            out[kind] = {k: v for k, v in summ(rs).items() if k in ("count", "p50_ms", "p99_ms", "mean_ms")}
+    return out

@@ -206,6 +206,8 @@ typedef struct gcsl_gauss_instance {
     int32_t *rec_pool;        /* device sepset record pool ([lo, hi, level, S...]), or NULL */
     int64_t rec_cap;
     const double *c_err;      /* device bound on |C - C_exact| (GCSL_PREC_SPLIT on a split correlation), or NULL */
+    void *state;              /* device solve state of gcsl_gauss_state_bytes(p) bytes (256-byte aligned) that
+                                 persists across plans, or NULL: a slice of the batch workspace */
     int32_t status;           /* out (collect): device status of this instance */
     int32_t levels_run;       /* out (collect) */
     int64_t n_records;        /* out (collect): ints used in rec_pool (may exceed rec_cap) */
@@ -231,6 +233,37 @@ int gcsl_gauss_batch_collect(const gcsl_batch_plan *plan, gcsl_gauss_instance *i
 /* Autotuner hook: lanes per edge (32 or 8; 8 only for levels <= 4) of a level's test
  * kernel.  Results do not depend on it. */
 int gcsl_gauss_batch_set_lanes(gcsl_batch_plan *plan, int32_t level, int32_t lanes);
+
+/* Level-by-level stepping for continuous batching (no counterpart in the reference: a
+ * server admits new problems between the levels of the ones in flight).  Instances
+ * that carry their own `state` (gcsl_gauss_state_bytes(p) bytes) keep their solve state
+ * there across plans, so each step's plan may group a different set of instances: those
+ * due for the same levels.
+ *   table_bytes       workspace of a plan whose instances all carry their state
+ *   prepare_staged    as prepare, but builds the plan's tables in the caller's pinned host
+ *                     buffer `stage` (table_bytes) and only enqueues their upload: the
+ *                     buffer must stay untouched until the stream has passed the copy
+ *   step              enqueues levels first_level..last_level of every instance of the plan
+ *                     (first_level 0: the state reset and level 0 first), then with finish
+ *                     the pmax write-back; instances whose loop ended skip the rest on the
+ *                     device.  host_status (pinned, 4 int32 per instance, or NULL) receives
+ *                     [done, last level run, status, record ints] once the stream has
+ *                     passed the step.
+ * Each instance's levels must be stepped in order, one plan at a time. */
+size_t gcsl_gauss_state_bytes(int32_t p);
+size_t gcsl_gauss_batch_table_bytes(int32_t count);
+int gcsl_gauss_batch_prepare_staged(const gcsl_gauss_instance *inst, int32_t count, int32_t max_level,
+                                    int32_t precision, void *workspace, size_t workspace_bytes, void *stage,
+                                    size_t stage_bytes, gcsl_batch_plan *plan, void *stream);
+int gcsl_gauss_batch_step(const gcsl_batch_plan *plan, int32_t first_level, int32_t last_level, int32_t finish,
+                          int32_t *host_status, void *stream);
+
+/* Host helper (replaces the dense sepset fill of gpucsl/pc/discover_skeleton_gaussian.py:
+ * 166-168): scatters an int32 record pool [lo, hi, level, S...] of n_ints ints into the
+ * reference's dense layout out[p][p][max_level] (host memory), -1 where no set; records
+ * above max_level are skipped.  Returns GCSL_ERR_INVALID_ARG on a record that leaves
+ * the pool or names a variable outside [0, p).  Runs on the calling thread(s), no GPU. */
+int gcsl_records_to_dense(const int32_t *rec, int64_t n_ints, int32_t p, int32_t max_level, int32_t *out);
 
 /* Batched tensor-core correlation (the digit-product path of gcsl_corr_f64_tc for many
  * sample matrices in one launch per stage).  X[k] is n[k] x p[k] (row stride ldx[k]),
