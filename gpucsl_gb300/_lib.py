@@ -21,6 +21,7 @@ GCSL_ERR_TIMEOUT = 4
 GCSL_ERR_DEVICE = 5
 GCSL_ERR_CAPACITY = 6
 GCSL_ERR_UNSUPPORTED = 7
+GCSL_ERR_DEBUG_CHECK = 8
 GCSL_MAX_LEVELS = 64
 GCSL_DTYPE_F64 = 0
 GCSL_DTYPE_F32 = 1
@@ -43,7 +44,7 @@ EXPORTED = [
     "gcsl_gauss_batch_flags", "gcsl_gauss_state_bytes", "gcsl_gauss_batch_table_bytes",
     "gcsl_gauss_batch_prepare_staged", "gcsl_gauss_batch_step", "gcsl_records_to_dense",
     "gcsl_orient_workspace_bytes", "gcsl_orient_edges", "gcsl_encode_workspace_bytes", "gcsl_ordinal_encode",
-    "gcsl_set_test_precision",
+    "gcsl_set_test_precision", "gcsl_debug_set_work_order",
 ]
 
 GCSL_PREC_F64 = 0
@@ -62,6 +63,7 @@ class GcslStats(ct.Structure):
         ("removed", ct.c_int64 * GCSL_MAX_LEVELS),
         ("max_degree", ct.c_int32 * GCSL_MAX_LEVELS),
         ("level_ms", ct.c_float * GCSL_MAX_LEVELS),
+        ("debug_site", ct.c_int32),
     ]
 
     def as_dict(self) -> dict:
@@ -76,6 +78,7 @@ class GcslStats(ct.Structure):
             "removed": [int(x) for x in self.removed[:n]],
             "max_degree": [int(x) for x in self.max_degree[:n]],
             "level_ms": [float(x) for x in self.level_ms[:GCSL_MAX_LEVELS] if x > 0],
+            "debug_site": int(self.debug_site),
         }
 
 
@@ -128,13 +131,21 @@ _sz = ct.c_size_t
 _dbl = ct.c_double
 
 
-@lru_cache(maxsize=1)
-def lib() -> ct.CDLL:
-    if not LIB_PATH.exists():
-        raise RuntimeError(
-            f"{LIB_PATH.name} is not built; run `python -c 'import __graft_entry__ as g; g.build()'` "
-            "(requires nvcc) before using gpucsl_gb300")
-    L = ct.CDLL(str(LIB_PATH))
+@lru_cache(maxsize=2)
+def lib(debug: bool = False) -> ct.CDLL:
+    """The release library, or with debug the bounds-checked build (compiled on first
+    use, as the reference compiles its kernels with -G when is_debug is set)."""
+    if debug:
+        from . import build as _build
+
+        path = _build.build(debug=True)
+    else:
+        path = LIB_PATH
+        if not path.exists():
+            raise RuntimeError(
+                f"{path.name} is not built; run `python -c 'import __graft_entry__ as g; g.build()'` "
+                "(requires nvcc) before using gpucsl_gb300")
+    L = ct.CDLL(str(path))
     L.gcsl_version.restype = ct.c_int
     L.gcsl_version.argtypes = []
     L.gcsl_kernel_launches.restype = ct.c_int64
@@ -218,6 +229,8 @@ def lib() -> ct.CDLL:
     L.gcsl_records_to_dense.argtypes = [_vp, _i64, _i32, _i32, _vp]
     L.gcsl_set_test_precision.restype = ct.c_int
     L.gcsl_set_test_precision.argtypes = [_i32]
+    L.gcsl_debug_set_work_order.restype = ct.c_int
+    L.gcsl_debug_set_work_order.argtypes = [ct.c_uint64]
     L.gcsl_encode_workspace_bytes.restype = _sz
     L.gcsl_encode_workspace_bytes.argtypes = [_i32]
     L.gcsl_ordinal_encode.restype = ct.c_int

@@ -345,6 +345,7 @@ int finish_stats(const DevState *d_st, gcsl_stats *stats, cudaStream_t s, bool d
         std::memset(stats, 0, sizeof(*stats));
         stats->levels_run = h.last_level + 1;
         stats->status = h.status;
+        stats->debug_site = h.debug_site;
         stats->n_records = (int64_t)h.n_rec_ints;
         for (int l = 0; l < GCSL_MAX_LEVELS; ++l) {
             stats->edges[l] = (int64_t)(discrete_edges ? h.edges[l] / 2 : h.edges[l]);
@@ -451,6 +452,9 @@ long long chunk_units_cap(int p) { return std::max<long long>(1ll << 16, 64ll * 
 // 2 = FP64 throughout.
 static thread_local int g_test_precision = 0;
 
+// Work-order seed of the calling thread's solves (debug build; see gcsl_debug_set_work_order).
+static thread_local unsigned long long g_work_order = 0;
+
 bool mixed_tests() {
     static const bool mixed = [] {
         const char *e = getenv("GCSL_F64_TESTS");
@@ -514,6 +518,8 @@ DiscWs carve_disc(void *ws, size_t cap, int p) {
 }
 
 }  // namespace
+
+unsigned long long gcsl::host::work_order_seed() { return GCSL_DEBUG_CHECKS ? g_work_order : 0ull; }
 
 int gcsl::host::gauss_skeleton_run(const double *C, int p, long long n_obs, const double *thresholds,
                                    int n_thresholds, int max_level, uint16_t *G, int *sepsets, int *rec_pool,
@@ -655,6 +661,16 @@ int64_t gcsl_kernel_launches(void) { return (int64_t)g_kernel_launches.load(std:
 
 const char *gcsl_last_error(void) { return g_last_error; }
 
+int gcsl_debug_set_work_order(uint64_t seed) {
+#if GCSL_DEBUG_CHECKS
+    g_work_order = (unsigned long long)seed;
+    return GCSL_OK;
+#else
+    (void)seed;
+    return GCSL_ERR_UNSUPPORTED;
+#endif
+}
+
 int gcsl_set_test_precision(int32_t mode) {
     if (mode < 0 || mode > 2) return GCSL_ERR_INVALID_ARG;
     g_test_precision = mode;
@@ -671,6 +687,7 @@ const char *gcsl_status_string(int status) {
     case GCSL_ERR_DEVICE: return "CUDA error";
     case GCSL_ERR_CAPACITY: return "sepset record pool too small";
     case GCSL_ERR_UNSUPPORTED: return "unsupported problem size";
+    case GCSL_ERR_DEBUG_CHECK: return "a bounds check of the debug build failed (gcsl_stats.debug_site)";
     default: return "unknown status";
     }
 }
@@ -759,6 +776,7 @@ int gcsl_disc_skeleton(const uint8_t *data, int64_t ld, int64_t n, int32_t p, co
     if (e == cudaSuccess) e = cudaMemsetAsync(G, 0, sizeof(uint16_t) * (size_t)p * p, s);
     if (e != cudaSuccess) return GCSL_ERR_DEVICE;
     DiscLevelArgs A{data, ld, n, p, dims, alpha, 0, w.adj, w.prefix, G, pmax, w.win, cap, 1024, w.st};
+    A.order = host::work_order_seed();
     host::disc_level_caps(cap, max_dim, 0, A.table_cap, A.part_cap);
     // codes in range once per solve; the test kernels skip the per-sample checks then
     if (host::launch_disc_validate(data, ld, n, p, dims, w.st, sms, s) != cudaSuccess) return GCSL_ERR_DEVICE;

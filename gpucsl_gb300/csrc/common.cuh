@@ -24,6 +24,9 @@ void note_launch(int kernels);
 // Records the first failing CUDA call of the calling thread's current entry point (kept
 // for gcsl_last_error) and returns e.
 cudaError_t note_error(const char *where, cudaError_t e);
+// The calling thread's work-order seed of the debug build (gcsl_debug_set_work_order; 0
+// in the release build).
+unsigned long long work_order_seed();
 // Modes of a batched correlation run (corr_tc.cu): every job with seven digits; every job
 // with five digits and an error bound; only flagged jobs, seven digits, on the digits of
 // a previous run.
@@ -133,6 +136,8 @@ struct DevState {
     int32_t done;                            // level loop finished (sticky)
     int32_t last_level;                      // highest level whose tests ran
     int32_t n_kept;                          // pairs kept at level 0 (Gaussian)
+    int32_t debug_site;                      // first failed check of the debug build (GCSL_DCHECK_*), 0 if none
+    int32_t reserved_;
     int32_t max_degree[GCSL_MAX_LEVELS];     // max compacted degree at level start
     unsigned long long edges[GCSL_MAX_LEVELS];
     unsigned long long tests[GCSL_MAX_LEVELS];
@@ -188,9 +193,54 @@ struct DiscLevelArgs {
     int table_cap;            // counters of shared memory for the table and its replicas
     int part_cap;             // strata of the per-stratum statistic buffer (after the table)
     DevState *st;
+    unsigned long long order = 0;  // work order of the debug build (0: launch order)
 };
 
 __device__ __forceinline__ void set_status(DevState *st, int code) { atomicCAS(&st->status, 0, code); }
+
+// ------------------------------------------------------------ debug build
+// The library built with GCSL_DEBUG_CHECKS=1 (selected by the reference's is_debug,
+// kernel_management.py:32-33) checks the indices its kernels derive before using them:
+// a failed check sets GCSL_ERR_DEBUG_CHECK and the site below in the solve's state and
+// the access is redirected to a valid index (never a trap).  It also walks the work of
+// the level and test loops in a permuted order (gcsl_debug_set_work_order), which must
+// not change any result.
+#ifndef GCSL_DEBUG_CHECKS
+#define GCSL_DEBUG_CHECKS 0
+#endif
+enum {
+    GCSL_DCHECK_EDGE = 1,      // an edge of the level's list outside [0, p) or not lo < hi
+    GCSL_DCHECK_POSITION = 2,  // an unranked position outside [1, K]
+    GCSL_DCHECK_SET = 3,       // a conditioning variable outside [0, p), equal to v_i / v_j, or unsorted
+    GCSL_DCHECK_DEGREE = 4,    // a compacted degree above p - 1
+};
+__device__ __forceinline__ bool dcheck(DevState *st, bool ok, int site) {
+#if GCSL_DEBUG_CHECKS
+    if (!ok && st != nullptr) {
+        set_status(st, GCSL_ERR_DEBUG_CHECK);
+        atomicCAS(&st->debug_site, 0, site);
+    }
+    return ok;
+#else
+    (void)st;
+    (void)site;
+    return true;
+#endif
+}
+// Work index e of n in the debug build's permuted order (a reflection and a rotation by
+// the seed, a bijection on [0, n)); the identity in the release build or for seed 0.
+__device__ __forceinline__ long long work_order(long long e, long long n, unsigned long long seed) {
+#if GCSL_DEBUG_CHECKS
+    if (seed == 0 || n <= 1) return e;
+    const long long r = (long long)(seed % (unsigned long long)n);
+    const long long x = n - 1 - e + r;
+    return x >= n ? x - n : x;
+#else
+    (void)n;
+    (void)seed;
+    return e;
+#endif
+}
 
 // C(n, k) for small k by the exact multiplicative recurrence; k is bounded by KMAX
 // so the divisors are compile-time constants after unrolling.

@@ -177,7 +177,8 @@ __device__ void count_table(const uint8_t *__restrict__ data, long long ld, long
     const uint4 *ci = reinterpret_cast<const uint4 *>(data + (size_t)vi * ld);
     const uint4 *cj = reinterpret_cast<const uint4 *>(data + (size_t)vj * ld);
     const long long nvec = (n + 15) >> 4;
-    if (trusted && T <= 256) {
+    // the debug build always takes the checked path below (every cell index is checked)
+    if (trusted && T <= 256 && !GCSL_DEBUG_CHECKS) {
         const long long nfull = n >> 4;  // vectors of 16 samples, all valid
         for (long long v = tid; v < nfull; v += nt) {
             uint32_t s4[4] = {0u, 0u, 0u, 0u};
@@ -407,7 +408,8 @@ __global__ void __launch_bounds__(256) disc_test_kernel(DiscLevelArgs A) {
     const long long total = (L == 0) ? (long long)A.p * (A.p - 1) / 2 : A.prefix[A.p];
     const int tid = threadIdx.x;
 
-    for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+    for (long long t0 = blockIdx.x; t0 < total; t0 += gridDim.x) {
+        const long long t = work_order(t0, total, A.order);
         if (tid == 0) {
             int vi, vj;
             long long rank = 0;

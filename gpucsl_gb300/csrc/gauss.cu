@@ -60,7 +60,7 @@ __device__ __forceinline__ void recompact_blocks(const uint16_t *__restrict__ G,
     const int warps = (nblocks * blockDim.x) >> 5;
     int maxdeg = 0;
     for (int r = (b * blockDim.x + threadIdx.x) >> 5; r < p; r += warps)
-        maxdeg = max(maxdeg, recompact_row(G, p, adj, up, r, lane, elist, &st->edges[level]));
+        maxdeg = max(maxdeg, recompact_row(G, p, adj, up, r, lane, elist, &st->edges[level], st));
     if (lane == 0) atomicMax(&st->max_degree[level], maxdeg);
 }
 
@@ -362,6 +362,7 @@ LevelCtx level_ctx(int L, const double *C, int p, const int *adj, const int2 *el
                    long long rec_cap, DevState *st, const float *C32, int *qbuf, long long qcap,
                    const ChunkBufs &ck) {
     LevelCtx x;
+    x.order = work_order_seed();
     x.C = C;
     x.p = p;
     x.adj = adj;

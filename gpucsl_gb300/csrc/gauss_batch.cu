@@ -321,7 +321,7 @@ __global__ void batch_compact_kernel(const BInst *__restrict__ inst, const long 
         const BInst &I = inst[inst_of(off_rows, count, g, r)];
         if (skip_inst(I, rerun) || I.st->done) continue;
         const int deg = (level == 1) ? compact_row(I.G, I.p, I.adj, I.up, (int)r, lane)
-                                     : recompact_row(I.G, I.p, I.adj, I.up, (int)r, lane);
+                                     : recompact_row(I.G, I.p, I.adj, I.up, (int)r, lane, nullptr, nullptr, I.st);
         if (lane == 0) atomicMax(&I.st->max_degree[level], deg);
     }
 }

@@ -168,10 +168,11 @@ __device__ __forceinline__ int compact_row(const uint16_t *__restrict__ G, int p
 // row's edges.  Returns the degree.
 __device__ __forceinline__ int recompact_row(const uint16_t *__restrict__ G, int p, int *__restrict__ adj,
                                              int *__restrict__ up, int r, int lane, int2 *elist = nullptr,
-                                             unsigned long long *ecount = nullptr) {
+                                             unsigned long long *ecount = nullptr, DevState *st = nullptr) {
     {
         int *row = adj + (size_t)r * p;
-        const int deg = row[0];
+        int deg = row[0];
+        if (!dcheck(st, deg >= 0 && deg <= p - 1, GCSL_DCHECK_DEGREE)) deg = deg < 0 ? 0 : p - 1;
         int cnt = 0, ups = 0;
         for (int k0 = 0; k0 < deg; k0 += 32) {
             const int k = k0 + lane;
@@ -355,8 +356,16 @@ __device__ __forceinline__ bool load_edge(const int *__restrict__ adj, const int
 // Edge e of the level from the explicit edge list (lo < hi) written by the edge scan.
 template <int KMAX>
 __device__ __forceinline__ bool load_edge_list(const int *__restrict__ adj, const int2 *__restrict__ elist, int p,
-                                               long long e, int L, EdgeJob &J) {
+                                               long long e, int L, EdgeJob &J, DevState *st = nullptr) {
     const int2 ed = elist[e];
+    if (!dcheck(st, ed.x >= 0 && ed.x < ed.y && ed.y < p, GCSL_DCHECK_EDGE)) {  // no tests for this edge
+        J.lo = 0;
+        J.hi = p > 1 ? 1 : 0;
+        J.deg_lo = J.deg_hi = 0;
+        J.R0 = J.R1 = J.T = J.Rmin = 0;
+        J.longer = 0;
+        return true;
+    }
     J.lo = ed.x;
     J.hi = ed.y;
     J.deg_lo = adj[(size_t)ed.x * p];
@@ -667,7 +676,17 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
             unrank_positions<L>(K, rank, pos, sb);
             const int *nbrs = adj + (size_t)vi * p + 1;
 #pragma unroll
-            for (int c = 0; c < L; ++c) S[c] = resolve_position(nbrs, vj, pos[c]);
+            for (int c = 0; c < L; ++c) {
+                const int q = pos[c];
+                S[c] = resolve_position(nbrs, vj, dcheck(st, q >= 1 && q <= K, GCSL_DCHECK_POSITION) ? q : 1);
+            }
+#if GCSL_DEBUG_CHECKS
+#pragma unroll
+            for (int c = 0; c < L; ++c) {
+                const bool ok = S[c] >= 0 && S[c] < p && S[c] != vi && S[c] != vj && (c == 0 || S[c] > S[c - 1]);
+                if (!dcheck(st, ok, GCSL_DCHECK_SET)) S[c] = S[c] < 0 || S[c] >= p ? 0 : S[c];
+            }
+#endif
             o = test(vi, vj, S);
         }
         const unsigned bal = (__ballot_sync(GCSL_FULL_MASK, o.remove) >> gshift) & gbits;

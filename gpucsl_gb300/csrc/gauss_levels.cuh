@@ -38,6 +38,7 @@ struct LevelCtx {
     DevState *st;
     MixArgs mix;
     ChunkBufs ck;  // ck.heavy == nullptr: every edge is walked whole
+    unsigned long long order;  // work order of the debug build (0: list order)
 };
 
 // The level's test (FP32-first or FP64) over the keys of range rg of edge J.
@@ -73,9 +74,10 @@ __device__ __forceinline__ void level_edge_phase(const LevelCtx &x, const BinomR
     const int lane = threadIdx.x & 31;
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
     unsigned long long n_tests = 0, n_full = 0, n_removed = 0;
-    for (long long e = w0; e < n_edges; e += nw) {
+    for (long long e0 = w0; e0 < n_edges; e0 += nw) {
+        const long long e = work_order(e0, n_edges, x.order);
         EdgeJob J;
-        if (!load_edge_list<L>(x.adj, x.elist, p, e, L, J)) {
+        if (!load_edge_list<L>(x.adj, x.elist, p, e, L, J, st)) {
             if (lane == 0) set_status(st, GCSL_ERR_UNSUPPORTED);
             J.T = 0;
         }
@@ -144,7 +146,8 @@ __device__ __forceinline__ void level_unit_phase(const LevelCtx &x, const BinomR
     const int lane = threadIdx.x & 31;
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
     unsigned long long n_extra = 0, n_removed = 0, unit_tests = 0;
-    for (long long u = w0; u < nu; u += nw) {
+    for (long long u0 = w0; u0 < nu; u0 += nw) {
+        const long long u = work_order(u0, nu, x.order);
         const int h = __ldcg(ck.unit_h + u);
         if (h < 0) continue;
         const HeavyEdge H = load_heavy(ck.heavy + h);

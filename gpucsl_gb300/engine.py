@@ -108,14 +108,35 @@ class test_precision:
         return False
 
 
-class GaussianSolver:
-    """Gaussian PC-stable skeleton of p variables up to max_level on one device."""
+class debug_work_order:
+    """Context manager for the work order of the bounds-checked build on this thread
+    (gcsl_debug_set_work_order): seed 0 is the release order, another seed reverses and
+    rotates the order in which edges, units and discrete tests are walked.  Results must
+    not depend on it."""
 
-    def __init__(self, p: int, max_level: int, device=None, dense_sepsets: bool = False, record_cap: int | None = None):
+    def __init__(self, seed: int):
+        self.seed = int(seed)
+
+    def __enter__(self):
+        _lib.check(_lib.lib(True).gcsl_debug_set_work_order(self.seed), "gcsl_debug_set_work_order")
+        return self
+
+    def __exit__(self, *exc):
+        _lib.lib(True).gcsl_debug_set_work_order(0)
+        return False
+
+
+class GaussianSolver:
+    """Gaussian PC-stable skeleton of p variables up to max_level on one device.  With
+    debug=True the solves run the bounds-checked build of the kernels (is_debug)."""
+
+    def __init__(self, p: int, max_level: int, device=None, dense_sepsets: bool = False, record_cap: int | None = None,
+                 debug: bool = False):
         torch = _torch()
         self.p, self.max_level = int(p), int(max_level)
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
-        L = _lib.lib()
+        self.debug = bool(debug)
+        L = _lib.lib(self.debug)
         ws = int(L.gcsl_gauss_workspace_bytes(self.p, self.max_level))
         self.workspace = torch.empty(ws, dtype=torch.uint8, device=self.device)
         self.G = torch.empty((self.p, self.p), dtype=torch.int16, device=self.device)
@@ -133,7 +154,7 @@ class GaussianSolver:
         """Enqueue one solve on the current stream.  With sync=True (default) the call
         waits for it, grows the record pool if it overflowed, and returns the stats."""
         torch = _torch()
-        L = _lib.lib()
+        L = _lib.lib(self.debug)
         thr = (ct.c_double * len(thresholds))(*[float(t) for t in thresholds])
         self._thr = thr
         if self.sep_dense is not None:
@@ -167,12 +188,14 @@ class GaussianSolver:
 class DiscreteSolver:
     """Discrete (chi-squared) PC-stable skeleton on one device."""
 
-    def __init__(self, p: int, n: int, max_level: int, max_dim: int, device=None, record_cap: int | None = None):
+    def __init__(self, p: int, n: int, max_level: int, max_dim: int, device=None, record_cap: int | None = None,
+                 debug: bool = False):
         torch = _torch()
         self.p, self.n, self.max_level, self.max_dim = int(p), int(n), int(max_level), int(max_dim)
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         self.ld = (self.n + 15) // 16 * 16
-        L = _lib.lib()
+        self.debug = bool(debug)
+        L = _lib.lib(self.debug)
         ws = int(L.gcsl_disc_workspace_bytes(self.p, self.n, self.max_level, self.max_dim))
         self.workspace = torch.empty(ws, dtype=torch.uint8, device=self.device)
         self.data = torch.zeros((self.p, self.ld), dtype=torch.uint8, device=self.device)
@@ -199,7 +222,7 @@ class DiscreteSolver:
 
     def run(self, alpha: float, sync: bool = True) -> SolveStats | None:
         torch = _torch()
-        L = _lib.lib()
+        L = _lib.lib(self.debug)
         while True:
             st = self.stats if sync else None
             rc = L.gcsl_disc_skeleton(

@@ -46,8 +46,9 @@ def discover_skeleton_gpu_discrete(
     else:
         codes, dims = engine.ordinal_encode(data)
     max_dim = int(dims.max()) if dims.size else 1
+    # is_debug: the bounds-checked build of the kernels (the reference compiles with -G)
     solver = kernels.discrete_solver(num_variables, num_observations, max_level, max_dim) if kernels is not None \
-        else engine.DiscreteSolver(num_variables, num_observations, max_level, max_dim)
+        else engine.DiscreteSolver(num_variables, num_observations, max_level, max_dim, debug=is_debug)
     if codes_dev is not None:
         solver.load(codes_dev=codes_dev[:, :num_observations], dims_dev=dims_dev)
     else:

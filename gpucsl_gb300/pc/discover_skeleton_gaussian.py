@@ -42,8 +42,9 @@ def discover_skeleton_gpu_gaussian(
             C = engine.correlation(X)
         else:
             C = torch.from_numpy(np.ascontiguousarray(correlation_matrix, dtype=np.float64)).to(dev)
+        # is_debug: the bounds-checked build of the kernels (the reference compiles with -G)
         solver = kernels.gaussian_solver(num_variables, max_level) if kernels is not None else \
-            engine.GaussianSolver(num_variables, max_level, device=dev)
+            engine.GaussianSolver(num_variables, max_level, device=dev, debug=is_debug)
         torch.cuda.synchronize(dev)
         start = timer()
         solver.run(C, num_observations, thresholds)

@@ -31,6 +31,7 @@ extern "C" {
 #define GCSL_ERR_DEVICE 5
 #define GCSL_ERR_CAPACITY 6
 #define GCSL_ERR_UNSUPPORTED 7
+#define GCSL_ERR_DEBUG_CHECK 8
 
 #define GCSL_MAX_LEVELS 64
 #define GCSL_DTYPE_F64 0
@@ -50,6 +51,7 @@ typedef struct gcsl_stats {
     int64_t removed[GCSL_MAX_LEVELS];   /* edges removed at this level */
     int32_t max_degree[GCSL_MAX_LEVELS];/* max compacted degree at level start */
     float level_ms[GCSL_MAX_LEVELS];    /* device time per level (0 when not timed) */
+    int32_t debug_site;                 /* debug build: first failed index check (0 = none) */
 } gcsl_stats;
 
 /* A sepset record in the int32 record pool: [lo, hi, level, S_0 .. S_{level-1}]. */
@@ -68,6 +70,15 @@ int64_t gcsl_kernel_launches(void);
  * FP64 throughout when GCSL_F64_TESTS=1 is set), 1 = FP32 first, 2 = FP64 throughout.
  * Both give the same skeleton, sepsets, test counts and pmax; mode 2 exists to show it. */
 int gcsl_set_test_precision(int32_t mode);
+/* Debug build only (libgpucsl_gb300_debug.so, the reference's is_debug compile of
+ * gpucsl/pc/kernel_management.py:32-33, selected by is_debug in the Python API): every
+ * index its kernels derive is checked before use, a failed check returns
+ * GCSL_ERR_DEBUG_CHECK with the site in gcsl_stats.debug_site instead of trapping, and
+ * this call sets the order in which the calling thread's solves walk the edges of a
+ * level, the units of chunked edges and the discrete tests (0 = the release order;
+ * another seed reverses and rotates it).  Results must not depend on the order.  The
+ * release library returns GCSL_ERR_UNSUPPORTED. */
+int gcsl_debug_set_work_order(uint64_t seed);
 
 /* ------------------------------------------------------------ correlation (a) */
 /* Replaces gpucsl/pc/helpers.py:58-59 (correlation_matrix_of = np.corrcoef(data,

@@ -157,3 +157,11 @@ def test_precision_switch_range(built_lib):
     assert L.gcsl_set_test_precision(3) == _lib.GCSL_ERR_INVALID_ARG
     assert L.gcsl_set_test_precision(-1) == _lib.GCSL_ERR_INVALID_ARG
     assert L.gcsl_set_test_precision(0) == _lib.GCSL_OK
+
+
+def test_release_library_has_no_debug_work_order(built_lib):
+    """The work-order switch belongs to the bounds-checked build; the release library
+    refuses it on the host (no device work)."""
+    from gpucsl_gb300 import _lib
+
+    assert _lib.lib().gcsl_debug_set_work_order(1) == _lib.GCSL_ERR_UNSUPPORTED
