@@ -27,8 +27,8 @@
 //   |C' - C| <= eps = 2.5 * 2^-35 * (1.02 w + sqrt(w)),  w = n / min_i sum_t y_ti^2,
 // where C is the seven-digit result (derivation at split_eps below); the diagonal
 // kernel writes eps per instance.  Instances whose tests cannot be decided exactly with
-// C' are flagged by the level loop and get the seven-digit product afterwards (the
-// digit planes hold all seven digits either way).
+// C' are flagged by the level loop and get the seven-digit product afterwards (the split
+// run writes five digit planes; the flagged jobs' seven are written by that later run).
 #include <type_traits>
 #include <vector>
 
@@ -42,12 +42,18 @@ constexpr int OZ_S_SPLIT = 5;           // digits of the split-precision product
 constexpr int OZ_TM = 128, OZ_TN = 64;  // output tile
 constexpr int OZ_KS = 32;               // sample padding granule
 constexpr int OZ_CHUNK_STEPS = 28;      // 448 samples (28 MMA K steps) between exact drains
-constexpr int OZ_NST = 4;               // shared-memory stages (one K step each)
 constexpr uint32_t OZ_TMEM_COLS = 512;
 // shared-memory bytes of one K step for NS digits: NS x (128 A rows + 64 B rows) x 16
 // samples x 2 bytes (NS = 7: 28672 + 14336)
 constexpr int oz_a_bytes(int ns) { return ns * OZ_TM * 16 * 2; }
 constexpr int oz_stage_bytes(int ns) { return ns * (OZ_TM + OZ_TN) * 16 * 2; }
+// Shared-memory stages of the copy ring (one K step each): as many as 210 KB hold, so the
+// bulk copies run as far ahead of the MMAs as the SM allows (5 for seven digits, 7 for
+// five).  Four stages left the tensor pipe idle 40 % of the time waiting on copies.
+constexpr int OZ_RING_BYTES = 215040;
+constexpr int OZ_NST_MAX = 8;
+constexpr int oz_nst(int ns) { return OZ_RING_BYTES / oz_stage_bytes(ns) < OZ_NST_MAX ? OZ_RING_BYTES / oz_stage_bytes(ns)
+                                                                                      : OZ_NST_MAX; }
 constexpr unsigned long long OZ_WAIT_NS = 2000000000ull;
 
 struct OzDims {
@@ -211,14 +217,16 @@ __global__ void col_mean_exp_kernel(Src src) {
 // 16-sample K step q, a 4 KB block in the canonical no-swizzle K-major layout
 // (byte ((k * nI + I) * nq + q) * 4096 + kmajor_offset(row % 128, sample % 16)), zero
 // padded to (p_pad, n_pad).  A 64-row operand tile is the first or second 2 KB half of a
-// block.  One CTA handles 32 samples x 32 columns.
-template <typename T, class Src>
+// block.  One CTA handles 32 samples x 32 columns.  Only the first NW digit planes are
+// written (the split-precision product reads five; the exact one seven).
+template <typename T, class Src, int NW = OZ_S>
 __global__ void digit_split_kernel(Src src) {
     __shared__ int16_t tile[OZ_S][32][33];  // [digit][sample][column]; the top digit reaches 128
     pdl_wait();
     pdl_trigger();
     long long lb;
     const OzJob &Jb = src.get(blockIdx.x, lb);
+    if (src.skip(Jb.index)) return;  // not selected in this run (uniform over the block)
     const T *__restrict__ X = static_cast<const T *>(Jb.X);
     const long long n = Jb.n, ldx = Jb.ldx;
     const int p = Jb.p, p_pad = Jb.D.p_pad;
@@ -271,7 +279,7 @@ __global__ void digit_split_kernel(Src src) {
     const int nI = p_pad / OZ_TM;
     const long long nq = n_pad / 16;
     // 16-byte chunks: (digit k, column c, 8-sample group g8 in 0..3)
-    for (int w = threadIdx.x; w < OZ_S * 32 * 4; w += blockDim.x) {
+    for (int w = threadIdx.x; w < NW * 32 * 4; w += blockDim.x) {
         const int k = w / 128, c = (w / 4) % 32, g8 = w % 4;
         const int j = j0 + c;
         const long long t = t0 + g8 * 8;
@@ -365,7 +373,8 @@ constexpr int OZ_THREADS = (OZ_DRAIN_WARPS + 2) * 32;    // + producer warp + MM
 template <class Src, int NS>
 __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t full_bar[OZ_NST], empty_bar[OZ_NST], chunk_bar, drained_bar;
+    constexpr int NST = oz_nst(NS);
+    __shared__ __align__(8) uint64_t full_bar[OZ_NST_MAX], empty_bar[OZ_NST_MAX], chunk_bar, drained_bar;
     __shared__ uint32_t tmem_slot;
     __shared__ int s_fail;
     // the job lives in shared memory: each role reads its fields where it uses them, so
@@ -395,7 +404,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
 
     if (warp == 0) tc::tmem_alloc(&tmem_slot, OZ_TMEM_COLS);
     if (tid == 0) {
-        for (int b = 0; b < OZ_NST; ++b) {
+        for (int b = 0; b < NST; ++b) {
             tc::mbar_init(&full_bar[b], 1);
             tc::mbar_init(&empty_bar[b], 1);
         }
@@ -414,8 +423,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
             // a register copy: the copies' memory clobbers would reload a shared-memory field
             const uint8_t *__restrict__ dig = s_job.dig;
             for (long long st = 0; st < nst; ++st) {
-                const int b = (int)(st % OZ_NST);
-                if (st >= OZ_NST && !mbar_wait_fast(&empty_bar[b], (uint32_t)(((st / OZ_NST) - 1) & 1))) {
+                const int b = (int)(st % NST);
+                if (st >= NST && !mbar_wait_fast(&empty_bar[b], (uint32_t)(((st / NST) - 1) & 1))) {
                     atomicExch(&s_fail, 1);
                     break;
                 }
@@ -444,8 +453,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
                 const long long c0 = (long long)c * OZ_CHUNK_STEPS, c1 = min(c0 + OZ_CHUNK_STEPS, nst);
                 bool bad = false;
                 for (long long st = c0; st < c1; ++st) {
-                    const int b = (int)(st % OZ_NST);
-                    if (!mbar_wait_fast(&full_bar[b], (uint32_t)((st / OZ_NST) & 1))) {
+                    const int b = (int)(st % NST);
+                    if (!mbar_wait_fast(&full_bar[b], (uint32_t)((st / NST) & 1))) {
                         bad = true;
                         break;
                     }
@@ -769,7 +778,7 @@ static cudaError_t set_ozaki_smem() {
     static std::atomic<bool> done{false};  // per instantiation; the value set is the same for every caller
     if (done.load()) return cudaSuccess;
     const cudaError_t e = cudaFuncSetAttribute(corr_ozaki_kernel<Src, NS>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_NST * oz_stage_bytes(NS));
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, oz_nst(NS) * oz_stage_bytes(NS));
     if (e == cudaSuccess) done.store(true);
     return e;
 }
@@ -813,7 +822,7 @@ static cudaError_t launch_product(const Src &src, const long long *nb, cudaStrea
     note_launch(3);
     cudaError_t e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<Src, NS>());
     if (e != cudaSuccess) return e;
-    e = launch_stage(corr_ozaki_kernel<Src, NS>, nb[OZ_PRODUCT], OZ_THREADS, (size_t)OZ_NST * oz_stage_bytes(NS), src,
+    e = launch_stage(corr_ozaki_kernel<Src, NS>, nb[OZ_PRODUCT], OZ_THREADS, (size_t)oz_nst(NS) * oz_stage_bytes(NS), src,
                      s, "corr_ozaki_kernel launch");
     if (e != cudaSuccess) return e;
     e = launch_stage(ozaki_diag_kernel<Src>, nb[OZ_DIAG], 256, 0, src, s, "ozaki_diag_kernel launch");
@@ -923,7 +932,15 @@ cudaError_t corr_tc_batch_run_mode(void *ws, int count, const long long *stage_t
         t[st].active = mode == CORR_BATCH_FLAGGED ? active : nullptr;
     }
     cudaError_t e;
-    if (mode != CORR_BATCH_FLAGGED) {
+    if (mode == CORR_BATCH_FLAGGED) {
+        // the split run wrote five digit planes: the flagged jobs get all seven (their
+        // column statistics are still in their workspace)
+        note_launch(1);
+        if (dtype == GCSL_DTYPE_F64)
+            digit_split_kernel<double, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
+        else digit_split_kernel<float, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
+        if ((e = note_error("digit_split_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    } else {
         note_launch(4);
         colstats_init_kernel<JobTable><<<(unsigned)nb[OZ_INIT], 256, 0, s>>>(t[OZ_INIT]);
         if ((e = note_error("colstats_init_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
@@ -933,9 +950,15 @@ cudaError_t corr_tc_batch_run_mode(void *ws, int count, const long long *stage_t
         if ((e = note_error("colstats_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
         col_mean_exp_kernel<JobTable><<<(unsigned)nb[OZ_MEAN], 256, 0, s>>>(t[OZ_MEAN]);
         if ((e = note_error("col_mean_exp_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
-        if (dtype == GCSL_DTYPE_F64)
-            digit_split_kernel<double, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
-        else digit_split_kernel<float, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
+        if (mode == CORR_BATCH_SPLIT) {
+            if (dtype == GCSL_DTYPE_F64)
+                digit_split_kernel<double, JobTable, OZ_S_SPLIT><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
+            else digit_split_kernel<float, JobTable, OZ_S_SPLIT><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
+        } else {
+            if (dtype == GCSL_DTYPE_F64)
+                digit_split_kernel<double, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
+            else digit_split_kernel<float, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
+        }
         if ((e = note_error("digit_split_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
     }
     note_launch(3);
@@ -943,11 +966,11 @@ cudaError_t corr_tc_batch_run_mode(void *ws, int count, const long long *stage_t
         if ((e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<JobTable, OZ_S_SPLIT>())) != cudaSuccess)
             return e;
         corr_ozaki_kernel<JobTable, OZ_S_SPLIT>
-            <<<(unsigned)nb[OZ_PRODUCT], OZ_THREADS, OZ_NST * oz_stage_bytes(OZ_S_SPLIT), s>>>(t[OZ_PRODUCT]);
+            <<<(unsigned)nb[OZ_PRODUCT], OZ_THREADS, oz_nst(OZ_S_SPLIT) * oz_stage_bytes(OZ_S_SPLIT), s>>>(t[OZ_PRODUCT]);
     } else {
         if ((e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<JobTable, OZ_S>())) != cudaSuccess) return e;
         corr_ozaki_kernel<JobTable, OZ_S>
-            <<<(unsigned)nb[OZ_PRODUCT], OZ_THREADS, OZ_NST * oz_stage_bytes(OZ_S), s>>>(t[OZ_PRODUCT]);
+            <<<(unsigned)nb[OZ_PRODUCT], OZ_THREADS, oz_nst(OZ_S) * oz_stage_bytes(OZ_S), s>>>(t[OZ_PRODUCT]);
     }
     if ((e = note_error("corr_ozaki_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
     ozaki_diag_kernel<JobTable><<<(unsigned)nb[OZ_DIAG], 256, 0, s>>>(t[OZ_DIAG]);

@@ -116,6 +116,33 @@ class _Admission:
             self.used -= nbytes
 
 
+class _PinnedPool:
+    """Reusable pinned host buffers for result copies, by power-of-two size class and
+    shared by every server of the process.  Page-locking fresh host memory takes
+    milliseconds and can hold up the device, so each finished request borrows a staging
+    buffer, its results are copied out of it on a finishing thread, and it goes back."""
+
+    def __init__(self):
+        self.free: dict[int, list] = {}
+        self.lock = threading.Lock()
+
+    def get(self, nbytes: int):
+        torch = _lib.require_cuda()
+        cap = max(1 << 16, 1 << (max(int(nbytes), 1) - 1).bit_length())
+        with self.lock:
+            lst = self.free.get(cap)
+            if lst:
+                return lst.pop()
+        return torch.empty(cap, dtype=torch.uint8, pin_memory=True)
+
+    def put(self, buf):
+        with self.lock:
+            self.free.setdefault(buf.numel(), []).append(buf)
+
+
+_PINNED = _PinnedPool()
+
+
 class _Tick:
     """One tick of the Gaussian engine in flight: its completion event and what must
     stay alive until the stream has passed it."""
@@ -183,6 +210,7 @@ class SkeletonServer:
         I.state = j.state.data_ptr()
         j.inst = I
         j.next_level = 0
+        j.host = None
         return j
 
     def _enqueue_group(self, torch, jobs, first, last, finish, stream, keep):
@@ -251,12 +279,13 @@ class SkeletonServer:
                         with torch.cuda.stream(level_stream):
                             for i, j in enumerate(js):
                                 j.status = (st, i)
-                                j.host = (torch.empty(j.G.shape, dtype=torch.int16, pin_memory=True),
-                                          torch.empty(j.pmax.shape, dtype=torch.float64, pin_memory=True),
-                                          torch.empty(j.rec.shape, dtype=torch.int32, pin_memory=True))
-                                j.host[0].copy_(j.G, non_blocking=True)
-                                j.host[1].copy_(j.pmax, non_blocking=True)
-                                j.host[2].copy_(j.rec, non_blocking=True)
+                                pp = j.r.p * j.r.p
+                                buf = _PINNED.get(10 * pp + 4 * j.rec.numel())  # G, pmax, records
+                                j.host = buf
+                                buf[:8 * pp].view(torch.float64).copy_(j.pmax.view(-1), non_blocking=True)
+                                buf[8 * pp:10 * pp].view(torch.int16).copy_(j.G.view(-1), non_blocking=True)
+                                buf[10 * pp:10 * pp + 4 * j.rec.numel()].view(torch.int32).copy_(
+                                    j.rec, non_blocking=True)
                         finishing += js
                     else:
                         self._enqueue_group(torch, js, lv, lv, False, level_stream, keep)
@@ -286,10 +315,14 @@ class SkeletonServer:
             # single-problem path, which grows its pool
             G, sep, pm = self._solve_alone(r, j.C)
         else:
-            Gh, Ph, Rh = j.host
-            G = Gh.numpy().view(np.uint16)
-            pm = Ph.numpy()
-            sep = records_to_dense(Rh.numpy(), n_rec, r.p, r.max_level)
+            pp = r.p * r.p
+            h = j.host.numpy()
+            pm = h[:8 * pp].view(np.float64).reshape(r.p, r.p).copy()
+            G = h[8 * pp:10 * pp].view(np.uint16).reshape(r.p, r.p).copy()
+            sep = records_to_dense(h[10 * pp:10 * pp + 4 * n_rec].view(np.int32), n_rec, r.p, r.max_level)
+        if j.host is not None:
+            _PINNED.put(j.host)
+            j.host = None
         out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, j.adm_t, clock() - t0, j.batch))
         adm.release(j.nbytes)
 

@@ -290,9 +290,9 @@ int gcsl_corr_tc_batch_run(const gcsl_batch_plan *plan, void *stream);
  * products); c_err (device, count doubles) receives per instance a bound eps on the
  * distance of each entry of C to the seven-digit result, eps = 2.5 * 2^-35 (1.02 w +
  * sqrt(w)) with w = n / min_i sum_t y_ti^2 (y: centred, power-of-two-scaled samples).
- * The digit planes keep all seven digits. */
+ * Only five digit planes are written; the flagged run writes all seven for its jobs. */
 int gcsl_corr_tc_batch_run_split(const gcsl_batch_plan *plan, double *c_err, void *stream);
-/* The seven-digit product, diagonal and normalisation for the instances whose device
+/* The seven digit planes, their product, diagonal and normalisation for the instances whose device
  * flag (count int32) is non-zero, on the digits of the preceding run of the plan. */
 int gcsl_corr_tc_batch_run_flagged(const gcsl_batch_plan *plan, const int32_t *flags, void *stream);
 
