@@ -219,14 +219,8 @@ __global__ void col_mean_exp_kernel(Src src) {
 // padded to (p_pad, n_pad).  A 64-row operand tile is the first or second 2 KB half of a
 // block.  One CTA handles 32 samples x 32 columns.  Only the first NW digit planes are
 // written (the split-precision product reads five; the exact one seven).
-template <typename T, class Src, int NW = OZ_S>
-__global__ void digit_split_kernel(Src src) {
-    __shared__ int16_t tile[OZ_S][32][33];  // [digit][sample][column]; the top digit reaches 128
-    pdl_wait();
-    pdl_trigger();
-    long long lb;
-    const OzJob &Jb = src.get(blockIdx.x, lb);
-    if (src.skip(Jb.index)) return;  // not selected in this run (uniform over the block)
+template <typename T, int NW>
+__device__ __forceinline__ void digit_split_block(const OzJob &Jb, long long lb, int16_t (*tile)[32][33]) {
     const T *__restrict__ X = static_cast<const T *>(Jb.X);
     const long long n = Jb.n, ldx = Jb.ldx;
     const int p = Jb.p, p_pad = Jb.D.p_pad;
@@ -298,6 +292,34 @@ __global__ void digit_split_kernel(Src src) {
         const size_t off = (((size_t)k * nI + j / OZ_TM) * nq + q) * 4096 +
                            tc::kmajor_offset((uint32_t)(j % OZ_TM), (uint32_t)(t % 16));
         *reinterpret_cast<uint4 *>(dig + off) = make_uint4(word[0], word[1], word[2], word[3]);
+    }
+}
+
+template <typename T, class Src, int NW = OZ_S>
+__global__ void digit_split_kernel(Src src) {
+    __shared__ int16_t tile[OZ_S][32][33];  // [digit][sample][column]; the top digit reaches 128
+    pdl_wait();
+    pdl_trigger();
+    long long lb;
+    const OzJob &Jb = src.get(blockIdx.x, lb);
+    if (src.skip(Jb.index)) return;  // not selected in this run (uniform over the block)
+    digit_split_block<T, NW>(Jb, lb, tile);
+}
+
+// All seven digit planes of the flagged jobs only: a small grid strides over the flagged
+// jobs' tiles (the full grid of a batch is millions of blocks, nearly all of which would
+// only find their job unflagged).
+template <typename T>
+__global__ void digit_split_flagged_kernel(const OzJob *__restrict__ jobs, int count, const int *__restrict__ active) {
+    __shared__ int16_t tile[OZ_S][32][33];
+    for (int k = 0; k < count; ++k) {
+        if (active[k] == 0) continue;  // uniform over the block
+        const OzJob J = jobs[k];
+        const long long nb = (long long)(J.D.n_pad / 32) * (J.D.p_pad / 32);
+        for (long long lb = blockIdx.x; lb < nb; lb += gridDim.x) {
+            digit_split_block<T, OZ_S>(J, lb, tile);
+            __syncthreads();  // the tile is reused by the next block index
+        }
     }
 }
 
@@ -936,10 +958,10 @@ cudaError_t corr_tc_batch_run_mode(void *ws, int count, const long long *stage_t
         // the split run wrote five digit planes: the flagged jobs get all seven (their
         // column statistics are still in their workspace)
         note_launch(1);
-        if (dtype == GCSL_DTYPE_F64)
-            digit_split_kernel<double, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
-        else digit_split_kernel<float, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
-        if ((e = note_error("digit_split_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+        const unsigned fb = 608;  // a few blocks per SM stride over the flagged jobs' tiles
+        if (dtype == GCSL_DTYPE_F64) digit_split_flagged_kernel<double><<<fb, 256, 0, s>>>(jobs, count, active);
+        else digit_split_flagged_kernel<float><<<fb, 256, 0, s>>>(jobs, count, active);
+        if ((e = note_error("digit_split_flagged_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
     } else {
         note_launch(4);
         colstats_init_kernel<JobTable><<<(unsigned)nb[OZ_INIT], 256, 0, s>>>(t[OZ_INIT]);

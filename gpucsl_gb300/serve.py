@@ -279,13 +279,15 @@ class SkeletonServer:
                         with torch.cuda.stream(level_stream):
                             for i, j in enumerate(js):
                                 j.status = (st, i)
-                                pp = j.r.p * j.r.p
-                                buf = _PINNED.get(10 * pp + 4 * j.rec.numel())  # G, pmax, records
+                                # staging layout: pmax (8 p^2 bytes), records, G (2 p^2): every
+                                # part starts at a multiple of its element size
+                                pp, nr = j.r.p * j.r.p, j.rec.numel()
+                                buf = _PINNED.get(8 * pp + 4 * nr + 2 * pp)
                                 j.host = buf
                                 buf[:8 * pp].view(torch.float64).copy_(j.pmax.view(-1), non_blocking=True)
-                                buf[8 * pp:10 * pp].view(torch.int16).copy_(j.G.view(-1), non_blocking=True)
-                                buf[10 * pp:10 * pp + 4 * j.rec.numel()].view(torch.int32).copy_(
-                                    j.rec, non_blocking=True)
+                                buf[8 * pp:8 * pp + 4 * nr].view(torch.int32).copy_(j.rec, non_blocking=True)
+                                buf[8 * pp + 4 * nr:10 * pp + 4 * nr].view(torch.int16).copy_(
+                                    j.G.view(-1), non_blocking=True)
                         finishing += js
                     else:
                         self._enqueue_group(torch, js, lv, lv, False, level_stream, keep)
@@ -315,11 +317,11 @@ class SkeletonServer:
             # single-problem path, which grows its pool
             G, sep, pm = self._solve_alone(r, j.C)
         else:
-            pp = r.p * r.p
+            pp, nr = r.p * r.p, j.rec.numel()
             h = j.host.numpy()
             pm = h[:8 * pp].view(np.float64).reshape(r.p, r.p).copy()
-            G = h[8 * pp:10 * pp].view(np.uint16).reshape(r.p, r.p).copy()
-            sep = records_to_dense(h[10 * pp:10 * pp + 4 * n_rec].view(np.int32), n_rec, r.p, r.max_level)
+            sep = records_to_dense(h[8 * pp:8 * pp + 4 * n_rec].view(np.int32), n_rec, r.p, r.max_level)
+            G = h[8 * pp + 4 * nr:10 * pp + 4 * nr].view(np.uint16).reshape(r.p, r.p).copy()
         if j.host is not None:
             _PINNED.put(j.host)
             j.host = None
