@@ -16,6 +16,9 @@ the head waits rather than being overtaken).
   solve state in its own device slice across ticks, so a request that arrives while
   others are in flight joins at the next tick and a finished one leaves at once.  No
   host read happens between the levels of a request.
+* Gaussian requests with more than `solo_p` (400) variables, which fill the GPU on their
+  own, and requests deeper than the batched kernels' 12 levels go to two single-problem
+  workers (one stream each) instead.
 * Discrete requests go to worker threads, one stream each, which solve them
   concurrently through the single-problem path.
 * Finished requests are turned into the reference's output arrays (dense sepsets by the
@@ -164,8 +167,13 @@ class SkeletonServer:
     MAX_LEVEL = 12  # the batched level kernels' range; deeper requests take the single-problem path
 
     def __init__(self, budget_bytes: float = 120e9, discrete_workers: int = 3, finishing_threads: int = 4,
-                 max_inflight_ticks: int = 2):
+                 max_inflight_ticks: int = 2, solo_p: int = 400, solo_workers: int = 2):
         self.budget = int(budget_bytes)
+        # Gaussian requests with more variables than solo_p fill the GPU on their own: they
+        # gain nothing from sharing a plan, and the single-problem path (FP32-first tests,
+        # chunked walks) solves them faster than the batched FP64 level kernels
+        self.solo_p = int(solo_p)
+        self.solo_workers = max(1, int(solo_workers))
         # discrete solves of different requests overlap on the device: each worker owns a
         # stream, and one solve's host reads between levels leave the GPU to the others
         self.discrete_workers = max(1, int(discrete_workers))
@@ -249,7 +257,7 @@ class SkeletonServer:
                 new = list(q)
                 q.clear()
             for item in new:
-                if item[0].max_level > self.MAX_LEVEL:
+                if item[0].max_level > self.MAX_LEVEL or item[0].p > self.solo_p:
                     with solo_cv:
                         solo_q.append(item)
                         solo_cv.notify()
@@ -335,7 +343,8 @@ class SkeletonServer:
         return s.to_host()
 
     def _solo_worker(self, q, cv, stop, adm, out, t0, clock):
-        """Gaussian requests beyond the batched kernels' level range, one at a time."""
+        """Gaussian requests beyond the batched kernels' level range or above solo_p
+        variables, one at a time per worker (each worker owns a stream)."""
         torch = _lib.require_cuda()
         stream = torch.cuda.Stream()
         while True:
@@ -398,12 +407,13 @@ class SkeletonServer:
 
         wg = threading.Thread(target=self._guard, args=(self._gaussian_engine, errors, stop, qg, cvg, stop, adm, out,
                                                         t0, clock, _Fin(), qs, cvs), daemon=True)
-        ws = threading.Thread(target=self._guard, args=(self._solo_worker, errors, stop, qs, cvs, stop, adm, out, t0,
-                                                        clock), daemon=True)
+        wss = [threading.Thread(target=self._guard, args=(self._solo_worker, errors, stop, qs, cvs, stop, adm, out,
+                                                          t0, clock), daemon=True)
+               for _ in range(self.solo_workers)]
         wds = [threading.Thread(target=self._guard, args=(self._discrete_worker, errors, stop, qd, cvd, stop, adm,
                                                           out, t0, clock), daemon=True)
                for _ in range(self.discrete_workers)]
-        for w in [wg, ws] + wds:
+        for w in [wg] + wss + wds:
             w.start()
         pending = deque(sorted(trace, key=lambda r: r.arrival))
         waiting: deque = deque()  # arrived, not admitted (FIFO)
@@ -434,7 +444,7 @@ class SkeletonServer:
             for cv in (cvg, cvd, cvs):
                 with cv:
                     cv.notify_all()
-            for w in [wg, ws] + wds:
+            for w in [wg] + wss + wds:
                 w.join()
             finisher.shutdown(wait=True)
         if errors:
