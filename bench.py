@@ -511,11 +511,15 @@ def serving_leg(world: int = 1, rank: int = 0) -> dict:
     serve_plain(warm)
 
     def pooled(resp):
-        # (kind, arrival, done, batch) of every rank's responses; done / arrival share a clock
-        # per rank, so latencies and spans stay per rank and only the lists are pooled
-        rows = gather_lists([(r.kind, r.arrival, r.done, r.batch) for r in resp], world)
-        fake = [Response(0, k, None, None, None, a, a, d, b) for k, a, d, b in rows]
-        return latency_summary(fake)
+        # (rid, kind, arrival, done, batch) of every rank's responses; done / arrival share a
+        # clock per rank, so latencies and spans stay per rank and only the lists are pooled
+        rows = gather_lists([(r.rid, r.kind, r.arrival, r.done, r.batch) for r in resp], world)
+        fake = [Response(i, k, None, None, None, a, a, d, b) for i, k, a, d, b in rows]
+        out = latency_summary(fake)
+        worst = sorted(fake, key=lambda r: -r.latency)[:3]
+        out["slowest"] = [{"kind": r.kind, "p": sizes[r.rid][1], "n": sizes[r.rid][2],
+                           "ms": round(1e3 * r.latency, 2)} for r in worst]
+        return out
 
     rows = []
     for rate in SERVE_RATES:

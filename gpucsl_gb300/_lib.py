@@ -44,7 +44,7 @@ EXPORTED = [
     "gcsl_gauss_batch_flags", "gcsl_gauss_state_bytes", "gcsl_gauss_batch_table_bytes",
     "gcsl_gauss_batch_prepare_staged", "gcsl_gauss_batch_step", "gcsl_records_to_dense",
     "gcsl_orient_workspace_bytes", "gcsl_orient_edges", "gcsl_encode_workspace_bytes", "gcsl_ordinal_encode",
-    "gcsl_set_test_precision", "gcsl_debug_set_work_order",
+    "gcsl_set_test_precision", "gcsl_debug_set_work_order", "gcsl_set_blocks_per_sm_cap",
 ]
 
 GCSL_PREC_F64 = 0
@@ -231,6 +231,8 @@ def lib(debug: bool = False) -> ct.CDLL:
     L.gcsl_set_test_precision.argtypes = [_i32]
     L.gcsl_debug_set_work_order.restype = ct.c_int
     L.gcsl_debug_set_work_order.argtypes = [ct.c_uint64]
+    L.gcsl_set_blocks_per_sm_cap.restype = ct.c_int
+    L.gcsl_set_blocks_per_sm_cap.argtypes = [_i32]
     L.gcsl_encode_workspace_bytes.restype = _sz
     L.gcsl_encode_workspace_bytes.argtypes = [_i32]
     L.gcsl_ordinal_encode.restype = ct.c_int

@@ -455,6 +455,9 @@ static thread_local int g_test_precision = 0;
 // Work-order seed of the calling thread's solves (debug build; see gcsl_debug_set_work_order).
 static thread_local unsigned long long g_work_order = 0;
 
+// Cap on the resident blocks per SM of the discrete test kernel launched by this thread.
+static thread_local int g_blocks_cap = 0;
+
 bool mixed_tests() {
     static const bool mixed = [] {
         const char *e = getenv("GCSL_F64_TESTS");
@@ -520,6 +523,8 @@ DiscWs carve_disc(void *ws, size_t cap, int p) {
 }  // namespace
 
 unsigned long long gcsl::host::work_order_seed() { return GCSL_DEBUG_CHECKS ? g_work_order : 0ull; }
+
+int gcsl::host::blocks_per_sm_cap() { return g_blocks_cap; }
 
 int gcsl::host::gauss_skeleton_run(const double *C, int p, long long n_obs, const double *thresholds,
                                    int n_thresholds, int max_level, uint16_t *G, int *sepsets, int *rec_pool,
@@ -669,6 +674,12 @@ int gcsl_debug_set_work_order(uint64_t seed) {
     (void)seed;
     return GCSL_ERR_UNSUPPORTED;
 #endif
+}
+
+int gcsl_set_blocks_per_sm_cap(int32_t cap) {
+    if (cap < 0) return GCSL_ERR_INVALID_ARG;
+    g_blocks_cap = cap;
+    return GCSL_OK;
 }
 
 int gcsl_set_test_precision(int32_t mode) {

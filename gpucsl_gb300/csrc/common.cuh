@@ -27,6 +27,9 @@ cudaError_t note_error(const char *where, cudaError_t e);
 // The calling thread's work-order seed of the debug build (gcsl_debug_set_work_order; 0
 // in the release build).
 unsigned long long work_order_seed();
+// The calling thread's cap on resident blocks per SM of the long grid-stride test kernel
+// (gcsl_set_blocks_per_sm_cap; 0 = as many as fit).
+int blocks_per_sm_cap();
 // Modes of a batched correlation run (corr_tc.cu): every job with seven digits; every job
 // with five digits and an error bound; only flagged jobs, seven digits, on the digits of
 // a previous run.

@@ -676,6 +676,8 @@ cudaError_t launch_disc_tests(const DiscLevelArgs &A, int num_sms, cudaStream_t 
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, disc_test_kernel, 256, smem) != cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
+    const int cap = blocks_per_sm_cap();  // room left on every SM for concurrent solves
+    if (cap > 0 && per_sm > cap) per_sm = cap;
     disc_test_kernel<<<num_sms * per_sm, 256, smem, s>>>(A);
     note_launch(1);
     return note_error("disc_test_kernel launch", cudaGetLastError());

@@ -167,13 +167,15 @@ class SkeletonServer:
     MAX_LEVEL = 12  # the batched level kernels' range; deeper requests take the single-problem path
 
     def __init__(self, budget_bytes: float = 120e9, discrete_workers: int = 3, finishing_threads: int = 4,
-                 max_inflight_ticks: int = 2, solo_p: int = 400, solo_workers: int = 2):
+                 max_inflight_ticks: int = 2, solo_p: int = 400, solo_workers: int = 2,
+                 discrete_blocks_per_sm: int = 1):
         self.budget = int(budget_bytes)
         # Gaussian requests with more variables than solo_p fill the GPU on their own: they
         # gain nothing from sharing a plan, and the single-problem path (FP32-first tests,
         # chunked walks) solves them faster than the batched FP64 level kernels
         self.solo_p = int(solo_p)
         self.solo_workers = max(1, int(solo_workers))
+        self.discrete_blocks_per_sm = max(0, int(discrete_blocks_per_sm))
         # discrete solves of different requests overlap on the device: each worker owns a
         # stream, and one solve's host reads between levels leave the GPU to the others
         self.discrete_workers = max(1, int(discrete_workers))
@@ -243,8 +245,9 @@ class SkeletonServer:
 
     def _gaussian_engine(self, q, cv, stop, adm, out, t0, clock, finisher, solo_q, solo_cv):
         torch = _lib.require_cuda()
-        corr_stream = torch.cuda.Stream()
-        level_stream = torch.cuda.Stream()
+        # the engine's many short kernels take precedence over the long discrete ones
+        corr_stream = torch.cuda.Stream(priority=-1)
+        level_stream = torch.cuda.Stream(priority=-1)
         starting: list[_GaussJob] = []    # correlation enqueued, levels not started
         active: list[_GaussJob] = []      # levels in progress
         inflight: deque[_Tick] = deque()
@@ -346,7 +349,7 @@ class SkeletonServer:
         """Gaussian requests beyond the batched kernels' level range or above solo_p
         variables, one at a time per worker (each worker owns a stream)."""
         torch = _lib.require_cuda()
-        stream = torch.cuda.Stream()
+        stream = torch.cuda.Stream(priority=-1)
         while True:
             with cv:
                 while not q and not stop[0]:
@@ -363,6 +366,9 @@ class SkeletonServer:
     def _discrete_worker(self, q, cv, stop, adm, out, t0, clock):
         torch = _lib.require_cuda()
         stream = torch.cuda.Stream()
+        # a discrete level kernel strides over all its tests with resident blocks; at one
+        # block per SM it leaves room on every SM for the Gaussian solves next to it
+        _lib.check(_lib.lib().gcsl_set_blocks_per_sm_cap(self.discrete_blocks_per_sm), "gcsl_set_blocks_per_sm_cap")
         while True:
             with cv:
                 while not q and not stop[0]:

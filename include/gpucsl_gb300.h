@@ -79,6 +79,12 @@ int gcsl_set_test_precision(int32_t mode);
  * another seed reverses and rotates it).  Results must not depend on the order.  The
  * release library returns GCSL_ERR_UNSUPPORTED. */
 int gcsl_debug_set_work_order(uint64_t seed);
+/* Serving (no reference counterpart): caps the resident blocks per SM of the discrete
+ * test kernel (a grid-stride kernel that otherwise fills every SM for the whole level)
+ * launched by the calling thread; 0 = as many as fit.  A server that runs discrete
+ * solves next to other work sets it so that the other work finds room on every SM.
+ * Results do not depend on it. */
+int gcsl_set_blocks_per_sm_cap(int32_t cap);
 
 /* ------------------------------------------------------------ correlation (a) */
 /* Replaces gpucsl/pc/helpers.py:58-59 (correlation_matrix_of = np.corrcoef(data,
