@@ -513,12 +513,14 @@ def serving_leg(world: int = 1, rank: int = 0) -> dict:
     def pooled(resp):
         # (rid, kind, arrival, done, batch) of every rank's responses; done / arrival share a
         # clock per rank, so latencies and spans stay per rank and only the lists are pooled
-        rows = gather_lists([(r.rid, r.kind, r.arrival, r.done, r.batch) for r in resp], world)
-        fake = [Response(i, k, None, None, None, a, a, d, b) for i, k, a, d, b in rows]
+        rows = gather_lists([(r.rid, r.kind, r.arrival, r.admitted, r.done, r.batch, r.stages) for r in resp], world)
+        fake = [Response(i, k, None, None, None, a, ad, d, b, st) for i, k, a, ad, d, b, st in rows]
         out = latency_summary(fake)
         worst = sorted(fake, key=lambda r: -r.latency)[:3]
         out["slowest"] = [{"kind": r.kind, "p": sizes[r.rid][1], "n": sizes[r.rid][2],
-                           "ms": round(1e3 * r.latency, 2)} for r in worst]
+                           "ms": round(1e3 * r.latency, 2), "admitted_ms": round(1e3 * (r.admitted - r.arrival), 2),
+                           **({k: round(1e3 * (v - r.arrival), 2) for k, v in r.stages.items()} if r.stages else {})}
+                          for r in worst]
         return out
 
     rows = []

@@ -69,6 +69,7 @@ class Response:
     admitted: float
     done: float
     batch: int = 1            # instances solved together with it (itself included)
+    stages: dict | None = None  # Gaussian engine: seconds of its milestones after the trace start
 
     @property
     def latency(self) -> float:
@@ -158,7 +159,7 @@ class _Tick:
 class _GaussJob:
     """A Gaussian request in the engine: its device buffers and where it stands."""
     __slots__ = ("r", "adm_t", "nbytes", "X", "cws", "C", "G", "pmax", "rec", "state", "thr", "inst", "corr_ev",
-                 "next_level", "status", "host", "batch")
+                 "next_level", "status", "host", "batch", "stages")
 
 
 class SkeletonServer:
@@ -221,6 +222,7 @@ class SkeletonServer:
         j.inst = I
         j.next_level = 0
         j.host = None
+        j.stages = {}
         return j
 
     def _enqueue_group(self, torch, jobs, first, last, finish, stream, keep):
@@ -245,8 +247,10 @@ class SkeletonServer:
 
     def _gaussian_engine(self, q, cv, stop, adm, out, t0, clock, finisher, solo_q, solo_cv):
         torch = _lib.require_cuda()
-        # the engine's many short kernels take precedence over the long discrete ones
-        corr_stream = torch.cuda.Stream(priority=-1)
+        # the engine's many short kernels take precedence over the long discrete ones; the
+        # correlations of successive requests alternate between two streams (they overlap)
+        corr_streams = [torch.cuda.Stream(priority=-1) for _ in range(2)]
+        n_started = 0
         level_stream = torch.cuda.Stream(priority=-1)
         starting: list[_GaussJob] = []    # correlation enqueued, levels not started
         active: list[_GaussJob] = []      # levels in progress
@@ -265,8 +269,19 @@ class SkeletonServer:
                         solo_q.append(item)
                         solo_cv.notify()
                     continue
-                starting.append(self._start(item, torch, corr_stream))
+                j = self._start(item, torch, corr_streams[n_started % len(corr_streams)])
+                n_started += 1
+                j.stages["corr_enqueued"] = clock() - t0
+                starting.append(j)
+            # retire the ticks the stream has passed (without waiting)
+            while inflight and inflight[0].event.query():
+                t = inflight.popleft()
+                for j in t.finishing:
+                    j.stages["finish_done_seen"] = clock() - t0
+                    finisher.submit(self._finish_gaussian, j, out, adm, t0, clock)
             ready = [j for j in starting if j.corr_ev.query()]
+            for j in ready:
+                j.stages.setdefault("corr_done_seen", clock() - t0)
             starting = [j for j in starting if j not in ready]
             # a plan's instances share their level cap: groups by (next level, cap)
             groups, starts = {}, {}
@@ -275,6 +290,13 @@ class SkeletonServer:
             for j in ready:
                 starts.setdefault(j.r.max_level, []).append(j)
             keep, finishing = [], []
+            if (ready or active) and len(inflight) >= self.max_inflight:
+                # the level stream is busy: keep the correlation-finished requests for the
+                # next tick and come back for new arrivals
+                starting = ready + starting
+                ready = []
+                time.sleep(0.0001)
+                continue
             if ready or active:
                 for j in ready:
                     level_stream.wait_event(j.corr_ev)  # completed already: orders the stream after it
@@ -299,6 +321,8 @@ class SkeletonServer:
                                 buf[8 * pp:8 * pp + 4 * nr].view(torch.int32).copy_(j.rec, non_blocking=True)
                                 buf[8 * pp + 4 * nr:10 * pp + 4 * nr].view(torch.int16).copy_(
                                     j.G.view(-1), non_blocking=True)
+                        for j in js:
+                            j.stages["finish_enqueued"] = clock() - t0
                         finishing += js
                     else:
                         self._enqueue_group(torch, js, lv, lv, False, level_stream, keep)
@@ -308,16 +332,8 @@ class SkeletonServer:
                 ev = torch.cuda.Event()
                 ev.record(level_stream)
                 inflight.append(_Tick(ev, keep, finishing))
-            # retire ticks: when too many are in flight, or when nothing else can progress
-            idle = not active and not ready
-            while inflight and (len(inflight) > self.max_inflight or inflight[0].event.query() or
-                                (idle and not starting and not q)):
-                t = inflight.popleft()
-                t.event.synchronize()
-                for j in t.finishing:
-                    finisher.submit(self._finish_gaussian, j, out, adm, t0, clock)
-            if not ready and not active and starting:
-                time.sleep(0.0002)  # correlations running: nothing to step yet
+            if not ready and not active and (starting or inflight):
+                time.sleep(0.0002)  # correlations or the last ticks running: nothing to step yet
 
     def _finish_gaussian(self, j, out, adm, t0, clock):
         st, i = j.status
@@ -336,7 +352,7 @@ class SkeletonServer:
         if j.host is not None:
             _PINNED.put(j.host)
             j.host = None
-        out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, j.adm_t, clock() - t0, j.batch))
+        out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, j.adm_t, clock() - t0, j.batch, j.stages))
         adm.release(j.nbytes)
 
     @staticmethod
