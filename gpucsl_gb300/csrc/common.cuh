@@ -153,17 +153,19 @@ struct DevState {
     unsigned long long units[GCSL_MAX_LEVELS];      // key units reserved per level
 };
 
-// Chunked edges of a Gaussian level (the unit kernel walks their keys after the first
-// step in parallel units of 32 keys; the last unit of an edge combines them).
+// Chunked edges of a Gaussian level (the unit kernel walks their keys from key k0 -- 32
+// after a first step walked by the level kernel, 0 when the level kernel hands over the
+// whole edge -- in parallel units of 32 keys; the last unit of an edge combines them).
 struct HeavyEdge {
     int lo, hi;
     long long T;
-    long long unit_base;  // units unit_base .. unit_base + n_units - 1 (keys 32 (k + 1) ..)
+    long long unit_base;  // units unit_base .. unit_base + n_units - 1 (keys k0 + 32 k ..)
     int n_units;
     int done;             // units finished (atomic)
     long long best;       // smallest removing key found so far (atomic min; T when none)
-    double r2_0, ze_0;    // minima of the first step (no remover there)
+    double r2_0, ze_0;    // minima of the first step (no remover there; +inf when k0 = 0)
     double floor;         // the pair's exact rho^2 minimum before the level
+    long long k0;         // first key of the units
 };
 
 struct UnitRes {

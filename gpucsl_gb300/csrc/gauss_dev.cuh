@@ -769,8 +769,8 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
 // buffers are full, and the caller walks the remaining keys itself.  Whole group calls.
 template <int G>
 __device__ __forceinline__ bool register_chunked(const EdgeJob &J, int gl, const ChunkBufs &ck, DevState *st, int L,
-                                                 double r2_0, double ze_0, double floor) {
-    const long long nu = (J.T - G + G - 1) / G;
+                                                 double r2_0, double ze_0, double floor, long long k0 = G) {
+    const long long nu = (J.T - k0 + G - 1) / G;
     long long h = 0, ub = 0;
     if (gl == 0) {
         h = (long long)atomicAdd(&st->heavy[L], 1ull);
@@ -792,6 +792,7 @@ __device__ __forceinline__ bool register_chunked(const EdgeJob &J, int gl, const
             H.r2_0 = r2_0;
             H.ze_0 = ze_0;
             H.floor = floor;
+            H.k0 = k0;
             ck.heavy[h] = H;
         }
         for (long long k = gl; k < nu; k += G) ck.unit_h[ub + k] = (int)h;

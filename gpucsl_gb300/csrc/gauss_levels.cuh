@@ -74,6 +74,13 @@ __device__ __forceinline__ void level_edge_phase(const LevelCtx &x, const BinomR
     const int lane = threadIdx.x & 31;
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
     unsigned long long n_tests = 0, n_full = 0, n_removed = 0;
+    // Upper levels after a level that removed few edges: every edge's keys go to the unit
+    // phase from key 0 and nothing is walked here, which takes one step off the level's
+    // critical path (the first step's early exit, which the unit phase loses, rarely pays
+    // when removals are rare).  The previous level's counts are final: its kernels
+    // completed before this kernel's wait returned.
+    const bool hand_over = x.ck.heavy != nullptr && L >= 3 &&
+                           8ull * __ldcg(&st->removed[L - 1]) < __ldcg(&st->edges[L - 1]);
     for (long long e0 = w0; e0 < n_edges; e0 += nw) {
         const long long e = work_order(e0, n_edges, x.order);
         EdgeJob J;
@@ -87,6 +94,8 @@ __device__ __forceinline__ void level_edge_phase(const LevelCtx &x, const BinomR
         bool removed = false;
         // the pair's exact rho^2 minimum from earlier levels (level 0 stored r^2)
         const double floor = MIXED ? x.r2min[(size_t)J.lo * p + J.hi] : 0.0;
+        if (hand_over && register_chunked<32>(J, lane, x.ck, st, L, inf, inf, floor, 0))
+            continue;  // tests, minima and the removal come from the unit phase
         // an edge with more than one step of keys walks its first step here; without a
         // remover there, the unit phase walks the rest in parallel
         const bool chunk = x.ck.heavy != nullptr && J.T > CHUNK_MIN_KEYS;
@@ -129,6 +138,7 @@ __device__ __forceinline__ HeavyEdge load_heavy(const HeavyEdge *e) {
     H.r2_0 = __ldcg(&e->r2_0);
     H.ze_0 = __ldcg(&e->ze_0);
     H.floor = __ldcg(&e->floor);
+    H.k0 = __ldcg(&e->k0);
     return H;
 }
 
@@ -153,7 +163,7 @@ __device__ __forceinline__ void level_unit_phase(const LevelCtx &x, const BinomR
         const HeavyEdge H = load_heavy(ck.heavy + h);
         EdgeJob J;
         edge_job_of<L>(x.adj, p, H.lo, H.hi, L, J);
-        const long long m0 = (u - H.unit_base + 1) * 32;
+        const long long m0 = H.k0 + (u - H.unit_base) * 32;
         const long long m1 = m0 + 32 < H.T ? m0 + 32 : H.T;
         WalkRange rg{m0, m1, true, h, H.T};
         double r2 = inf, ze = inf;
@@ -186,7 +196,7 @@ __device__ __forceinline__ void level_unit_phase(const LevelCtx &x, const BinomR
         }
         double r2c = inf, zec = inf;
         for (int k = lane; k < H.n_units; k += 32) {
-            if ((long long)(k + 1) * 32 <= R) {  // the unit starts at or before the remover
+            if (H.k0 + (long long)k * 32 <= R) {  // the unit starts at or before the remover
                 r2c = fmin(r2c, __ldcg(&ck.units[H.unit_base + k].r2));
                 zec = fmin(zec, __ldcg(&ck.units[H.unit_base + k].ze));
             }
@@ -212,7 +222,7 @@ __device__ __forceinline__ void level_unit_phase(const LevelCtx &x, const BinomR
             const size_t ix = (size_t)J.lo * p + J.hi;
             if (zec < inf) atomic_min_nonneg_f64(x.zmin + ix, zec);
             if (r2c < inf) atomic_min_nonneg_f64(x.r2min + ix, r2c);
-            n_extra += (unsigned long long)((R < H.T ? R + 1 : H.T) - 32);
+            n_extra += (unsigned long long)((R < H.T ? R + 1 : H.T) - H.k0);
         }
     }
     if (lane == 0) {

@@ -144,7 +144,7 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
  * read the level loop's control words into the calling thread's stack.  Calls share
  * the array, so calls whose device work overlaps race and must be serialised. */
 #define GCSL_NOALLOC_MAX_P 512
-#define GCSL_NOALLOC_SCRATCH_BYTES 16526336
+#define GCSL_NOALLOC_SCRATCH_BYTES 17825792
 int gcsl_gauss_skeleton_noalloc(const double *C, int32_t p, int64_t n_obs, const double *thresholds,
                                 int32_t n_thresholds, int32_t max_level, uint16_t *G, int32_t *sepsets,
                                 int32_t *rec_pool, int64_t rec_cap, double *pmax, gcsl_stats *stats, void *stream);
