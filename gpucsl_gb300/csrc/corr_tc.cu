@@ -29,6 +29,7 @@
 // kernel writes eps per instance.  Instances whose tests cannot be decided exactly with
 // C' are flagged by the level loop and get the seven-digit product afterwards (the split
 // run writes five digit planes; the flagged jobs' seven are written by that later run).
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
@@ -93,6 +94,12 @@ struct OneJob {
         lb = b;
         return job;
     }
+    // also the first block index past the job's blocks in the stage (unbounded here)
+    __device__ __forceinline__ OzJob get(long long b, long long &lb, long long &end) const {
+        lb = b;
+        end = 0x7fffffffffffffffll;
+        return job;
+    }
     __device__ __forceinline__ bool skip(int) const { return false; }
     __device__ __forceinline__ double *err_slot(int) const { return nullptr; }
 };
@@ -105,6 +112,12 @@ struct JobTable {
     __device__ __forceinline__ OzJob get(long long b, long long &lb) const {
         const int k = upper_row(off, count, b);
         lb = b - off[k];
+        return jobs[k];
+    }
+    __device__ __forceinline__ OzJob get(long long b, long long &lb, long long &end) const {
+        const int k = upper_row(off, count, b);
+        lb = b - off[k];
+        end = off[k + 1];
         return jobs[k];
     }
     __device__ __forceinline__ bool skip(int index) const { return active != nullptr && active[index] == 0; }
@@ -144,22 +157,41 @@ __global__ void colstats_init_kernel(Src src) {
     }
 }
 
+// Persistent blocks over the `total` blocks of a stage: grid block b takes the contiguous
+// range [b per, (b + 1) per) and looks up the job once for each job its range enters
+// (thread 0, shared with the block through s_job), so a stage of millions of small
+// blocks (a batch's digit tiles) costs one job search per job and grid block rather than
+// one per block.  body(job, lb) runs for every block of the range with the whole block
+// and must end with a __syncthreads() when it reuses shared memory.
+template <class Src, class Body>
+__device__ __forceinline__ void stage_blocks(const Src &src, long long total, OzJob &s_job, long long (&s_rng)[2],
+                                             Body &&body) {
+    const long long per = (total + gridDim.x - 1) / gridDim.x;
+    long long b = (long long)blockIdx.x * per;
+    const long long b1 = min(total, b + per);
+    while (b < b1) {
+        if (threadIdx.x == 0) {
+            long long lb, end;
+            s_job = src.get(b, lb, end);
+            s_rng[0] = lb;
+            s_rng[1] = end;
+        }
+        __syncthreads();
+        const long long lb0 = s_rng[0], stop = min(b1, s_rng[1]);
+        for (long long i = 0; i < stop - b; ++i) body(s_job, lb0 + i);
+        b = stop;
+        __syncthreads();  // s_job is rewritten for the next job
+    }
+}
+
 // One read of X: per (512-sample chunk, column) FP64 partial sum in a fixed order, and
 // column min / max through ordered-key atomics.
-template <typename T, class Src>
-__global__ void colstats_kernel(Src src) {
-    __shared__ double ssum[8][32];
-    __shared__ long long smin[8][32], smax[8][32];
-    pdl_wait();
-    pdl_trigger();
-    long long lb;
-    const OzJob &Jb = src.get(blockIdx.x, lb);
+template <typename T>
+__device__ __forceinline__ void colstats_block(const OzJob &Jb, long long lb, double (*ssum)[32],
+                                               long long (*smin)[32], long long (*smax)[32]) {
     const T *__restrict__ X = static_cast<const T *>(Jb.X);
     const long long n = Jb.n, ldx = Jb.ldx;
     const int p = Jb.p;
-    double *__restrict__ partial = Jb.partial;
-    long long *__restrict__ kmin = Jb.kmin;
-    long long *__restrict__ kmax = Jb.kmax;
     const int nbx = (p + 31) / 32;
     const int bx = (int)(lb % nbx), by = (int)(lb / nbx);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -186,9 +218,29 @@ __global__ void colstats_kernel(Src src) {
             mn = smin[q][lane] < mn ? smin[q][lane] : mn;
             mx = smax[q][lane] > mx ? smax[q][lane] : mx;
         }
-        partial[(size_t)by * p + j] = sum;
-        atomicMin(&kmin[j], mn);
-        atomicMax(&kmax[j], mx);
+        Jb.partial[(size_t)by * p + j] = sum;
+        atomicMin(&Jb.kmin[j], mn);
+        atomicMax(&Jb.kmax[j], mx);
+    }
+    __syncthreads();  // the shared partials are reused by the next block of the range
+}
+
+// A single job: one block per stage block, the job from the kernel parameter; a batch:
+// persistent blocks over the stage (stage_blocks).
+template <typename T, class Src>
+__global__ void colstats_kernel(Src src, long long total) {
+    __shared__ double ssum[8][32];
+    __shared__ long long smin[8][32], smax[8][32];
+    pdl_wait();
+    pdl_trigger();
+    if constexpr (std::is_same<Src, OneJob>::value) {
+        (void)total;
+        colstats_block<T>(src.job, blockIdx.x, ssum, smin, smax);
+    } else {
+        __shared__ OzJob s_job;
+        __shared__ long long s_rng[2];
+        stage_blocks(src, total, s_job, s_rng,
+                     [&](const OzJob &J, long long lb) { colstats_block<T>(J, lb, ssum, smin, smax); });
     }
 }
 
@@ -219,7 +271,7 @@ __global__ void col_mean_exp_kernel(Src src) {
 // padded to (p_pad, n_pad).  A 64-row operand tile is the first or second 2 KB half of a
 // block.  One CTA handles 32 samples x 32 columns.  Only the first NW digit planes are
 // written (the split-precision product reads five; the exact one seven).
-template <typename T, int NW>
+template <typename T, int NW, bool PRELOAD = false>
 __device__ __forceinline__ void digit_split_block(const OzJob &Jb, long long lb, int16_t (*tile)[32][33]) {
     const T *__restrict__ X = static_cast<const T *>(Jb.X);
     const long long n = Jb.n, ldx = Jb.ldx;
@@ -232,14 +284,15 @@ __device__ __forceinline__ void digit_split_block(const OzJob &Jb, long long lb,
     const long long t0 = (lb % nbx) * 32;
     const int j0 = (int)(lb / nbx) * 32;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 warps
-    for (int r = ty; r < 32; r += 8) {
+    const int j = j0 + tx;
+    // digits of the sample in row r (x: the sample when in range) into the tile
+    auto split_row = [&](int r, double x) {
         const long long t = t0 + r;
-        const int j = j0 + tx;
         long long I = 0;
         if (t < n && j < p) {
             // y = fl(x - mean) as numpy centres; I = round(|y| 2^(49 - E)) with the sign of y,
             // from the bits of y: |y| = m 2^(ey - 1075), so I = round(m 2^(ey - 1075 + 49 - E)).
-            const double y = (double)X[t * ldx + j] - mean[j];
+            const double y = x - mean[j];
             const long long bits = __double_as_longlong(y);
             const int ey = (int)((bits >> 52) & 0x7ff);
             long long m = bits & 0xfffffffffffffll;
@@ -249,17 +302,20 @@ __device__ __forceinline__ void digit_split_block(const OzJob &Jb, long long lb,
             if (sh < 63) mag = (m + (1ll << (sh - 1))) >> sh;
             I = bits < 0 ? -mag : mag;
         }
-        // digits by rounding half up (arithmetic shifts); after the third digit the
-        // remainder is below 2^27 in magnitude and the rest runs in 32-bit arithmetic
-        long long rem = I;
+        // digits by rounding half up (arithmetic shifts), in 32-bit arithmetic: with
+        // I = H 2^21 + Lo (0 <= Lo < 2^21, |H| <= 2^28) the first three digits (weights
+        // 2^42, 2^35, 2^28) round at 2^41, 2^34, 2^27, all above Lo, so they follow from
+        // H alone: d = floor((H + 2^(s-1)) / 2^s) for s = 21, 14, 7 with H reduced after
+        // each; the remainder H 2^21 + Lo is then below 2^27 in magnitude
+        int hi = (int)(I >> 21);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            const int sh = 7 * (OZ_S - 1 - k);
-            const long long d = (rem + (1ll << (sh - 1))) >> sh;
-            rem -= d * (1ll << sh);
+            const int sh = 7 * (2 - k) + 7;  // 21, 14, 7
+            const int d = (hi + (1 << (sh - 1))) >> sh;
+            hi -= d * (1 << sh);
             tile[k][r][tx] = (int16_t)d;
         }
-        int rem32 = (int)rem;
+        int rem32 = hi * (1 << 21) + (int)(I & 0x1fffff);
 #pragma unroll
         for (int k = 3; k < OZ_S - 1; ++k) {
             const int sh = 7 * (OZ_S - 1 - k);
@@ -268,6 +324,21 @@ __device__ __forceinline__ void digit_split_block(const OzJob &Jb, long long lb,
             tile[k][r][tx] = (int16_t)d;
         }
         tile[OZ_S - 1][r][tx] = (int16_t)rem32;
+    };
+    auto sample = [&](int r) -> double {
+        const long long t = t0 + r;
+        return (t < n && j < p) ? (double)X[t * ldx + j] : 0.0;
+    };
+    if constexpr (PRELOAD) {
+        // the thread's four samples are loaded before any is split: the persistent batch
+        // kernel walks its blocks one after another, and nothing else hides their latency
+        double xv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) xv[i] = sample(ty + 8 * i);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) split_row(ty + 8 * i, xv[i]);
+    } else {
+        for (int r = ty; r < 32; r += 8) split_row(r, sample(r));
     }
     __syncthreads();
     const int nI = p_pad / OZ_TM;
@@ -296,14 +367,22 @@ __device__ __forceinline__ void digit_split_block(const OzJob &Jb, long long lb,
 }
 
 template <typename T, class Src, int NW = OZ_S>
-__global__ void digit_split_kernel(Src src) {
+__global__ void digit_split_kernel(Src src, long long total) {
     __shared__ int16_t tile[OZ_S][32][33];  // [digit][sample][column]; the top digit reaches 128
     pdl_wait();
     pdl_trigger();
-    long long lb;
-    const OzJob &Jb = src.get(blockIdx.x, lb);
-    if (src.skip(Jb.index)) return;  // not selected in this run (uniform over the block)
-    digit_split_block<T, NW>(Jb, lb, tile);
+    if constexpr (std::is_same<Src, OneJob>::value) {
+        (void)total;
+        digit_split_block<T, NW>(src.job, blockIdx.x, tile);
+    } else {
+        __shared__ OzJob s_job;
+        __shared__ long long s_rng[2];
+        stage_blocks(src, total, s_job, s_rng, [&](const OzJob &J, long long lb) {
+            if (src.skip(J.index)) return;  // not selected in this run (uniform over the block)
+            digit_split_block<T, NW, true>(J, lb, tile);
+            __syncthreads();  // the tile is reused by the next block of the range
+        });
+    }
 }
 
 // All seven digit planes of the flagged jobs only: a small grid strides over the flagged
@@ -805,21 +884,61 @@ static cudaError_t set_ozaki_smem() {
     return e;
 }
 
+
 // Stage launches shared by the single-job and batched paths; nb[] = blocks per stage.
 // One stage: the single-job path launches with programmatic dependent launch (each
 // kernel waits for its predecessor with pdl_wait); the batched path, captured into CUDA
 // graphs, launches plainly.
-template <class Src, typename K>
+template <class Src, typename K, typename... A>
 static cudaError_t launch_stage(K kernel, long long blocks, int threads, size_t smem, const Src &src, cudaStream_t s,
-                                const char *what) {
+                                const char *what, A... extra) {
     cudaError_t e;
     if constexpr (std::is_same<Src, OneJob>::value) {
-        e = launch_pdl(kernel, dim3((unsigned)blocks), dim3(threads), smem, s, src);
+        e = launch_pdl(kernel, dim3((unsigned)blocks), dim3(threads), smem, s, src, extra...);
     } else {
-        kernel<<<(unsigned)blocks, threads, smem, s>>>(src);
+        kernel<<<(unsigned)blocks, threads, smem, s>>>(src, extra...);
         e = cudaGetLastError();
     }
     return note_error(what, e);
+}
+
+// Grid of a persistent stage kernel (stage_blocks): as many 256-thread blocks as are
+// resident at once, at most one per stage block.
+template <typename K>
+static long long persistent_grid(K kernel, long long total) {
+    // resident blocks per SM, once per kernel (kernels of one signature share K)
+    static std::mutex mu;
+    static std::vector<std::pair<const void *, int>> known;
+    int occ = 0;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        for (const auto &kv : known)
+            if (kv.first == (const void *)kernel) occ = kv.second;
+        if (occ == 0) {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0) != cudaSuccess || occ < 1) occ = 1;
+            known.emplace_back((const void *)kernel, occ);
+        }
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+    return std::max(1ll, std::min(total, (long long)sms * occ));
+}
+
+// Launches a stage kernel written with stage_blocks over `total` stage blocks: a batch
+// with as many blocks as are resident (each walks a range of its stage's blocks), a
+// single job with one block per stage block (there is no job to look up, and the
+// block turnover overlaps the loads of new blocks with the stores of finishing ones).
+template <class Src, typename K>
+static cudaError_t launch_persistent(K kernel, long long total, const Src &src, cudaStream_t s, const char *what) {
+    const long long grid = std::is_same<Src, OneJob>::value ? total : persistent_grid(kernel, total);
+    return launch_stage(kernel, grid, 256, 0, src, s, what, total);
+}
+
+template <class Src, int NS>
+static cudaError_t launch_ozaki(const Src &src, long long blocks, cudaStream_t s) {
+    return launch_stage(corr_ozaki_kernel<Src, NS>, blocks, OZ_THREADS, (size_t)oz_nst(NS) * oz_stage_bytes(NS), src, s,
+                        "corr_ozaki_kernel launch");
 }
 
 // Stage launches shared by the single-job and batched paths; nb[] = blocks per stage.
@@ -829,14 +948,14 @@ static cudaError_t launch_digits(const Src &src, const long long *nb, int dtype,
     cudaError_t e = launch_stage(colstats_init_kernel<Src>, nb[OZ_INIT], 256, 0, src, s, "colstats_init_kernel launch");
     if (e != cudaSuccess) return e;
     e = dtype == GCSL_DTYPE_F64
-            ? launch_stage(colstats_kernel<double, Src>, nb[OZ_STATS], 256, 0, src, s, "colstats_kernel launch")
-            : launch_stage(colstats_kernel<float, Src>, nb[OZ_STATS], 256, 0, src, s, "colstats_kernel launch");
+            ? launch_persistent(colstats_kernel<double, Src>, nb[OZ_STATS], src, s, "colstats_kernel launch")
+            : launch_persistent(colstats_kernel<float, Src>, nb[OZ_STATS], src, s, "colstats_kernel launch");
     if (e != cudaSuccess) return e;
     e = launch_stage(col_mean_exp_kernel<Src>, nb[OZ_MEAN], 256, 0, src, s, "col_mean_exp_kernel launch");
     if (e != cudaSuccess) return e;
     return dtype == GCSL_DTYPE_F64
-               ? launch_stage(digit_split_kernel<double, Src>, nb[OZ_DIGITS], 256, 0, src, s, "digit_split_kernel launch")
-               : launch_stage(digit_split_kernel<float, Src>, nb[OZ_DIGITS], 256, 0, src, s, "digit_split_kernel launch");
+               ? launch_persistent(digit_split_kernel<double, Src>, nb[OZ_DIGITS], src, s, "digit_split_kernel launch")
+               : launch_persistent(digit_split_kernel<float, Src>, nb[OZ_DIGITS], src, s, "digit_split_kernel launch");
 }
 
 template <class Src, int NS = OZ_S>
@@ -844,8 +963,7 @@ static cudaError_t launch_product(const Src &src, const long long *nb, cudaStrea
     note_launch(3);
     cudaError_t e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<Src, NS>());
     if (e != cudaSuccess) return e;
-    e = launch_stage(corr_ozaki_kernel<Src, NS>, nb[OZ_PRODUCT], OZ_THREADS, (size_t)oz_nst(NS) * oz_stage_bytes(NS), src,
-                     s, "corr_ozaki_kernel launch");
+    e = launch_ozaki<Src, NS>(src, nb[OZ_PRODUCT], s);
     if (e != cudaSuccess) return e;
     e = launch_stage(ozaki_diag_kernel<Src>, nb[OZ_DIAG], 256, 0, src, s, "ozaki_diag_kernel launch");
     if (e != cudaSuccess) return e;
@@ -966,35 +1084,33 @@ cudaError_t corr_tc_batch_run_mode(void *ws, int count, const long long *stage_t
         note_launch(4);
         colstats_init_kernel<JobTable><<<(unsigned)nb[OZ_INIT], 256, 0, s>>>(t[OZ_INIT]);
         if ((e = note_error("colstats_init_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
-        if (dtype == GCSL_DTYPE_F64)
-            colstats_kernel<double, JobTable><<<(unsigned)nb[OZ_STATS], 256, 0, s>>>(t[OZ_STATS]);
-        else colstats_kernel<float, JobTable><<<(unsigned)nb[OZ_STATS], 256, 0, s>>>(t[OZ_STATS]);
-        if ((e = note_error("colstats_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+        e = dtype == GCSL_DTYPE_F64
+                ? launch_persistent(colstats_kernel<double, JobTable>, nb[OZ_STATS], t[OZ_STATS], s, "colstats_kernel launch")
+                : launch_persistent(colstats_kernel<float, JobTable>, nb[OZ_STATS], t[OZ_STATS], s, "colstats_kernel launch");
+        if (e != cudaSuccess) return e;
         col_mean_exp_kernel<JobTable><<<(unsigned)nb[OZ_MEAN], 256, 0, s>>>(t[OZ_MEAN]);
         if ((e = note_error("col_mean_exp_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
-        if (mode == CORR_BATCH_SPLIT) {
-            if (dtype == GCSL_DTYPE_F64)
-                digit_split_kernel<double, JobTable, OZ_S_SPLIT><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
-            else digit_split_kernel<float, JobTable, OZ_S_SPLIT><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
-        } else {
-            if (dtype == GCSL_DTYPE_F64)
-                digit_split_kernel<double, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
-            else digit_split_kernel<float, JobTable><<<(unsigned)nb[OZ_DIGITS], 256, 0, s>>>(t[OZ_DIGITS]);
-        }
-        if ((e = note_error("digit_split_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+        const JobTable &td = t[OZ_DIGITS];
+        const char *what = "digit_split_kernel launch";
+        if (mode == CORR_BATCH_SPLIT)
+            e = dtype == GCSL_DTYPE_F64
+                    ? launch_persistent(digit_split_kernel<double, JobTable, OZ_S_SPLIT>, nb[OZ_DIGITS], td, s, what)
+                    : launch_persistent(digit_split_kernel<float, JobTable, OZ_S_SPLIT>, nb[OZ_DIGITS], td, s, what);
+        else
+            e = dtype == GCSL_DTYPE_F64 ? launch_persistent(digit_split_kernel<double, JobTable>, nb[OZ_DIGITS], td, s, what)
+                                        : launch_persistent(digit_split_kernel<float, JobTable>, nb[OZ_DIGITS], td, s, what);
+        if (e != cudaSuccess) return e;
     }
     note_launch(3);
     if (mode == CORR_BATCH_SPLIT) {
         if ((e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<JobTable, OZ_S_SPLIT>())) != cudaSuccess)
             return e;
-        corr_ozaki_kernel<JobTable, OZ_S_SPLIT>
-            <<<(unsigned)nb[OZ_PRODUCT], OZ_THREADS, oz_nst(OZ_S_SPLIT) * oz_stage_bytes(OZ_S_SPLIT), s>>>(t[OZ_PRODUCT]);
+        e = launch_ozaki<JobTable, OZ_S_SPLIT>(t[OZ_PRODUCT], nb[OZ_PRODUCT], s);
     } else {
         if ((e = note_error("corr_ozaki_kernel attribute", set_ozaki_smem<JobTable, OZ_S>())) != cudaSuccess) return e;
-        corr_ozaki_kernel<JobTable, OZ_S>
-            <<<(unsigned)nb[OZ_PRODUCT], OZ_THREADS, oz_nst(OZ_S) * oz_stage_bytes(OZ_S), s>>>(t[OZ_PRODUCT]);
+        e = launch_ozaki<JobTable, OZ_S>(t[OZ_PRODUCT], nb[OZ_PRODUCT], s);
     }
-    if ((e = note_error("corr_ozaki_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
+    if (e != cudaSuccess) return e;
     ozaki_diag_kernel<JobTable><<<(unsigned)nb[OZ_DIAG], 256, 0, s>>>(t[OZ_DIAG]);
     if ((e = note_error("ozaki_diag_kernel launch", cudaGetLastError())) != cudaSuccess) return e;
     ozaki_finish_kernel<JobTable><<<(unsigned)nb[OZ_FINISH], 256, 0, s>>>(t[OZ_FINISH]);

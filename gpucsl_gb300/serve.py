@@ -23,6 +23,14 @@ the head waits rather than being overtaken).
   concurrently through the single-problem path.
 * Finished requests are turned into the reference's output arrays (dense sepsets by the
   library's host routine, outside the GIL) by a pool of finishing threads.
+* Without a backlog the batching is skipped: while nothing is in flight concurrently
+  and at most `exclusive_backlog` (4) requests wait, the request at the head of the
+  queue is solved alone on the whole device through the single-problem path, by the
+  dispatching thread on its current stream, exactly as the plain path does, and the
+  next one waits for it.
+  Once more requests wait (or concurrent work is still in flight), every waiting request
+  goes to the concurrent engines above.  Sharing the device only pays when requests
+  queue up; at low load it only slows each request down.
 
 Latency is measured from a request's arrival to the moment its results are on the
 host.  `serve_plain` serves the same trace one request at a time through the plain
@@ -33,10 +41,11 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import ctypes as ct
+import sys
 import threading
 import time
 from collections import deque
-from dataclasses import dataclass
+from dataclasses import dataclass, replace
 
 import numpy as np
 
@@ -70,6 +79,7 @@ class Response:
     done: float
     batch: int = 1            # instances solved together with it (itself included)
     stages: dict | None = None  # Gaussian engine: seconds of its milestones after the trace start
+    path: str = "plain"       # server: "exclusive", "batched", "solo" or "discrete"
 
     @property
     def latency(self) -> float:
@@ -120,6 +130,37 @@ class _Admission:
             self.used -= nbytes
 
 
+class _Flow:
+    """Requests in flight on the concurrent engines (thread-safe).  Every completion
+    wakes the dispatcher, which otherwise sleeps until the next arrival (no polling
+    thread competes for the interpreter lock)."""
+
+    def __init__(self):
+        self.concurrent = 0
+        self.events = 0
+        self.cv = threading.Condition()
+
+    def state(self) -> tuple[int, int]:
+        with self.cv:
+            return self.concurrent, self.events
+
+    def started(self):
+        with self.cv:
+            self.concurrent += 1
+
+    def finished(self):
+        with self.cv:
+            self.concurrent -= 1
+            self.events += 1
+            self.cv.notify_all()
+
+    def wait(self, seen: int, timeout: float):
+        """Sleeps up to `timeout` seconds unless a request finished since `seen`."""
+        with self.cv:
+            if self.events == seen and timeout > 0:
+                self.cv.wait(timeout)
+
+
 class _PinnedPool:
     """Reusable pinned host buffers for result copies, by power-of-two size class and
     shared by every server of the process.  Page-locking fresh host memory takes
@@ -146,6 +187,23 @@ class _PinnedPool:
 
 _PINNED = _PinnedPool()
 
+_STREAMS: dict = {}
+_STREAMS_LOCK = threading.Lock()
+
+
+def _stream(role: str, index: int = 0, priority: int = 0):
+    """The process's stream for a server role on the current device, created once.
+    PyTorch's caching allocator keeps a pool per stream, so a server that made fresh
+    streams per call would find none of the device buffers cached by earlier calls (or by
+    a warm-up) and pay a device allocation for every request size it meets again."""
+    torch = _lib.require_cuda()
+    key = (torch.cuda.current_device(), role, index)
+    with _STREAMS_LOCK:
+        st = _STREAMS.get(key)
+        if st is None:
+            st = _STREAMS[key] = torch.cuda.Stream(priority=priority)
+        return st
+
 
 class _Tick:
     """One tick of the Gaussian engine in flight: its completion event and what must
@@ -169,8 +227,15 @@ class SkeletonServer:
 
     def __init__(self, budget_bytes: float = 120e9, discrete_workers: int = 3, finishing_threads: int = 4,
                  max_inflight_ticks: int = 2, solo_p: int = 400, solo_workers: int = 2,
-                 discrete_blocks_per_sm: int = 1):
+                 discrete_blocks_per_sm: int = 1, exclusive_backlog: int = 4, switch_interval: float = 5e-4):
         self.budget = int(budget_bytes)
+        # waiting requests up to which the head of the queue is solved alone (negative:
+        # never, every request goes to the concurrent engines)
+        self.exclusive_backlog = int(exclusive_backlog)
+        # the engine thread steps levels in short slices of Python; with the interpreter's
+        # default 5 ms switch interval a busy finishing or worker thread holds it off for
+        # whole milliseconds per tick
+        self.switch_interval = float(switch_interval)
         # Gaussian requests with more variables than solo_p fill the GPU on their own: they
         # gain nothing from sharing a plan, and the single-problem path (FP32-first tests,
         # chunked walks) solves them faster than the batched FP64 level kernels
@@ -249,16 +314,16 @@ class SkeletonServer:
         torch = _lib.require_cuda()
         # the engine's many short kernels take precedence over the long discrete ones; the
         # correlations of successive requests alternate between two streams (they overlap)
-        corr_streams = [torch.cuda.Stream(priority=-1) for _ in range(2)]
+        corr_streams = [_stream("corr", i, priority=-1) for i in range(2)]
         n_started = 0
-        level_stream = torch.cuda.Stream(priority=-1)
+        level_stream = _stream("levels", priority=-1)
         starting: list[_GaussJob] = []    # correlation enqueued, levels not started
         active: list[_GaussJob] = []      # levels in progress
         inflight: deque[_Tick] = deque()
         while True:
             with cv:
                 while not q and not starting and not active and not inflight and not stop[0]:
-                    cv.wait(0.001)
+                    cv.wait(0.05)  # woken by every enqueue and by stop
                 if stop[0] and not (q or starting or active or inflight):
                     return
                 new = list(q)
@@ -352,8 +417,10 @@ class SkeletonServer:
         if j.host is not None:
             _PINNED.put(j.host)
             j.host = None
-        out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, j.adm_t, clock() - t0, j.batch, j.stages))
+        out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, j.adm_t, clock() - t0, j.batch, j.stages,
+                            "batched"))
         adm.release(j.nbytes)
+        self._flow.finished()
 
     @staticmethod
     def _solve_alone(r, C):
@@ -361,34 +428,35 @@ class SkeletonServer:
         s.run(C, r.n, gaussian_thresholds(r.n, r.alpha))
         return s.to_host()
 
-    def _solo_worker(self, q, cv, stop, adm, out, t0, clock):
+    def _solo_worker(self, q, cv, stop, adm, out, t0, clock, idx):
         """Gaussian requests beyond the batched kernels' level range or above solo_p
         variables, one at a time per worker (each worker owns a stream)."""
         torch = _lib.require_cuda()
-        stream = torch.cuda.Stream(priority=-1)
+        stream = _stream("solo", idx, priority=-1)
         while True:
             with cv:
                 while not q and not stop[0]:
-                    cv.wait(0.001)
+                    cv.wait(0.05)  # woken by every enqueue and by stop
                 if not q and stop[0]:
                     return
                 r, adm_t, nbytes = q.popleft()
             with torch.cuda.stream(stream):
                 X = r.samples.to("cuda", non_blocking=True)
                 G, sep, pm = self._solve_alone(r, correlation(X))
-            out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, adm_t, clock() - t0))
+            out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, adm_t, clock() - t0, path="solo"))
             adm.release(nbytes)
+            self._flow.finished()
 
-    def _discrete_worker(self, q, cv, stop, adm, out, t0, clock):
+    def _discrete_worker(self, q, cv, stop, adm, out, t0, clock, idx):
         torch = _lib.require_cuda()
-        stream = torch.cuda.Stream()
+        stream = _stream("discrete", idx)
         # a discrete level kernel strides over all its tests with resident blocks; at one
         # block per SM it leaves room on every SM for the Gaussian solves next to it
         _lib.check(_lib.lib().gcsl_set_blocks_per_sm_cap(self.discrete_blocks_per_sm), "gcsl_set_blocks_per_sm_cap")
         while True:
             with cv:
                 while not q and not stop[0]:
-                    cv.wait(0.001)
+                    cv.wait(0.05)  # woken by every enqueue and by stop
                 if not q and stop[0]:
                     return
                 r, adm_t, nbytes = q.popleft()
@@ -399,15 +467,31 @@ class SkeletonServer:
                 ds.load(codes_dev=codes, dims_dev=dims)
                 ds.run(r.alpha)
                 G, sep, pm = ds.to_host()
-            out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, adm_t, clock() - t0))
+            out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, adm_t, clock() - t0, path="discrete"))
             adm.release(nbytes)
+            self._flow.finished()
             del ds, codes
 
     # -------------------------------------------------------------- serve
+    def warmup(self, requests: list[Request]):
+        """Serves every request once through the concurrent engines and once alone (all
+        arriving at once), so that the device buffers of every size the requests need are
+        cached on each stream the server uses."""
+        trace = [replace(r, arrival=0.0) for r in requests]
+        saved = self.exclusive_backlog
+        try:
+            self.exclusive_backlog = -1
+            self.serve(trace)
+            self.exclusive_backlog = len(trace) + 1
+            self.serve(trace)
+        finally:
+            self.exclusive_backlog = saved
+
     def serve(self, trace: list[Request], clock=time.perf_counter) -> list[Response]:
         """Serve `trace` (arrival times relative to the call) and return one response per
         request, in completion order."""
         adm = _Admission(self.budget)
+        self._flow = flow = _Flow()
         qg, qd, qs = deque(), deque(), deque()
         cvg, cvd, cvs = threading.Condition(), threading.Condition(), threading.Condition()
         stop = [False]
@@ -430,12 +514,15 @@ class SkeletonServer:
         wg = threading.Thread(target=self._guard, args=(self._gaussian_engine, errors, stop, qg, cvg, stop, adm, out,
                                                         t0, clock, _Fin(), qs, cvs), daemon=True)
         wss = [threading.Thread(target=self._guard, args=(self._solo_worker, errors, stop, qs, cvs, stop, adm, out,
-                                                          t0, clock), daemon=True)
-               for _ in range(self.solo_workers)]
+                                                          t0, clock, i), daemon=True)
+               for i in range(self.solo_workers)]
         wds = [threading.Thread(target=self._guard, args=(self._discrete_worker, errors, stop, qd, cvd, stop, adm,
-                                                          out, t0, clock), daemon=True)
-               for _ in range(self.discrete_workers)]
-        for w in [wg] + wss + wds:
+                                                          out, t0, clock, i), daemon=True)
+               for i in range(self.discrete_workers)]
+        workers = [wg] + wss + wds
+        old_switch = sys.getswitchinterval()
+        sys.setswitchinterval(self.switch_interval)
+        for w in workers:
             w.start()
         pending = deque(sorted(trace, key=lambda r: r.arrival))
         waiting: deque = deque()  # arrived, not admitted (FIFO)
@@ -446,57 +533,75 @@ class SkeletonServer:
                 now = clock() - t0
                 while pending and pending[0].arrival <= now:
                     waiting.append(pending.popleft())
-                while waiting:
-                    r = waiting[0]
-                    nbytes = footprint(r)
-                    if not adm.try_admit(nbytes):
-                        break
-                    waiting.popleft()
-                    item = (r, clock() - t0, nbytes)
-                    q, cv = (qg, cvg) if r.kind == "gaussian" else (qd, cvd)
-                    with cv:
-                        q.append(item)
-                        cv.notify()
-                if pending and not waiting:
-                    time.sleep(max(0.0, min(0.0005, pending[0].arrival - (clock() - t0))))
-                elif waiting:
-                    time.sleep(0.0002)
+                concurrent, seen = flow.state()
+                if waiting and concurrent == 0 and len(waiting) <= self.exclusive_backlog:
+                    # no backlog and nothing in flight: the head is solved alone, here, on
+                    # this thread's current stream (what the plain path does); arrivals
+                    # meanwhile queue up behind it
+                    r = waiting.popleft()
+                    adm_t = clock() - t0
+                    G, sep, pm = solve_plain(r)
+                    out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, adm_t, clock() - t0, path="exclusive"))
+                    continue
+                else:
+                    while waiting:
+                        r = waiting[0]
+                        nbytes = footprint(r)
+                        if not adm.try_admit(nbytes):
+                            break
+                        waiting.popleft()
+                        flow.started()
+                        item = (r, clock() - t0, nbytes)
+                        q, cv = (qg, cvg) if r.kind == "gaussian" else (qd, cvd)
+                        with cv:
+                            q.append(item)
+                            cv.notify()
+                # sleep until the next arrival, or until a request finishes when some wait
+                # (for the exclusive worker or for budget)
+                until_next = pending[0].arrival - (clock() - t0) if pending else 0.05
+                flow.wait(seen, min(until_next, 0.05) if waiting else until_next)
         finally:
             stop[0] = True
             for cv in (cvg, cvd, cvs):
                 with cv:
                     cv.notify_all()
-            for w in [wg] + wss + wds:
+            for w in workers:
                 w.join()
             finisher.shutdown(wait=True)
+            sys.setswitchinterval(old_switch)
         if errors:
             raise errors[0]
         return out
 
 
+def solve_plain(r: Request):
+    """One request through the plain single-problem API on the current stream:
+    (skeleton, sepsets, pmax) on the host."""
+    torch = _lib.require_cuda()
+    if r.kind == "gaussian":
+        X = r.samples.to("cuda", non_blocking=True)
+        C = correlation(X)
+        s = GaussianSolver(r.p, r.max_level)
+        s.run(C, r.n, gaussian_thresholds(r.n, r.alpha))
+        return s.to_host()
+    ds = DiscreteSolver(r.p, r.n, r.max_level, int(r.dims.max()))
+    codes = r.codes.to("cuda", non_blocking=True)
+    dims = torch.from_numpy(np.ascontiguousarray(r.dims, dtype=np.uint8)).to("cuda", non_blocking=True)
+    ds.load(codes_dev=codes, dims_dev=dims)
+    ds.run(r.alpha)
+    return ds.to_host()
+
+
 def serve_plain(trace: list[Request], clock=time.perf_counter) -> list[Response]:
     """The same trace through the plain single-problem API, one request at a time in
     arrival order (a request waits for its arrival and for the previous one)."""
-    torch = _lib.require_cuda()
     out: list[Response] = []
     t0 = clock()
     for r in sorted(trace, key=lambda r: r.arrival):
         while clock() - t0 < r.arrival:
             time.sleep(max(0.0, min(0.0005, r.arrival - (clock() - t0))))
         start = clock() - t0
-        if r.kind == "gaussian":
-            X = r.samples.to("cuda", non_blocking=True)
-            C = correlation(X)
-            s = GaussianSolver(r.p, r.max_level)
-            s.run(C, r.n, gaussian_thresholds(r.n, r.alpha))
-            G, sep, pm = s.to_host()
-        else:
-            ds = DiscreteSolver(r.p, r.n, r.max_level, int(r.dims.max()))
-            codes = r.codes.to("cuda", non_blocking=True)
-            dims = torch.from_numpy(np.ascontiguousarray(r.dims, dtype=np.uint8)).to("cuda")
-            ds.load(codes_dev=codes, dims_dev=dims)
-            ds.run(r.alpha)
-            G, sep, pm = ds.to_host()
+        G, sep, pm = solve_plain(r)
         out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, start, clock() - t0))
     return out
 
@@ -513,6 +618,10 @@ def latency_summary(resp: list[Response]) -> dict:
                 "mean_batch": round(float(np.mean([r.batch for r in rs])), 2)}
 
     out = summ(resp)
+    paths: dict[str, int] = {}
+    for r in resp:
+        paths[r.path] = paths.get(r.path, 0) + 1
+    out["paths"] = paths
     for kind in ("gaussian", "discrete"):
         rs = [r for r in resp if r.kind == kind]
         if rs:

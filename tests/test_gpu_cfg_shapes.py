@@ -120,7 +120,7 @@ def test_cfg5_shapes_served_equal_plain(cfg5_requests):
 
     trace = poisson_arrivals(cfg5_requests, rate=200.0, seed=5)
     plain = {r.rid: r for r in serve_plain(trace)}
-    served = SkeletonServer(budget_bytes=120e9).serve(trace)
+    served = SkeletonServer(budget_bytes=120e9, exclusive_backlog=-1).serve(trace)
     assert len(served) == len(trace)
     for r in served:
         q = plain[r.rid]

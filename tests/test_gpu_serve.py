@@ -30,12 +30,32 @@ def test_batched_serving_equals_plain(requests):
 
     trace = poisson_arrivals(requests, rate=400.0)
     plain = by_rid(serve_plain(trace))
-    served = SkeletonServer(budget_bytes=120e9).serve(trace)
+    # exclusive_backlog=-1: every request goes to the concurrent engines
+    served = SkeletonServer(budget_bytes=120e9, exclusive_backlog=-1).serve(trace)
     assert len(served) == len(trace)
     assert max(r.batch for r in served) >= 1
+    assert "exclusive" not in {r.path for r in served}
     for r in served:
         assert_same(r, plain[r.rid])
         assert r.done >= r.admitted >= r.arrival - 1e-9
+
+
+def test_exclusive_without_backlog_then_batching(requests):
+    from dataclasses import replace
+
+    from gpucsl_gb300.serve import SkeletonServer, serve_plain
+
+    # the first request arrives alone (solved exclusively); the rest arrive together
+    # later, a backlog beyond exclusive_backlog, and go to the concurrent engines
+    trace = [replace(r, arrival=0.0 if i == 0 else 0.25) for i, r in enumerate(requests)]
+    plain = by_rid(serve_plain(trace))
+    served = SkeletonServer(budget_bytes=120e9, exclusive_backlog=2).serve(trace)
+    assert len(served) == len(trace)
+    paths = {r.rid: r.path for r in served}
+    assert paths[trace[0].rid] == "exclusive"
+    assert "batched" in paths.values()
+    for r in served:
+        assert_same(r, plain[r.rid])
 
 
 def test_all_at_once_batches_every_gaussian_request(requests):
