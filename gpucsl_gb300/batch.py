@@ -263,6 +263,9 @@ class GaussianBatch:
         """(skeleton uint16, sepsets int32 (p, p, max_level), pmax float64) of instance k."""
         p = self.ps[k]
         n_ints = int(self._inst[k].n_records)
+        if n_ints > self.rec_caps[k]:
+            raise RuntimeError(f"instance {k}: its sepset records ({n_ints} ints) overflowed the record pool "
+                               f"({self.rec_caps[k]} ints); run(sync=True) grows the pools and solves again")
         rec = self.rec[k][:n_ints].cpu().numpy() if n_ints else np.zeros(0, np.int32)
         G = self.G[k].cpu().numpy().view(np.uint16)
         pmax = self.pmax[k].cpu().numpy()

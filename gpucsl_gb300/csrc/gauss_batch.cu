@@ -222,27 +222,28 @@ struct SplitTest {
     double tau, t2;
     float t2lo, t2hi;
     unsigned long long *retests;
-    double eps;  // bound on |C - C_exact|, or a negative value when C is exact
+    double eps;   // bound on |C - C_exact|, or a negative value when C is exact
+    float eps32;  // (float)(eps * 1.001), formed once per edge rather than per test
     int *flag;
     __device__ __forceinline__ TestOut operator()(int vi, int vj, const int *S) const {
-        if (eps < 0.0) {
+        if (eps32 < 0.f) {
             float r2;
             const bool ok = gauss_test_f32<L>(C32, p, vi, vj, S, r2);
             if (ok && (r2 < t2lo || r2 > t2hi)) {
                 TestOut o;
-                o.rho2 = (double)r2;
+                o.rho2 = f32_nonneg_to_f64(r2);
                 o.zexact = __longlong_as_double(0x7ff0000000000000ll);
                 o.remove = r2 < t2lo;
                 return o;
             }
             ++*retests;
-            return gauss_test_reg<L>(C, p, vi, vj, S, tau, t2);
+            return gauss_test_reg_call<L>(C, p, vi, vj, S, tau, t2);  // out of line: keeps its registers off this path
         }
         float r, e;
-        const bool ok = gauss_test_bound<L, float>(C32Acc{C32, p}, vi, vj, S, (float)(eps * 1.001), r, e);
+        const bool ok = gauss_test_bound<L, float>(C32Acc{C32, p}, vi, vj, S, eps32, r, e);
         if (ok && (__fadd_ru(r, e) < t2lo || __fsub_rd(r, e) > t2hi)) {
             TestOut o;
-            o.rho2 = (double)r;
+            o.rho2 = f32_nonneg_to_f64(r);
             o.zexact = __longlong_as_double(0x7ff0000000000000ll);
             o.remove = __fadd_ru(r, e) < t2lo;
             return o;
@@ -399,7 +400,7 @@ __global__ void __launch_bounds__(256) batch_level_kernel(const BInst *__restric
             // the rerun has the exact C: no bound
             const double eps = (has && !rerun && I.c_err != nullptr) ? *I.c_err : -1.0;
             walk_edge<L, G>(J, has, I.adj, I.p, gl, gshift, gbits,
-                            SplitTest<L>{I.C, I.C32, I.p, I.tau[L], I.t2[L], I.t2lo[L], I.t2hi[L], &retests, eps,
+                            SplitTest<L>{I.C, I.C32, I.p, I.tau[L], I.t2[L], I.t2lo[L], I.t2hi[L], &retests, eps, (float)(eps * 1.001),
                                          I.flag},
                             I.G, nullptr, BATCH_MAX_LEVEL, I.rec, I.rec_cap, I.st, r2min, zmin_exact, removed,
                             n_tests);

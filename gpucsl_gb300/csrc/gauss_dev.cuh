@@ -448,12 +448,53 @@ __device__ __forceinline__ bool level_active(DevState *st, int level, bool tau_v
     return true;
 }
 
-// Min over the G-lane group (aligned groups of G lanes inside the warp).
+// Minima of the statistics folded into z* (rho^2 and Z: zero or positive, or +inf, never
+// NaN here).  For such values the order of the bit patterns as signed 64-bit integers is
+// the numeric order, so the comparisons run on the integer pipe: GB300's FP64 pipe runs
+// at 1/64 of its FP32 rate, and FP64 minima of every test made it the bound of the
+// batched level kernels.
+__device__ __forceinline__ double min_nonneg(double a, double b) {
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return __longlong_as_double(x < y ? x : y);
+}
+
+// The double of a float that is zero or positive (or +inf), built from its bits on the
+// integer pipe (the conversion instruction runs on the FP64 pipe).
+__device__ __forceinline__ double f32_nonneg_to_f64(float x) {
+    uint32_t u = __float_as_uint(x) & 0x7fffffffu;
+    uint32_t e = u >> 23, m = u & 0x7fffffu;
+    unsigned long long bits;
+    if (e == 255u) {
+        bits = 0x7ff0000000000000ull | ((unsigned long long)m << 29);
+    } else if (e == 0u) {
+        if (m == 0u) {
+            bits = 0ull;
+        } else {  // subnormal: normalise the significand
+            const int lz = __clz((int)m) - 8;  // shifts bit 23 into place
+            m = (m << lz) & 0x7fffffu;
+            bits = ((unsigned long long)(897 - lz) << 52) | ((unsigned long long)m << 29);
+        }
+    } else {
+        bits = ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+    }
+    return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ bool nan_bits(double v) {
+    return (__double_as_longlong(v) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+
+// Min over the G-lane group (aligned groups of G lanes inside the warp) of values as
+// min_nonneg takes them.
 template <int G>
 __device__ __forceinline__ double group_min(double v) {
+    long long b = __double_as_longlong(v);
 #pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(GCSL_FULL_MASK, v, o));
-    return v;
+    for (int o = G / 2; o > 0; o >>= 1) {
+        const long long c = __shfl_xor_sync(GCSL_FULL_MASK, b, o);
+        b = c < b ? c : b;
+    }
+    return __longlong_as_double(b);
 }
 
 // The FP64 test out of line: the mixed kernels call it rarely (guard band, unusable
@@ -652,6 +693,9 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
                                           const BinomRows *sb = nullptr, double r2_floor = 0.0,
                                           WalkRange *rg = nullptr) {
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    // r2_floor rounded up to FP32: a key whose FP32 interval starts above it cannot lower
+    // z* (the rounding only admits a few more candidates), compared in FP32 per step
+    const float floor32 = __double2float_ru(r2_floor);
     long long base = rg ? rg->m0 : 0;
     const long long mend = rg ? rg->m1 : J.T;
     bool done = !has || base >= mend;
@@ -697,7 +741,7 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
             // exact minimum so far (r2_floor, from earlier levels) cannot lower z*
             const float lo32 = __fsub_rd(o.r32, o.e32);
             const float hi = group_min_f<G>((fold && !o.exact) ? __fadd_ru(o.r32, o.e32) : __int_as_float(0x7f800000));
-            bool cand = fold && !o.exact && lo32 <= hi && (double)lo32 <= r2_floor;
+            bool cand = fold && !o.exact && lo32 <= hi && lo32 <= floor32;
             const unsigned cm = __ballot_sync(GCSL_FULL_MASK, cand);
             if (cm) {
                 constexpr int W = CAND_HEADER + L;
@@ -729,18 +773,18 @@ __device__ __forceinline__ void walk_edge(const EdgeJob &J, bool has, const int 
             const bool ex = fold && (o.exact || cand);
             if (__any_sync(GCSL_FULL_MASK, ex)) {
                 const double r2 = group_min<G>(ex ? o.rho2 : inf);
-                const double ze = group_min<G>((ex && !isnan(o.zexact)) ? o.zexact : inf);
+                const double ze = group_min<G>((ex && !nan_bits(o.zexact)) ? o.zexact : inf);
                 if (!done) {
-                    r2min = fmin(r2min, r2);
-                    zmin_exact = fmin(zmin_exact, ze);
+                    r2min = min_nonneg(r2min, r2);
+                    zmin_exact = min_nonneg(zmin_exact, ze);
                 }
             }
         } else {
             const double r2 = group_min<G>(fold ? o.rho2 : inf);
-            const double ze = group_min<G>((fold && !isnan(o.zexact)) ? o.zexact : inf);
+            const double ze = group_min<G>((fold && !nan_bits(o.zexact)) ? o.zexact : inf);
             if (!done) {
-                r2min = fmin(r2min, r2);
-                zmin_exact = fmin(zmin_exact, ze);
+                r2min = min_nonneg(r2min, r2);
+                zmin_exact = min_nonneg(zmin_exact, ze);
             }
         }
         if (!done) {

@@ -25,6 +25,8 @@ def records_to_dense(rec: np.ndarray, n_ints: int, p: int, max_level: int) -> np
     the library's host routine (gcsl_records_to_dense: multi-threaded fill, no GIL)."""
     out = np.empty((p, p, max_level), np.int32)
     rec = np.ascontiguousarray(np.asarray(rec[:n_ints], dtype=np.int32))
+    if rec.size < n_ints:
+        raise ValueError(f"{n_ints} record ints announced, {rec.size} given (an overflowed record pool?)")
     _lib.check(_lib.lib().gcsl_records_to_dense(rec.ctypes.data if n_ints else None, int(n_ints), int(p),
                                                 int(max_level), out.ctypes.data if out.size else None),
                "gcsl_records_to_dense")

@@ -9,6 +9,7 @@ wide   Gaussian p = 5000, n = 2000, degree 3, seed 5, alpha 0.01, levels <= 1: C
        run against HBM
 cfg3   discrete p = 200, n = 50000, cardinality 2..5, degree 2, seed 3, alpha 0.05, levels <= 3
 cfg4   512 uneven Gaussian instances (p 50..400, n 500..20000), split precision, levels <= 4
+       (--instances N: the first N of them)
 orient edge orientation (v-structures and Meek's rules) of the cfg2 skeleton and sepsets
 encode device ordinal encoding of the cfg3 samples (200 int64 columns, n = 50000)
 
@@ -28,6 +29,8 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="cfg2", choices=sorted(list(GAUSS) + ["cfg3", "cfg4", "orient", "encode"]))
     ap.add_argument("--repeat", type=int, default=2)
+    ap.add_argument("--instances", type=int, default=512,
+                    help="cfg4: solve the first N of the 512 instances (smaller cases for profiling)")
     args = ap.parse_args(argv)
 
     import torch
@@ -93,7 +96,7 @@ def main(argv=None):
         from .batch import GaussianBatch
         from .synthetic import batch_instance_sizes
 
-        sizes = batch_instance_sizes(512)
+        sizes = batch_instance_sizes(512)[:max(1, min(512, args.instances))]
         Xs = [gaussian_dag_data_device(p, n, d, s) for (p, n, d, s) in sizes]
         b = GaussianBatch([s[0] for s in sizes], [s[1] for s in sizes], 0.01, 4, "split")
         b.bind_samples(Xs)

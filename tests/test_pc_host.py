@@ -92,6 +92,9 @@ def test_records_to_dense():
     assert out[0, 3].tolist() == [2, -1] and out[3, 0].tolist() == [2, -1]
     assert (out[2, 3] == -1).all()
     assert int((out >= 0).sum()) == 6
+    # more record ints announced than given (an overflowed pool): refused, never read past
+    with pytest.raises(ValueError):
+        engine.records_to_dense(rec[:9], 15, 5, 2)
 
 
 def _dense_by_loop(rec, n_ints, p, max_level):
