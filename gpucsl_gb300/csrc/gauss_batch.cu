@@ -369,8 +369,12 @@ __global__ void batch_edge_offsets_kernel(const long long *__restrict__ edges, i
     block_scan_rows(edges, count, off);
 }
 
+// Levels 1 and 2 (most of a batch's tests) run at three 256-thread blocks per SM: their
+// FP32 tests need few registers, and the 24 resident warps hide more of the gathers'
+// latency than the 16 that the register count of their rare FP64 re-test path allowed
+// (a few spilled values of that path stay in L1).  Higher levels keep their registers.
 template <int L, int G, bool SPLIT>
-__global__ void __launch_bounds__(256) batch_level_kernel(const BInst *__restrict__ inst,
+__global__ void __launch_bounds__(256, (L <= 2 ? 3 : 1)) batch_level_kernel(const BInst *__restrict__ inst,
                                                          const long long *__restrict__ edge_off, int count,
                                                          bool rerun) {
     constexpr int GPW = 32 / G;
