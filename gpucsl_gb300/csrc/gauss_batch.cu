@@ -223,7 +223,7 @@ struct SplitTest {
     float t2lo, t2hi;
     unsigned long long *retests;
     double eps;   // bound on |C - C_exact|, or a negative value when C is exact
-    float eps32;  // (float)(eps * 1.001), formed once per edge rather than per test
+    float eps32;  // eps * 1.001 rounded up to FP32, formed once per edge rather than per test
     int *flag;
     __device__ __forceinline__ TestOut operator()(int vi, int vj, const int *S) const {
         if (eps32 < 0.f) {
@@ -403,8 +403,10 @@ __global__ void __launch_bounds__(256, (L <= 2 ? 3 : 1)) batch_level_kernel(cons
         if constexpr (SPLIT) {
             // the rerun has the exact C: no bound
             const double eps = (has && !rerun && I.c_err != nullptr) ? *I.c_err : -1.0;
+            // eps widened by 0.1 % in FP32, rounded up (no FP64 instruction per edge)
+            const float eps32 = __fmul_ru(f64_nonneg_to_f32_ru(eps), 1.001f);
             walk_edge<L, G>(J, has, I.adj, I.p, gl, gshift, gbits,
-                            SplitTest<L>{I.C, I.C32, I.p, I.tau[L], I.t2[L], I.t2lo[L], I.t2hi[L], &retests, eps, (float)(eps * 1.001),
+                            SplitTest<L>{I.C, I.C32, I.p, I.tau[L], I.t2[L], I.t2lo[L], I.t2hi[L], &retests, eps, eps32,
                                          I.flag},
                             I.G, nullptr, BATCH_MAX_LEVEL, I.rec, I.rec_cap, I.st, r2min, zmin_exact, removed,
                             n_tests);
@@ -415,8 +417,10 @@ __global__ void __launch_bounds__(256, (L <= 2 ? 3 : 1)) batch_level_kernel(cons
         if (SPLIT && retests) atomicAdd(&I.st->retests, retests);
         if (has && gl == 0 && J.T > 0) {
             const size_t ix = (size_t)J.lo * I.p + J.hi;
-            if (zmin_exact < inf) I.zmin[ix] = fmin(I.zmin[ix], zmin_exact);
-            if (r2min < inf) I.r2min[ix] = fmin(I.r2min[ix], r2min);
+            // both non-negative for a pair alive at this level (integer compares, as in walk_edge)
+            if (__double_as_longlong(zmin_exact) < __double_as_longlong(inf))
+                I.zmin[ix] = min_nonneg(I.zmin[ix], zmin_exact);
+            if (__double_as_longlong(r2min) < __double_as_longlong(inf)) I.r2min[ix] = min_nonneg(I.r2min[ix], r2min);
             atomicAdd(&I.st->tests[L], n_tests);
             atomicAdd(&I.st->tests_full[L], (unsigned long long)J.T);
             if (removed) atomicAdd(&I.st->removed[L], 1ull);

@@ -480,6 +480,20 @@ __device__ __forceinline__ double f32_nonneg_to_f64(float x) {
     return __longlong_as_double((long long)bits);
 }
 
+// A double that is zero or positive rounded up to FP32 from its bits (negative values
+// give -1): the bound eps of a split-precision C, widened rather than rounded.
+__device__ __forceinline__ float f64_nonneg_to_f32_ru(double v) {
+    const long long b = __double_as_longlong(v);
+    if (b < 0) return -1.0f;
+    if (b == 0) return 0.0f;
+    const int e = (int)(b >> 52);  // biased exponent
+    if (e < 1023 - 126) return __int_as_float(0x00800000);  // below FP32's normal range: 2^-126
+    if (e > 1023 + 127) return __int_as_float(0x7f800000);
+    unsigned fb = ((unsigned)(e - 1023 + 127) << 23) | (unsigned)((b >> 29) & 0x7fffff);
+    if (b & ((1ll << 29) - 1)) ++fb;  // round up (a carry moves into the exponent)
+    return __uint_as_float(fb);
+}
+
 __device__ __forceinline__ bool nan_bits(double v) {
     return (__double_as_longlong(v) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
 }

@@ -24,7 +24,7 @@ the head waits rather than being overtaken).
 * Finished requests are turned into the reference's output arrays (dense sepsets by the
   library's host routine, outside the GIL) by a pool of finishing threads.
 * Without a backlog the batching is skipped: while nothing is in flight concurrently
-  and at most `exclusive_backlog` (4) requests wait, the request at the head of the
+  and at most `exclusive_backlog` (8) requests wait, the request at the head of the
   queue is solved alone on the whole device through the single-problem path, by the
   dispatching thread on its current stream, exactly as the plain path does, and the
   next one waits for it.
@@ -227,7 +227,7 @@ class SkeletonServer:
 
     def __init__(self, budget_bytes: float = 120e9, discrete_workers: int = 3, finishing_threads: int = 4,
                  max_inflight_ticks: int = 2, solo_p: int = 400, solo_workers: int = 2,
-                 discrete_blocks_per_sm: int = 1, exclusive_backlog: int = 4, switch_interval: float = 5e-4):
+                 discrete_blocks_per_sm: int = 1, exclusive_backlog: int = 8, switch_interval: float = 5e-4):
         self.budget = int(budget_bytes)
         # waiting requests up to which the head of the queue is solved alone (negative:
         # never, every request goes to the concurrent engines)
@@ -511,6 +511,20 @@ class SkeletonServer:
             def submit(self_, fn, *a):
                 return finisher.submit(fin_guard, fn, *a)
 
+        # requests solved alone whose host part is still pending: at most two per
+        # finishing thread, so the host work cannot fall behind without bound
+        host_slots = threading.BoundedSemaphore(2 * self.finishing_threads)
+
+        def finish_alone(r, fin, adm_t):
+            try:
+                G, sep, pm = fin()
+                out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, adm_t, clock() - t0, path="exclusive"))
+            except BaseException as e:  # surfaced by serve()
+                errors.append(e)
+                stop[0] = True
+            finally:
+                host_slots.release()
+
         wg = threading.Thread(target=self._guard, args=(self._gaussian_engine, errors, stop, qg, cvg, stop, adm, out,
                                                         t0, clock, _Fin(), qs, cvs), daemon=True)
         wss = [threading.Thread(target=self._guard, args=(self._solo_worker, errors, stop, qs, cvs, stop, adm, out,
@@ -520,10 +534,19 @@ class SkeletonServer:
                                                           out, t0, clock, i), daemon=True)
                for i in range(self.discrete_workers)]
         workers = [wg] + wss + wds
+        # the engines' threads (and the short switch interval they need) exist only from
+        # the first request that goes to them: while every request is solved alone, no
+        # other thread of the server shares the interpreter with the solving one
         old_switch = sys.getswitchinterval()
-        sys.setswitchinterval(self.switch_interval)
-        for w in workers:
-            w.start()
+        started = [False]
+
+        def start_engines():
+            if not started[0]:
+                started[0] = True
+                sys.setswitchinterval(self.switch_interval)
+                for w in workers:
+                    w.start()
+
         pending = deque(sorted(trace, key=lambda r: r.arrival))
         waiting: deque = deque()  # arrived, not admitted (FIFO)
         try:
@@ -538,12 +561,16 @@ class SkeletonServer:
                     # no backlog and nothing in flight: the head is solved alone, here, on
                     # this thread's current stream (what the plain path does); arrivals
                     # meanwhile queue up behind it
+                    # the host part (copies out, dense sepsets) of each such request is
+                    # finished on a finishing thread while the next one is solved
                     r = waiting.popleft()
                     adm_t = clock() - t0
-                    G, sep, pm = solve_plain(r)
-                    out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, adm_t, clock() - t0, path="exclusive"))
+                    host_slots.acquire()
+                    fin = start_plain(r)
+                    finisher.submit(finish_alone, r, fin, adm_t)
                     continue
-                else:
+                elif waiting:
+                    start_engines()
                     while waiting:
                         r = waiting[0]
                         nbytes = footprint(r)
@@ -557,7 +584,7 @@ class SkeletonServer:
                             q.append(item)
                             cv.notify()
                 # sleep until the next arrival, or until a request finishes when some wait
-                # (for the exclusive worker or for budget)
+                # (for budget)
                 until_next = pending[0].arrival - (clock() - t0) if pending else 0.05
                 flow.wait(seen, min(until_next, 0.05) if waiting else until_next)
         finally:
@@ -565,8 +592,9 @@ class SkeletonServer:
             for cv in (cvg, cvd, cvs):
                 with cv:
                     cv.notify_all()
-            for w in workers:
-                w.join()
+            if started[0]:
+                for w in workers:
+                    w.join()
             finisher.shutdown(wait=True)
             sys.setswitchinterval(old_switch)
         if errors:
@@ -590,6 +618,48 @@ def solve_plain(r: Request):
     ds.load(codes_dev=codes, dims_dev=dims)
     ds.run(r.alpha)
     return ds.to_host()
+
+
+def start_plain(r: Request):
+    """The device part of `solve_plain` on the current stream: the solve, then copies of
+    its results into a pinned staging buffer.  Returns a function that finishes the
+    request on the host (waits for the copies; skeleton, dense sepsets and pmax as
+    `solve_plain` returns them), so that a caller can run it on another thread while the
+    next request's solve proceeds."""
+    torch = _lib.require_cuda()
+    if r.kind == "gaussian":
+        X = r.samples.to("cuda", non_blocking=True)
+        s = GaussianSolver(r.p, r.max_level)
+        s.run(correlation(X), r.n, gaussian_thresholds(r.n, r.alpha))
+    else:
+        s = DiscreteSolver(r.p, r.n, r.max_level, int(r.dims.max()))
+        codes = r.codes.to("cuda", non_blocking=True)
+        dims = torch.from_numpy(np.ascontiguousarray(r.dims, dtype=np.uint8)).to("cuda", non_blocking=True)
+        s.load(codes_dev=codes, dims_dev=dims)
+        s.run(r.alpha)
+    p, n_rec = r.p, int(s.stats.n_records)
+    pp = p * p
+    # staging layout: pmax (8 p^2 bytes), records, G (2 p^2): every part starts at a
+    # multiple of its element size
+    buf = _PINNED.get(8 * pp + 4 * n_rec + 2 * pp)
+    buf[:8 * pp].view(torch.float64).copy_(s.pmax.view(-1), non_blocking=True)
+    if n_rec:
+        buf[8 * pp:8 * pp + 4 * n_rec].view(torch.int32).copy_(s.rec[:n_rec], non_blocking=True)
+    buf[8 * pp + 4 * n_rec:10 * pp + 4 * n_rec].view(torch.int16).copy_(s.G.view(-1), non_blocking=True)
+    done = torch.cuda.Event()
+    done.record()
+
+    def finish():
+        done.synchronize()
+        h = buf.numpy()
+        pm = h[:8 * pp].view(np.float64).reshape(p, p).copy()
+        sep = records_to_dense(h[8 * pp:8 * pp + 4 * n_rec].view(np.int32), n_rec, p, r.max_level)
+        G = h[8 * pp + 4 * n_rec:10 * pp + 4 * n_rec].view(np.uint16).reshape(p, p).copy()
+        _PINNED.put(buf)
+        return G, sep, pm
+
+    finish.solver = s  # the device buffers stay alive until the copies have run
+    return finish
 
 
 def serve_plain(trace: list[Request], clock=time.perf_counter) -> list[Response]:
