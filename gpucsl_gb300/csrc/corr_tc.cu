@@ -29,9 +29,12 @@
 // kernel writes eps per instance.  Instances whose tests cannot be decided exactly with
 // C' are flagged by the level loop and get the seven-digit product afterwards (the split
 // run writes five digit planes; the flagged jobs' seven are written by that later run).
+#include <cstring>
 #include <mutex>
 #include <type_traits>
 #include <vector>
+
+#include <cuda.h>
 
 #include "common.cuh"
 #include "tc.cuh"
@@ -438,6 +441,17 @@ __device__ __forceinline__ void bulk_g2s(void *smem_dst, const void *gmem_src, u
                  : "memory");
 }
 
+// One tensor copy of a box of the digit planes (a 5-D tensor map, see
+// digit_tensor_maps) into shared memory, completing on the mbarrier.
+__device__ __forceinline__ void tma_g2s_5d(void *smem_dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                           int c4, uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+        "%6}], [%7];" ::"r"(tc::smem_u32(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(tc::smem_u32(mbar))
+        : "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(mbar)) : "memory");
 }
@@ -471,8 +485,9 @@ constexpr int OZ_THREADS = (OZ_DRAIN_WARPS + 2) * 32;    // + producer warp + MM
 // copies; warp 17 (lane 0) issues the tensor-core MMAs.  They synchronise only through
 // mbarriers: full (copy landed), empty (MMAs done reading a stage), chunk (MMAs of a
 // chunk done), drained (TMEM read, accumulators may be overwritten).
-template <class Src, int NS>
-__global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
+template <class Src, int NS, bool TMAP>
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    corr_ozaki_kernel(Src src, const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b) {
     extern __shared__ __align__(1024) uint8_t smem[];
     constexpr int NST = oz_nst(NS);
     __shared__ __align__(8) uint64_t full_bar[OZ_NST_MAX], empty_bar[OZ_NST_MAX], chunk_bar, drained_bar;
@@ -534,11 +549,20 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) corr_ozaki_kernel(Src src) {
                 uint8_t *sB = sA + oz_a_bytes(NS);
                 mbar_expect_tx(&full_bar[b], (uint32_t)oz_stage_bytes(NS));
                 const long long q = q0 + st;
-                for (int k = 0; k < NS; ++k) {
-                    bulk_g2s(sA + k * 4096, dig + (((size_t)k * nI + I) * nq + q) * 4096, 4096u, &full_bar[b]);
-                    bulk_g2s(sB + k * 2048,
-                             dig + (((size_t)k * nI + (J >> 1)) * nq + q) * 4096 + (size_t)(J & 1) * 2048, 2048u,
-                             &full_bar[b]);
+                if constexpr (TMAP) {
+                    // two tensor copies per step: the NS A blocks (both halves) and the NS B
+                    // halves, each landing digit-major as the loop below lays them out; the
+                    // copy engine's cost is per copy, so 2 instead of 2 NS copies measured
+                    // as fast as no copies at all
+                    tma_g2s_5d(sA, &tm_a, 0, 0, (int)q, I, 0, &full_bar[b]);
+                    tma_g2s_5d(sB, &tm_b, 0, J & 1, (int)q, J >> 1, 0, &full_bar[b]);
+                } else {
+                    for (int k = 0; k < NS; ++k) {
+                        bulk_g2s(sA + k * 4096, dig + (((size_t)k * nI + I) * nq + q) * 4096, 4096u, &full_bar[b]);
+                        bulk_g2s(sB + k * 2048,
+                                 dig + (((size_t)k * nI + (J >> 1)) * nq + q) * 4096 + (size_t)(J & 1) * 2048, 2048u,
+                                 &full_bar[b]);
+                    }
                 }
             }
         }
@@ -878,8 +902,11 @@ template <class Src, int NS>
 static cudaError_t set_ozaki_smem() {
     static std::atomic<bool> done{false};  // per instantiation; the value set is the same for every caller
     if (done.load()) return cudaSuccess;
-    const cudaError_t e = cudaFuncSetAttribute(corr_ozaki_kernel<Src, NS>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, oz_nst(NS) * oz_stage_bytes(NS));
+    cudaError_t e = cudaFuncSetAttribute(corr_ozaki_kernel<Src, NS, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, oz_nst(NS) * oz_stage_bytes(NS));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(corr_ozaki_kernel<Src, NS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 oz_nst(NS) * oz_stage_bytes(NS));
     if (e == cudaSuccess) done.store(true);
     return e;
 }
@@ -935,10 +962,61 @@ static cudaError_t launch_persistent(K kernel, long long total, const Src &src, 
     return launch_stage(kernel, grid, 256, 0, src, s, what, total);
 }
 
+// Tensor maps of a job's digit planes as a 5-D tensor of 8-byte elements: (256 elements =
+// 2 KB half of a 128-row block, 2 halves, nq K steps, nI row blocks, OZ_S planes), and
+// the boxes of one K step: A = NS planes x both halves of block I, B = NS planes x half
+// J & 1 of block J >> 1.  Encoded through the driver entry point (no link to libcuda).
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled_fn() {
+    static EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+static cudaError_t digit_tensor_maps(const OzJob &J, int ns, CUtensorMap &a, CUtensorMap &b) {
+    const EncodeTiledFn enc = encode_tiled_fn();
+    if (enc == nullptr) return note_error("cuTensorMapEncodeTiled entry point", cudaErrorNotSupported);
+    const cuuint64_t nq = (cuuint64_t)(J.D.n_pad / 16), nI = (cuuint64_t)(J.D.p_pad / OZ_TM);
+    const cuuint64_t dims[5] = {256, 2, nq, nI, (cuuint64_t)OZ_S};
+    const cuuint64_t strides[4] = {2048, 4096, nq * 4096, nI * nq * 4096};  // bytes, dims 1..4
+    const cuuint32_t box_a[5] = {256, 2, 1, 1, (cuuint32_t)ns}, box_b[5] = {256, 1, 1, 1, (cuuint32_t)ns};
+    const cuuint32_t unit[5] = {1, 1, 1, 1, 1};
+    for (int m = 0; m < 2; ++m) {
+        const CUresult r = enc(m == 0 ? &a : &b, CU_TENSOR_MAP_DATA_TYPE_UINT64, 5, J.dig, dims, strides,
+                               m == 0 ? box_a : box_b, unit, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return note_error("cuTensorMapEncodeTiled", cudaErrorInvalidValue);
+    }
+    return cudaSuccess;
+}
+
+// A single job's product copies its digits with two tensor copies per K step; a batch's
+// jobs (one tensor map each would have to live in device memory) with 2 NS bulk copies.
 template <class Src, int NS>
 static cudaError_t launch_ozaki(const Src &src, long long blocks, cudaStream_t s) {
-    return launch_stage(corr_ozaki_kernel<Src, NS>, blocks, OZ_THREADS, (size_t)oz_nst(NS) * oz_stage_bytes(NS), src, s,
-                        "corr_ozaki_kernel launch");
+    const size_t smem = (size_t)oz_nst(NS) * oz_stage_bytes(NS);
+    CUtensorMap ta, tb;
+    std::memset(&ta, 0, sizeof(ta));
+    std::memset(&tb, 0, sizeof(tb));
+    if constexpr (std::is_same<Src, OneJob>::value) {
+        const cudaError_t e = digit_tensor_maps(src.job, NS, ta, tb);
+        if (e != cudaSuccess) return e;
+        return launch_stage(corr_ozaki_kernel<Src, NS, true>, blocks, OZ_THREADS, smem, src, s, "corr_ozaki_kernel launch",
+                            ta, tb);
+    } else {
+        return launch_stage(corr_ozaki_kernel<Src, NS, false>, blocks, OZ_THREADS, smem, src, s,
+                            "corr_ozaki_kernel launch", ta, tb);
+    }
 }
 
 // Stage launches shared by the single-job and batched paths; nb[] = blocks per stage.
