@@ -112,6 +112,10 @@ struct JobTable {
     int count;
     double *c_err = nullptr;
     const int *active = nullptr;
+    // per job, in device memory: the tensor maps of its digit planes for the product,
+    // [A, B] with all seven planes then [A, B] with the split product's five (or null:
+    // the product copies with bulk copies)
+    const CUtensorMap *maps = nullptr;
     __device__ __forceinline__ OzJob get(long long b, long long &lb) const {
         const int k = upper_row(off, count, b);
         lb = b - off[k];
@@ -538,6 +542,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         if (lane == 0) {
             // a register copy: the copies' memory clobbers would reload a shared-memory field
             const uint8_t *__restrict__ dig = s_job.dig;
+            // the tensor maps: kernel parameters of a single job, or the job's maps in device
+            // memory (written before the launch; the proxy fence orders their use)
+            const CUtensorMap *map_a = &tm_a, *map_b = &tm_b;
+            if constexpr (TMAP && !std::is_same<Src, OneJob>::value) {
+                map_a = src.maps + 4 * s_job.index + (NS == OZ_S ? 0 : 2);
+                map_b = map_a + 1;
+                asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map_a) : "memory");
+                asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map_b) : "memory");
+            }
+            (void)map_a;
+            (void)map_b;
             for (long long st = 0; st < nst; ++st) {
                 const int b = (int)(st % NST);
                 if (st >= NST && !mbar_wait_fast(&empty_bar[b], (uint32_t)(((st / NST) - 1) & 1))) {
@@ -554,8 +569,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                     // halves, each landing digit-major as the loop below lays them out; the
                     // copy engine's cost is per copy, so 2 instead of 2 NS copies measured
                     // as fast as no copies at all
-                    tma_g2s_5d(sA, &tm_a, 0, 0, (int)q, I, 0, &full_bar[b]);
-                    tma_g2s_5d(sB, &tm_b, 0, J & 1, (int)q, J >> 1, 0, &full_bar[b]);
+                    tma_g2s_5d(sA, map_a, 0, 0, (int)q, I, 0, &full_bar[b]);
+                    tma_g2s_5d(sB, map_b, 0, J & 1, (int)q, J >> 1, 0, &full_bar[b]);
                 } else {
                     for (int k = 0; k < NS; ++k) {
                         bulk_g2s(sA + k * 4096, dig + (((size_t)k * nI + I) * nq + q) * 4096, 4096u, &full_bar[b]);
@@ -1000,8 +1015,8 @@ static cudaError_t digit_tensor_maps(const OzJob &J, int ns, CUtensorMap &a, CUt
     return cudaSuccess;
 }
 
-// A single job's product copies its digits with two tensor copies per K step; a batch's
-// jobs (one tensor map each would have to live in device memory) with 2 NS bulk copies.
+// The product copies its digits with two tensor copies per K step: a single job's maps
+// are kernel parameters, a batch's are in its workspace header (JobTable::maps).
 template <class Src, int NS>
 static cudaError_t launch_ozaki(const Src &src, long long blocks, cudaStream_t s) {
     const size_t smem = (size_t)oz_nst(NS) * oz_stage_bytes(NS);
@@ -1014,6 +1029,9 @@ static cudaError_t launch_ozaki(const Src &src, long long blocks, cudaStream_t s
         return launch_stage(corr_ozaki_kernel<Src, NS, true>, blocks, OZ_THREADS, smem, src, s, "corr_ozaki_kernel launch",
                             ta, tb);
     } else {
+        if (src.maps != nullptr)
+            return launch_stage(corr_ozaki_kernel<Src, NS, true>, blocks, OZ_THREADS, smem, src, s,
+                                "corr_ozaki_kernel launch", ta, tb);
         return launch_stage(corr_ozaki_kernel<Src, NS, false>, blocks, OZ_THREADS, smem, src, s,
                             "corr_ozaki_kernel launch", ta, tb);
     }
@@ -1083,11 +1101,16 @@ cudaError_t corr_tc(const void *X, int dtype, long long n, int p, long long ldx,
 }
 
 // ------------------------------------------------------------------ batches
-// Workspace: [job table | stage offsets (OZ_NSTAGES x (count + 1)) | job slices].  The
+// Workspace: [job table | stage offsets (OZ_NSTAGES x (count + 1)) | tensor maps | job
+// slices].  The
 // plan (host) keeps the block totals per stage so the run needs no device reads.
-static size_t batch_header_bytes(int count) {
+static size_t batch_maps_offset(int count) {
     const size_t a = ((size_t)count * sizeof(OzJob) + 255) / 256 * 256;
     return a + ((size_t)OZ_NSTAGES * (count + 1) * sizeof(long long) + 255) / 256 * 256;
+}
+// [job table | stage offsets | 4 tensor maps per job]
+static size_t batch_header_bytes(int count) {
+    return batch_maps_offset(count) + ((size_t)count * 4 * sizeof(CUtensorMap) + 255) / 256 * 256;
 }
 
 size_t corr_tc_batch_workspace_bytes(const long long *n, const int *p, int count) {
@@ -1119,10 +1142,22 @@ cudaError_t corr_tc_batch_prepare(const void *const *X, const long long *n, cons
             off[(size_t)st * (count + 1) + k + 1] = off[(size_t)st * (count + 1) + k] + nb[st];
     }
     for (int st = 0; st < OZ_NSTAGES; ++st) stage_totals[st] = off[(size_t)st * (count + 1) + count];
+    // per job the tensor maps of its digit planes: [A, B] over seven planes, [A, B] over the
+    // split product's five
+    std::vector<CUtensorMap> maps((size_t)count * 4);
+    for (int k = 0; k < count; ++k) {
+        cudaError_t e = digit_tensor_maps(jobs[(size_t)k], OZ_S, maps[4 * (size_t)k], maps[4 * (size_t)k + 1]);
+        if (e == cudaSuccess)
+            e = digit_tensor_maps(jobs[(size_t)k], OZ_S_SPLIT, maps[4 * (size_t)k + 2], maps[4 * (size_t)k + 3]);
+        if (e != cudaSuccess) return e;
+    }
     const size_t a = ((size_t)count * sizeof(OzJob) + 255) / 256 * 256;
     cudaError_t e = cudaMemcpyAsync(base, jobs.data(), (size_t)count * sizeof(OzJob), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(base + a, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(base + batch_maps_offset(count), maps.data(), maps.size() * sizeof(CUtensorMap),
+                            cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host vectors die with this call
     return e;
 }
@@ -1144,10 +1179,12 @@ cudaError_t corr_tc_batch_run_mode(void *ws, int count, const long long *stage_t
     // one JobTable per stage (the offsets differ); the stage launchers take the table of
     // their first kernel, so launch stage by stage
     JobTable t[OZ_NSTAGES];
+    const CUtensorMap *maps = reinterpret_cast<const CUtensorMap *>(base + batch_maps_offset(count));
     for (int st = 0; st < OZ_NSTAGES; ++st) {
         t[st] = JobTable{jobs, off + (size_t)st * (count + 1), count};
         t[st].c_err = mode == CORR_BATCH_SPLIT ? c_err : nullptr;
         t[st].active = mode == CORR_BATCH_FLAGGED ? active : nullptr;
+        t[st].maps = maps;
     }
     cudaError_t e;
     if (mode == CORR_BATCH_FLAGGED) {
