@@ -276,35 +276,58 @@ __global__ void col_mean_exp_kernel(Src src) {
 // 16-sample K step q, a 4 KB block in the canonical no-swizzle K-major layout
 // (byte ((k * nI + I) * nq + q) * 4096 + kmajor_offset(row % 128, sample % 16)), zero
 // padded to (p_pad, n_pad).  A 64-row operand tile is the first or second 2 KB half of a
-// block.  One CTA handles 32 samples x 32 columns.  Only the first NW digit planes are
-// written (the split-precision product reads five; the exact one seven).
-template <typename T, int NW, bool PRELOAD = false>
-__device__ __forceinline__ void digit_split_block(const OzJob &Jb, long long lb, int16_t (*tile)[32][33]) {
+// block.  Only the first NW digit planes are written (the split-precision product reads
+// five; the exact one seven).
+//
+// One block covers 32 columns x 64 samples: lane = column, warp = group of 8 consecutive
+// samples, so a thread owns one 16-byte row of a core matrix per digit (8 samples of one
+// column).  It loads its 8 samples (each load a coalesced row of 32 columns), splits
+// them, packs each digit's 8 BF16 values and stores the 16 bytes: no shared memory and
+// no barrier.
+constexpr int OZ_DIG_SAMPLES = 64;  // samples per digit-split block
+
+// digit-split blocks of a job: 64-sample strips x 32-column strips
+__host__ __device__ inline long long oz_digit_blocks(const OzDims &D) {
+    return (long long)((D.n_pad + OZ_DIG_SAMPLES - 1) / OZ_DIG_SAMPLES) * (D.p_pad / 32);
+}
+
+template <typename T, int NW>
+__device__ __forceinline__ void digit_split_block(const OzJob &Jb, long long lb) {
     const T *__restrict__ X = static_cast<const T *>(Jb.X);
     const long long n = Jb.n, ldx = Jb.ldx;
     const int p = Jb.p, p_pad = Jb.D.p_pad;
     const long long n_pad = Jb.D.n_pad;
-    const double *__restrict__ mean = Jb.mean;
-    const int *__restrict__ expo = Jb.expo;
-    uint8_t *__restrict__ dig = Jb.dig;
-    const long long nbx = n_pad / 32;
-    const long long t0 = (lb % nbx) * 32;
-    const int j0 = (int)(lb / nbx) * 32;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 warps
-    const int j = j0 + tx;
-    // digits of the sample in row r (x: the sample when in range) into the tile
-    auto split_row = [&](int r, double x) {
-        const long long t = t0 + r;
+    const long long ntx = (n_pad + OZ_DIG_SAMPLES - 1) / OZ_DIG_SAMPLES;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;  // 8 warps
+    const long long tg = (lb % ntx) * OZ_DIG_SAMPLES + 8 * w;  // the thread's first sample
+    const int j = (int)(lb / ntx) * 32 + lane;
+    if (tg >= n_pad) return;  // the last block of a column strip may cover only 32 samples (uniform per warp)
+    const bool col = j < p;
+    const double mu = col ? Jb.mean[j] : 0.0;
+    const int ej = col ? Jb.expo[j] : 0;
+    double x[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        const long long t = tg + e;
+        x[e] = (col && t < n) ? (double)X[t * ldx + j] : 0.0;
+    }
+    uint32_t wds[OZ_S][4];
+#pragma unroll
+    for (int k = 0; k < OZ_S; ++k)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) wds[k][q] = 0u;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
         long long I = 0;
-        if (t < n && j < p) {
+        if (col && tg + e < n) {
             // y = fl(x - mean) as numpy centres; I = round(|y| 2^(49 - E)) with the sign of y,
             // from the bits of y: |y| = m 2^(ey - 1075), so I = round(m 2^(ey - 1075 + 49 - E)).
-            const double y = x - mean[j];
+            const double y = x[e] - mu;
             const long long bits = __double_as_longlong(y);
             const int ey = (int)((bits >> 52) & 0x7ff);
             long long m = bits & 0xfffffffffffffll;
             if (ey != 0) m |= 1ll << 52;
-            const int sh = 1075 - (ey != 0 ? ey : 1) - 49 + expo[j];  // right shift, >= 4 since |y| < 2^E
+            const int sh = 1075 - (ey != 0 ? ey : 1) - 49 + ej;  // right shift, >= 4 since |y| < 2^E
             long long mag = 0;
             if (sh < 63) mag = (m + (1ll << (sh - 1))) >> sh;
             I = bits < 0 ? -mag : mag;
@@ -314,80 +337,55 @@ __device__ __forceinline__ void digit_split_block(const OzJob &Jb, long long lb,
         // 2^42, 2^35, 2^28) round at 2^41, 2^34, 2^27, all above Lo, so they follow from
         // H alone: d = floor((H + 2^(s-1)) / 2^s) for s = 21, 14, 7 with H reduced after
         // each; the remainder H 2^21 + Lo is then below 2^27 in magnitude
+        int d[OZ_S];
         int hi = (int)(I >> 21);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const int sh = 7 * (2 - k) + 7;  // 21, 14, 7
-            const int d = (hi + (1 << (sh - 1))) >> sh;
-            hi -= d * (1 << sh);
-            tile[k][r][tx] = (int16_t)d;
+            d[k] = (hi + (1 << (sh - 1))) >> sh;
+            hi -= d[k] * (1 << sh);
         }
         int rem32 = hi * (1 << 21) + (int)(I & 0x1fffff);
 #pragma unroll
         for (int k = 3; k < OZ_S - 1; ++k) {
             const int sh = 7 * (OZ_S - 1 - k);
-            const int d = (rem32 + (1 << (sh - 1))) >> sh;
-            rem32 -= d * (1 << sh);
-            tile[k][r][tx] = (int16_t)d;
+            d[k] = (rem32 + (1 << (sh - 1))) >> sh;
+            rem32 -= d[k] * (1 << sh);
         }
-        tile[OZ_S - 1][r][tx] = (int16_t)rem32;
-    };
-    auto sample = [&](int r) -> double {
-        const long long t = t0 + r;
-        return (t < n && j < p) ? (double)X[t * ldx + j] : 0.0;
-    };
-    if constexpr (PRELOAD) {
-        // the thread's four samples are loaded before any is split: the persistent batch
-        // kernel walks its blocks one after another, and nothing else hides their latency
-        double xv[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) xv[i] = sample(ty + 8 * i);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) split_row(ty + 8 * i, xv[i]);
-    } else {
-        for (int r = ty; r < 32; r += 8) split_row(r, sample(r));
-    }
-    __syncthreads();
-    const int nI = p_pad / OZ_TM;
-    const long long nq = n_pad / 16;
-    // 16-byte chunks: (digit k, column c, 8-sample group g8 in 0..3)
-    for (int w = threadIdx.x; w < NW * 32 * 4; w += blockDim.x) {
-        const int k = w / 128, c = (w / 4) % 32, g8 = w % 4;
-        const int j = j0 + c;
-        const long long t = t0 + g8 * 8;
-        if (j >= p_pad || t >= n_pad) continue;
+        d[OZ_S - 1] = rem32;
         // small integers to float exactly by the 1.5 * 2^23 offset (an integer add and an
         // FP32 subtraction); a digit (|d| <= 128) has at most 8 significant bits, so the
         // upper half of its float is the exact BF16
-        uint32_t word[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const float lo = __int_as_float(0x4B400000 + (int)tile[k][g8 * 8 + 2 * e][c]) - 12582912.0f;
-            const float hi = __int_as_float(0x4B400000 + (int)tile[k][g8 * 8 + 2 * e + 1][c]) - 12582912.0f;
-            word[e] = (__float_as_uint(lo) >> 16) | (__float_as_uint(hi) & 0xffff0000u);
+        for (int k = 0; k < NW; ++k) {
+            const uint32_t b16 = __float_as_uint(__int_as_float(0x4B400000 + d[k]) - 12582912.0f) >> 16;
+            wds[k][e >> 1] |= b16 << (16 * (e & 1));
         }
-        const long long q = t / 16;
-        const size_t off = (((size_t)k * nI + j / OZ_TM) * nq + q) * 4096 +
-                           tc::kmajor_offset((uint32_t)(j % OZ_TM), (uint32_t)(t % 16));
-        *reinterpret_cast<uint4 *>(dig + off) = make_uint4(word[0], word[1], word[2], word[3]);
+    }
+    const int nI = p_pad / OZ_TM;
+    const long long nq = n_pad / 16;
+    uint8_t *__restrict__ dig = Jb.dig;
+    const size_t roff = tc::kmajor_offset((uint32_t)(j % OZ_TM), (uint32_t)(tg % 16));
+#pragma unroll
+    for (int k = 0; k < NW; ++k) {
+        const size_t off = (((size_t)k * nI + j / OZ_TM) * nq + tg / 16) * 4096 + roff;
+        *reinterpret_cast<uint4 *>(dig + off) = make_uint4(wds[k][0], wds[k][1], wds[k][2], wds[k][3]);
     }
 }
 
 template <typename T, class Src, int NW = OZ_S>
-__global__ void digit_split_kernel(Src src, long long total) {
-    __shared__ int16_t tile[OZ_S][32][33];  // [digit][sample][column]; the top digit reaches 128
+__global__ void __launch_bounds__(256) digit_split_kernel(Src src, long long total) {
     pdl_wait();
     pdl_trigger();
     if constexpr (std::is_same<Src, OneJob>::value) {
         (void)total;
-        digit_split_block<T, NW>(src.job, blockIdx.x, tile);
+        digit_split_block<T, NW>(src.job, blockIdx.x);
     } else {
         __shared__ OzJob s_job;
         __shared__ long long s_rng[2];
         stage_blocks(src, total, s_job, s_rng, [&](const OzJob &J, long long lb) {
             if (src.skip(J.index)) return;  // not selected in this run (uniform over the block)
-            digit_split_block<T, NW, true>(J, lb, tile);
-            __syncthreads();  // the tile is reused by the next block of the range
+            digit_split_block<T, NW>(J, lb);
         });
     }
 }
@@ -397,15 +395,11 @@ __global__ void digit_split_kernel(Src src, long long total) {
 // only find their job unflagged).
 template <typename T>
 __global__ void digit_split_flagged_kernel(const OzJob *__restrict__ jobs, int count, const int *__restrict__ active) {
-    __shared__ int16_t tile[OZ_S][32][33];
     for (int k = 0; k < count; ++k) {
         if (active[k] == 0) continue;  // uniform over the block
         const OzJob J = jobs[k];
-        const long long nb = (long long)(J.D.n_pad / 32) * (J.D.p_pad / 32);
-        for (long long lb = blockIdx.x; lb < nb; lb += gridDim.x) {
-            digit_split_block<T, OZ_S>(J, lb, tile);
-            __syncthreads();  // the tile is reused by the next block index
-        }
+        const long long nb = oz_digit_blocks(J.D);
+        for (long long lb = blockIdx.x; lb < nb; lb += gridDim.x) digit_split_block<T, OZ_S>(J, lb);
     }
 }
 
@@ -901,7 +895,7 @@ static void oz_stage_blocks(const OzJob &J, long long *nb) {
     nb[OZ_INIT] = (J.p + 255) / 256;
     nb[OZ_STATS] = (long long)((J.p + 31) / 32) * J.chunks;
     nb[OZ_MEAN] = (J.p + 255) / 256;
-    nb[OZ_DIGITS] = (long long)(J.D.n_pad / 32) * (J.D.p_pad / 32);
+    nb[OZ_DIGITS] = oz_digit_blocks(J.D);
     nb[OZ_PRODUCT] = (long long)J.tiles * J.D.splits;
     nb[OZ_DIAG] = (J.p + 255) / 256;
     const long long tb = (J.p + 31) / 32;
