@@ -227,8 +227,13 @@ class SkeletonServer:
 
     def __init__(self, budget_bytes: float = 120e9, discrete_workers: int = 3, finishing_threads: int = 4,
                  max_inflight_ticks: int = 2, solo_p: int = 400, solo_workers: int = 2,
-                 discrete_blocks_per_sm: int = 1, exclusive_backlog: int = 8, switch_interval: float = 5e-4):
+                 discrete_blocks_per_sm: int = 1, exclusive_backlog: int = 8, switch_interval: float = 5e-4,
+                 overlap_host: bool = True):
         self.budget = int(budget_bytes)
+        # requests solved alone: their host part (copies out, dense sepsets) runs on a
+        # finishing thread while the next request is solved (False: inline, as the plain
+        # path does)
+        self.overlap_host = bool(overlap_host)
         # waiting requests up to which the head of the queue is solved alone (negative:
         # never, every request goes to the concurrent engines)
         self.exclusive_backlog = int(exclusive_backlog)
@@ -565,9 +570,14 @@ class SkeletonServer:
                     # finished on a finishing thread while the next one is solved
                     r = waiting.popleft()
                     adm_t = clock() - t0
-                    host_slots.acquire()
-                    fin = start_plain(r)
-                    finisher.submit(finish_alone, r, fin, adm_t)
+                    if self.overlap_host:
+                        host_slots.acquire()
+                        fin = start_plain(r)
+                        finisher.submit(finish_alone, r, fin, adm_t)
+                    else:
+                        G, sep, pm = solve_plain(r)
+                        out.append(Response(r.rid, r.kind, G, sep, pm, r.arrival, adm_t, clock() - t0,
+                                            path="exclusive"))
                     continue
                 elif waiting:
                     start_engines()
