@@ -27,7 +27,8 @@ the head waits rather than being overtaken).
   and at most `exclusive_backlog` (8) requests wait, the request at the head of the
   queue is solved alone on the whole device through the single-problem path, by the
   dispatching thread on its current stream, exactly as the plain path does, and the
-  next one waits for it.
+  next one waits for it (`overlap_host=True` finishes such a request's host part on a
+  finishing thread while the next one is solved).
   Once more requests wait (or concurrent work is still in flight), every waiting request
   goes to the concurrent engines above.  Sharing the device only pays when requests
   queue up; at low load it only slows each request down.
@@ -228,11 +229,12 @@ class SkeletonServer:
     def __init__(self, budget_bytes: float = 120e9, discrete_workers: int = 3, finishing_threads: int = 4,
                  max_inflight_ticks: int = 2, solo_p: int = 400, solo_workers: int = 2,
                  discrete_blocks_per_sm: int = 1, exclusive_backlog: int = 8, switch_interval: float = 5e-4,
-                 overlap_host: bool = True):
+                 overlap_host: bool = False):
         self.budget = int(budget_bytes)
-        # requests solved alone: their host part (copies out, dense sepsets) runs on a
-        # finishing thread while the next request is solved (False: inline, as the plain
-        # path does)
+        # requests solved alone: inline, as the plain path does (True: their host part --
+        # copies out, dense sepsets -- runs on a finishing thread while the next request is
+        # solved; measured no better at p99, the copies and the scatter then compete with
+        # the next solve for the host)
         self.overlap_host = bool(overlap_host)
         # waiting requests up to which the head of the queue is solved alone (negative:
         # never, every request goes to the concurrent engines)
@@ -594,9 +596,13 @@ class SkeletonServer:
                             q.append(item)
                             cv.notify()
                 # sleep until the next arrival, or until a request finishes when some wait
-                # (for budget)
+                # (for budget); while every request has been solved alone, in the plain
+                # path's short slices
                 until_next = pending[0].arrival - (clock() - t0) if pending else 0.05
-                flow.wait(seen, min(until_next, 0.05) if waiting else until_next)
+                if not started[0] and not waiting:
+                    time.sleep(max(0.0, min(0.0005, until_next)))
+                else:
+                    flow.wait(seen, min(until_next, 0.05) if waiting else until_next)
         finally:
             stop[0] = True
             for cv in (cvg, cvd, cvs):

@@ -49,13 +49,15 @@ def test_exclusive_without_backlog_then_batching(requests):
     # later, a backlog beyond exclusive_backlog, and go to the concurrent engines
     trace = [replace(r, arrival=0.0 if i == 0 else 0.25) for i, r in enumerate(requests)]
     plain = by_rid(serve_plain(trace))
-    served = SkeletonServer(budget_bytes=120e9, exclusive_backlog=2).serve(trace)
-    assert len(served) == len(trace)
-    paths = {r.rid: r.path for r in served}
-    assert paths[trace[0].rid] == "exclusive"
-    assert "batched" in paths.values()
-    for r in served:
-        assert_same(r, plain[r.rid])
+    # inline host part (default) and host part on a finishing thread
+    for overlap in (False, True):
+        served = SkeletonServer(budget_bytes=120e9, exclusive_backlog=2, overlap_host=overlap).serve(trace)
+        assert len(served) == len(trace)
+        paths = {r.rid: r.path for r in served}
+        assert paths[trace[0].rid] == "exclusive"
+        assert "batched" in paths.values()
+        for r in served:
+            assert_same(r, plain[r.rid])
 
 
 def test_all_at_once_batches_every_gaussian_request(requests):
