@@ -172,37 +172,46 @@ __device__ __forceinline__ void level_unit_phase(const LevelCtx &x, const BinomR
         // neither folds it nor takes its remover
         if (m0 <= __ldcg(&ck.heavy[h].best))
             walk_level_keys<L, MIXED>(J, true, lane, x, r2, ze, rem, unit_tests, sb, H.floor, &rg);
-        int d = 0;
-        if (lane == 0) {
-            if (rg.first < H.T) atomicMin(reinterpret_cast<unsigned long long *>(&ck.heavy[h].best),
-                                          (unsigned long long)rg.first);
-            ck.units[u] = UnitRes{rg.first, r2, ze};
-            __threadfence();
-            d = atomicAdd(&ck.heavy[h].done, 1);
-        }
-        d = __shfl_sync(GCSL_FULL_MASK, d, 0);
-        if (d != H.n_units - 1) continue;
-        // last unit of the edge: combine in key order
-        __threadfence();
         long long R = H.T;
-        for (int k = lane; k < H.n_units; k += 32) {
-            const long long f = __ldcg(&ck.units[H.unit_base + k].first);
-            R = f < R ? f : R;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const long long y = __shfl_xor_sync(GCSL_FULL_MASK, R, o);
-            R = y < R ? y : R;
-        }
         double r2c = inf, zec = inf;
-        for (int k = lane; k < H.n_units; k += 32) {
-            if (H.k0 + (long long)k * 32 <= R) {  // the unit starts at or before the remover
-                r2c = fmin(r2c, __ldcg(&ck.units[H.unit_base + k].r2));
-                zec = fmin(zec, __ldcg(&ck.units[H.unit_base + k].ze));
+        if (H.n_units == 1) {
+            // the edge's only unit (an edge handed over whole with at most 32 keys): nothing
+            // to wait for or combine, so its result is final without the round trip through
+            // the unit records
+            R = rg.first;
+            r2c = min_nonneg(r2, H.r2_0);
+            zec = min_nonneg(ze, H.ze_0);
+        } else {
+            int d = 0;
+            if (lane == 0) {
+                if (rg.first < H.T) atomicMin(reinterpret_cast<unsigned long long *>(&ck.heavy[h].best),
+                                              (unsigned long long)rg.first);
+                ck.units[u] = UnitRes{rg.first, r2, ze};
+                __threadfence();
+                d = atomicAdd(&ck.heavy[h].done, 1);
             }
+            d = __shfl_sync(GCSL_FULL_MASK, d, 0);
+            if (d != H.n_units - 1) continue;
+            // last unit of the edge: combine in key order
+            __threadfence();
+            for (int k = lane; k < H.n_units; k += 32) {
+                const long long f = __ldcg(&ck.units[H.unit_base + k].first);
+                R = f < R ? f : R;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const long long y = __shfl_xor_sync(GCSL_FULL_MASK, R, o);
+                R = y < R ? y : R;
+            }
+            for (int k = lane; k < H.n_units; k += 32) {
+                if (H.k0 + (long long)k * 32 <= R) {  // the unit starts at or before the remover
+                    r2c = fmin(r2c, __ldcg(&ck.units[H.unit_base + k].r2));
+                    zec = fmin(zec, __ldcg(&ck.units[H.unit_base + k].ze));
+                }
+            }
+            r2c = fmin(warp_min(r2c), H.r2_0);
+            zec = fmin(warp_min(zec), H.ze_0);
         }
-        r2c = fmin(warp_min(r2c), H.r2_0);
-        zec = fmin(warp_min(zec), H.ze_0);
         if (lane == 0) {
             ck.chunk_first[h] = R;
             if (R < H.T) {
