@@ -286,6 +286,13 @@ __global__ void col_mean_exp_kernel(Src src) {
 // no barrier.
 constexpr int OZ_DIG_SAMPLES = 64;  // samples per digit-split block
 
+// Two floats as one word of two BF16 values, lo in the low half (the lower address).
+__device__ __forceinline__ uint32_t bf16x2_rn(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
 // digit-split blocks of a job: 64-sample strips x 32-column strips
 __host__ __device__ inline long long oz_digit_blocks(const OzDims &D) {
     return (long long)((D.n_pad + OZ_DIG_SAMPLES - 1) / OZ_DIG_SAMPLES) * (D.p_pad / 32);
@@ -312,10 +319,7 @@ __device__ __forceinline__ void digit_split_block(const OzJob &Jb, long long lb)
         x[e] = (col && t < n) ? (double)X[t * ldx + j] : 0.0;
     }
     uint32_t wds[OZ_S][4];
-#pragma unroll
-    for (int k = 0; k < OZ_S; ++k)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) wds[k][q] = 0u;
+    float fe[OZ_S];  // the digits of the even sample of the current pair
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
         long long I = 0;
@@ -354,12 +358,13 @@ __device__ __forceinline__ void digit_split_block(const OzJob &Jb, long long lb)
         }
         d[OZ_S - 1] = rem32;
         // small integers to float exactly by the 1.5 * 2^23 offset (an integer add and an
-        // FP32 subtraction); a digit (|d| <= 128) has at most 8 significant bits, so the
-        // upper half of its float is the exact BF16
+        // FP32 subtraction); a digit (|d| <= 128) has at most 8 significant bits, so it is
+        // exact in BF16, and two samples' digits become one packed word by one conversion
 #pragma unroll
         for (int k = 0; k < NW; ++k) {
-            const uint32_t b16 = __float_as_uint(__int_as_float(0x4B400000 + d[k]) - 12582912.0f) >> 16;
-            wds[k][e >> 1] |= b16 << (16 * (e & 1));
+            const float f = __int_as_float(0x4B400000 + d[k]) - 12582912.0f;
+            if (e & 1) wds[k][e >> 1] = bf16x2_rn(fe[k], f);
+            else fe[k] = f;
         }
     }
     const int nI = p_pad / OZ_TM;
