@@ -165,7 +165,8 @@ struct HeavyEdge {
     long long best;       // smallest removing key found so far (atomic min; T when none)
     double r2_0, ze_0;    // minima of the first step (no remover there; +inf when k0 = 0)
     double floor;         // the pair's exact rho^2 minimum before the level
-    long long k0;         // first key of the units
+    int k0;               // first key of the units (0 or one step)
+    int degs;             // compacted degrees of lo (low 16 bits) and hi (high 16 bits), p <= 46340
 };
 
 struct UnitRes {

@@ -379,14 +379,15 @@ __device__ __forceinline__ bool load_edge_list(const int *__restrict__ adj, cons
     return J.R0 < GCSL_RANK_LIMIT && J.R1 < GCSL_RANK_LIMIT;
 }
 
-// The job of edge (lo, hi) from the current adjacency lists.
+// The job of edge (lo, hi) from degrees already known (the unit kernel takes them from the
+// chunk record instead of reloading the adjacency rows' counts).
 template <int KMAX>
-__device__ __forceinline__ void edge_job_of(const int *__restrict__ adj, int p, int lo, int hi, int L, EdgeJob &J) {
+__device__ __forceinline__ void edge_job_from(int lo, int hi, int deg_lo, int deg_hi, int L, EdgeJob &J) {
     J.lo = lo;
     J.hi = hi;
-    J.deg_lo = adj[(size_t)lo * p];
-    J.deg_hi = adj[(size_t)hi * p];
-    const int K0 = J.deg_lo - 1, K1 = J.deg_hi - 1;
+    J.deg_lo = deg_lo;
+    J.deg_hi = deg_hi;
+    const int K0 = deg_lo - 1, K1 = deg_hi - 1;
     J.R0 = (K0 >= L) ? binom_fast<KMAX>(K0, L) : 0;
     J.R1 = (K1 >= L) ? binom_fast<KMAX>(K1, L) : 0;
     J.T = J.R0 + J.R1;
@@ -850,7 +851,8 @@ __device__ __forceinline__ bool register_chunked(const EdgeJob &J, int gl, const
             H.r2_0 = r2_0;
             H.ze_0 = ze_0;
             H.floor = floor;
-            H.k0 = k0;
+            H.k0 = (int)k0;
+            H.degs = J.deg_lo | (J.deg_hi << 16);
             ck.heavy[h] = H;
         }
         for (long long k = gl; k < nu; k += G) ck.unit_h[ub + k] = (int)h;

@@ -139,6 +139,7 @@ __device__ __forceinline__ HeavyEdge load_heavy(const HeavyEdge *e) {
     H.ze_0 = __ldcg(&e->ze_0);
     H.floor = __ldcg(&e->floor);
     H.k0 = __ldcg(&e->k0);
+    H.degs = __ldcg(&e->degs);
     return H;
 }
 
@@ -162,7 +163,7 @@ __device__ __forceinline__ void level_unit_phase(const LevelCtx &x, const BinomR
         if (h < 0) continue;
         const HeavyEdge H = load_heavy(ck.heavy + h);
         EdgeJob J;
-        edge_job_of<L>(x.adj, p, H.lo, H.hi, L, J);
+        edge_job_from<L>(H.lo, H.hi, H.degs & 0xffff, H.degs >> 16, L, J);
         const long long m0 = H.k0 + (u - H.unit_base) * 32;
         const long long m1 = m0 + 32 < H.T ? m0 + 32 : H.T;
         WalkRange rg{m0, m1, true, h, H.T};
