@@ -105,12 +105,18 @@ __global__ void __launch_bounds__(256) gauss_level_reg_kernel(LevelCtx x) {
 }
 
 //
-// The units of a level are known only when the level kernel has finished, and most levels
-// chunk few edges or none: blocks check their share after the wait and only blocks with
-// units load the binomial rows (block 0 always stays, as in the level kernel).
+// The units of a level are known only when the level kernel has finished: blocks check
+// their share after the wait; the binomial rows are loaded before it by the blocks that
+// the level's edge count says will have work, after it by any other block with units.
 template <int L, bool MIXED>
 __global__ void __launch_bounds__(256) gauss_level_units_kernel(LevelCtx x) {
     __shared__ BinomRows sb;
+    // blocks that will likely have units load the binomial rows before the wait, while the
+    // level kernel still runs: after a quiet level every edge is handed over as about one
+    // unit, so the level's edge count (written by the recompaction, which completed before
+    // the level kernel released this one) bounds them
+    const bool early = L >= 2 && (long long)blockIdx.x * (blockDim.x >> 5) < (long long)__ldcg(&x.st->edges[L]);
+    if (early) binom_rows_load(sb);
     pdl_wait();
     pdl_trigger();
     if (!level_active(x.st, L, x.tau_valid)) return;
@@ -118,7 +124,7 @@ __global__ void __launch_bounds__(256) gauss_level_units_kernel(LevelCtx x) {
     const long long nu = reserved < x.ck.unit_cap ? reserved : x.ck.unit_cap;
     if ((long long)blockIdx.x * (blockDim.x >> 5) >= nu) return;
     if (L >= 2) {
-        binom_rows_load(sb);
+        if (!early) binom_rows_load(sb);
         __syncthreads();
     }
     level_unit_phase<L, MIXED>(x, L >= 2 ? &sb : nullptr, ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5,

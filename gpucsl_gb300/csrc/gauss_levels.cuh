@@ -166,23 +166,34 @@ __device__ __forceinline__ void level_unit_phase(const LevelCtx &x, const BinomR
         edge_job_from<L>(H.lo, H.hi, H.degs & 0xffff, H.degs >> 16, L, J);
         const long long m0 = H.k0 + (u - H.unit_base) * 32;
         const long long m1 = m0 + 32 < H.T ? m0 + 32 : H.T;
-        WalkRange rg{m0, m1, true, h, H.T};
+        // the edge's only unit (most edges handed over whole have at most 32 keys) walks
+        // like an unchunked edge: its remover, found in key order, is final and is written
+        // by the lane that found it, and its tests are the canonical count; nothing is
+        // deferred to a combine
+        const bool single = H.n_units == 1;
+        WalkRange rg{m0, m1, !single, h, H.T};
         double r2 = inf, ze = inf;
         bool rem = false;
+        unsigned long long own_tests = 0;
         // a unit that starts behind a remover already found cannot matter: the combine
         // neither folds it nor takes its remover
         if (m0 <= __ldcg(&ck.heavy[h].best))
-            walk_level_keys<L, MIXED>(J, true, lane, x, r2, ze, rem, unit_tests, sb, H.floor, &rg);
+            walk_level_keys<L, MIXED>(J, true, lane, x, r2, ze, rem, single ? own_tests : unit_tests, sb, H.floor,
+                                      &rg);
+        if (single) {
+            if (lane == 0) {
+                const size_t ix = (size_t)J.lo * p + J.hi;
+                const double zc = min_nonneg(ze, H.ze_0), rc = min_nonneg(r2, H.r2_0);
+                if (__double_as_longlong(zc) < __double_as_longlong(inf)) atomic_min_nonneg_f64(x.zmin + ix, zc);
+                if (__double_as_longlong(rc) < __double_as_longlong(inf)) atomic_min_nonneg_f64(x.r2min + ix, rc);
+                n_extra += own_tests;
+                n_removed += rem;
+            }
+            continue;
+        }
         long long R = H.T;
         double r2c = inf, zec = inf;
-        if (H.n_units == 1) {
-            // the edge's only unit (an edge handed over whole with at most 32 keys): nothing
-            // to wait for or combine, so its result is final without the round trip through
-            // the unit records
-            R = rg.first;
-            r2c = min_nonneg(r2, H.r2_0);
-            zec = min_nonneg(ze, H.ze_0);
-        } else {
+        {
             int d = 0;
             if (lane == 0) {
                 if (rg.first < H.T) atomicMin(reinterpret_cast<unsigned long long *>(&ck.heavy[h].best),
