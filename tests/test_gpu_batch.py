@@ -137,3 +137,21 @@ def test_record_pool_growth(cuda, workloads):
         assert res[k].n_records <= b.rec_caps[k]
         for x, y in zip(b.to_host(k), ref.to_host(k)):
             assert np.array_equal(x, y), k
+
+
+@pytest.mark.parametrize("p,n", [(1000, 10000), (700, 4321)])
+def test_single_job_k_splits_equal_batch(cuda, p, n):
+    """The single-problem product splits each tile's K steps across CTAs (one wave over
+    the SMs: two splits at p = 1000, four at p = 700), the batched product gives each tile its
+    whole K range in one CTA.  Exact integer sums: the two correlation matrices are
+    identical bit for bit."""
+    from gpucsl_gb300 import engine
+    from gpucsl_gb300.batch import GaussianBatch
+
+    torch = cuda
+    w = gaussian_dag_data(p, n, 3, p + n)
+    X = torch.from_numpy(w.data).cuda()
+    b = GaussianBatch([p], [n], ALPHA, 1, "f64")
+    b.bind_samples([X])
+    b.run(graph=False)
+    assert torch.equal(b.C[0], engine.correlation(X))
