@@ -8,10 +8,11 @@ the head waits rather than being overtaken).
 * Gaussian requests go to one engine thread that owns two CUDA streams.  On the
   correlation stream an admitted request's samples are copied in and its correlation is
   computed at once.  On the level stream the engine advances, tick by tick, every
-  request in flight by one level: requests whose correlation is done start (state
-  reset, level 0 and level 1), the others run their next level, and those past their
-  last level get the pmax write-back and their results copied into pinned host memory.
-  The requests due for the same levels form one batched plan per tick
+  request in flight by one level: first those past their last level get the pmax
+  write-back and their results copied into pinned host memory, with an event that
+  hands them to the finishing threads as soon as it passes; then the requests in
+  progress run their next level; then requests whose correlation is done start (state
+  reset, level 0 and level 1).  The requests due for the same levels form one batched plan per tick
   (gcsl_gauss_batch_prepare_staged / gcsl_gauss_batch_step); each request keeps its
   solve state in its own device slice across ticks, so a request that arrives while
   others are in flight joins at the next tick and a finished one leaves at once.  No
@@ -207,12 +208,13 @@ def _stream(role: str, index: int = 0, priority: int = 0):
 
 
 class _Tick:
-    """One tick of the Gaussian engine in flight: its completion event and what must
-    stay alive until the stream has passed it."""
-    __slots__ = ("event", "keep", "finishing")
+    """One tick of the Gaussian engine in flight: its completion event, what must stay
+    alive until the stream has passed it, and the requests it finishes with the event
+    recorded right after their results were copied out (the tick's first work)."""
+    __slots__ = ("event", "keep", "finishing", "fin_event")
 
-    def __init__(self, event, keep, finishing):
-        self.event, self.keep, self.finishing = event, keep, finishing
+    def __init__(self, event, keep, finishing, fin_event):
+        self.event, self.keep, self.finishing, self.fin_event = event, keep, finishing, fin_event
 
 
 class _GaussJob:
@@ -345,12 +347,16 @@ class SkeletonServer:
                 n_started += 1
                 j.stages["corr_enqueued"] = clock() - t0
                 starting.append(j)
-            # retire the ticks the stream has passed (without waiting)
-            while inflight and inflight[0].event.query():
-                t = inflight.popleft()
-                for j in t.finishing:
-                    j.stages["finish_done_seen"] = clock() - t0
-                    finisher.submit(self._finish_gaussian, j, out, adm, t0, clock)
+            # hand finished requests to the finishing threads as soon as their copies are
+            # done, and retire the ticks the stream has passed (without waiting)
+            for t in inflight:
+                if t.finishing and t.fin_event.query():
+                    for j in t.finishing:
+                        j.stages["finish_done_seen"] = clock() - t0
+                        finisher.submit(self._finish_gaussian, j, out, adm, t0, clock)
+                    t.finishing = []
+            while inflight and not inflight[0].finishing and inflight[0].event.query():
+                inflight.popleft()
             ready = [j for j in starting if j.corr_ev.query()]
             for j in ready:
                 j.stages.setdefault("corr_done_seen", clock() - t0)
@@ -370,6 +376,42 @@ class SkeletonServer:
                 time.sleep(0.0001)
                 continue
             if ready or active:
+                # a tick's order: the requests past their last level first (pmax, results
+                # copied out, an event), so their host part starts without waiting for the
+                # rest of the tick; then the levels of the requests in progress, oldest
+                # levels first; then the first levels of the requests whose correlation
+                # is done
+                fin_ev = None
+                for lv, cap in sorted(groups):
+                    js = groups[(lv, cap)]
+                    if lv <= cap:
+                        continue
+                    st = self._enqueue_group(torch, js, lv, lv - 1, True, level_stream, keep)
+                    with torch.cuda.stream(level_stream):
+                        for i, j in enumerate(js):
+                            j.status = (st, i)
+                            # staging layout: pmax (8 p^2 bytes), records, G (2 p^2): every
+                            # part starts at a multiple of its element size
+                            pp, nr = j.r.p * j.r.p, j.rec.numel()
+                            buf = _PINNED.get(8 * pp + 4 * nr + 2 * pp)
+                            j.host = buf
+                            buf[:8 * pp].view(torch.float64).copy_(j.pmax.view(-1), non_blocking=True)
+                            buf[8 * pp:8 * pp + 4 * nr].view(torch.int32).copy_(j.rec, non_blocking=True)
+                            buf[8 * pp + 4 * nr:10 * pp + 4 * nr].view(torch.int16).copy_(
+                                j.G.view(-1), non_blocking=True)
+                    for j in js:
+                        j.stages["finish_enqueued"] = clock() - t0
+                    finishing += js
+                if finishing:
+                    fin_ev = torch.cuda.Event()
+                    fin_ev.record(level_stream)
+                for lv, cap in sorted(groups):
+                    if lv > cap:
+                        continue
+                    js = groups[(lv, cap)]
+                    self._enqueue_group(torch, js, lv, lv, False, level_stream, keep)
+                    for j in js:
+                        j.next_level = lv + 1
                 for j in ready:
                     level_stream.wait_event(j.corr_ev)  # completed already: orders the stream after it
                 for cap, js in starts.items():  # start: state reset, level 0 and level 1
@@ -377,33 +419,10 @@ class SkeletonServer:
                     for j in js:
                         j.next_level, j.batch = 2, len(js)
                         j.cws = j.X = None  # the correlation is done with them
-                for lv, cap in sorted(groups):
-                    js = groups[(lv, cap)]
-                    if lv > cap:  # past the last level: pmax and results
-                        st = self._enqueue_group(torch, js, lv, lv - 1, True, level_stream, keep)
-                        with torch.cuda.stream(level_stream):
-                            for i, j in enumerate(js):
-                                j.status = (st, i)
-                                # staging layout: pmax (8 p^2 bytes), records, G (2 p^2): every
-                                # part starts at a multiple of its element size
-                                pp, nr = j.r.p * j.r.p, j.rec.numel()
-                                buf = _PINNED.get(8 * pp + 4 * nr + 2 * pp)
-                                j.host = buf
-                                buf[:8 * pp].view(torch.float64).copy_(j.pmax.view(-1), non_blocking=True)
-                                buf[8 * pp:8 * pp + 4 * nr].view(torch.int32).copy_(j.rec, non_blocking=True)
-                                buf[8 * pp + 4 * nr:10 * pp + 4 * nr].view(torch.int16).copy_(
-                                    j.G.view(-1), non_blocking=True)
-                        for j in js:
-                            j.stages["finish_enqueued"] = clock() - t0
-                        finishing += js
-                    else:
-                        self._enqueue_group(torch, js, lv, lv, False, level_stream, keep)
-                        for j in js:
-                            j.next_level = lv + 1
                 active = [j for j in active if j not in finishing] + ready
                 ev = torch.cuda.Event()
                 ev.record(level_stream)
-                inflight.append(_Tick(ev, keep, finishing))
+                inflight.append(_Tick(ev, keep, finishing, fin_ev))
             if not ready and not active and (starting or inflight):
                 time.sleep(0.0002)  # correlations or the last ticks running: nothing to step yet
 
