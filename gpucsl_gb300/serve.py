@@ -12,11 +12,11 @@ the head waits rather than being overtaken).
   write-back and their results copied into pinned host memory, with an event that
   hands them to the finishing threads as soon as it passes; then the requests in
   progress run their next level; then requests whose correlation is done start (state
-  reset, level 0 and level 1).  The requests due for the same levels form one batched plan per tick
-  (gcsl_gauss_batch_prepare_staged / gcsl_gauss_batch_step); each request keeps its
-  solve state in its own device slice across ticks, so a request that arrives while
-  others are in flight joins at the next tick and a finished one leaves at once.  No
-  host read happens between the levels of a request.
+  reset, level 0 and level 1).  The requests due for the same levels form one batched
+  plan per tick (gcsl_gauss_batch_prepare_staged / gcsl_gauss_batch_step); each request
+  keeps its solve state in its own device slice across ticks, so a request that arrives
+  while others are in flight joins at the next tick and a finished one leaves at once.
+  No host read happens between the levels of a request.
 * Gaussian requests with more than `solo_p` (400) variables, which fill the GPU on their
   own, and requests deeper than the batched kernels' 12 levels go to two single-problem
   workers (one stream each) instead.
