@@ -141,7 +141,8 @@ int gcsl_gauss_skeleton(const double *C, int32_t p, int64_t n_obs, const double 
  * capture; a cudaDeviceReset after it is not supported).  The call creates nothing, on
  * a thread's first call or later: no device or pinned host allocation, no stream, no
  * event.  All its kernels run in order on `stream`, and it synchronises `stream` to
- * read the level loop's control words into the calling thread's stack.  Calls share
+ * read the level loop's control words into the calling thread's stack, so the call
+ * cannot be captured into a CUDA graph.  Calls share
  * the array, so calls whose device work overlaps race and must be serialised. */
 #define GCSL_NOALLOC_MAX_P 512
 #define GCSL_NOALLOC_SCRATCH_BYTES 17825792
