@@ -52,8 +52,8 @@ constexpr uint32_t OZ_TMEM_COLS = 512;
 constexpr int oz_a_bytes(int ns) { return ns * OZ_TM * 16 * 2; }
 constexpr int oz_stage_bytes(int ns) { return ns * (OZ_TM + OZ_TN) * 16 * 2; }
 // Shared-memory stages of the copy ring (one K step each): as many as 210 KB hold, so the
-// bulk copies run as far ahead of the MMAs as the SM allows (5 for seven digits, 7 for
-// five).  Four stages left the tensor pipe idle 40 % of the time waiting on copies.
+// copies run as far ahead of the MMAs as the SM allows (5 for seven digits, 7 for five).
+// Four stages measured the same: the copies' latency is not what idles the tensor pipe.
 constexpr int OZ_RING_BYTES = 215040;
 constexpr int OZ_NST_MAX = 8;
 constexpr int oz_nst(int ns) { return OZ_RING_BYTES / oz_stage_bytes(ns) < OZ_NST_MAX ? OZ_RING_BYTES / oz_stage_bytes(ns)
@@ -484,8 +484,9 @@ constexpr int OZ_DRAIN_WARPS = 16;                       // 4 TMEM lane quarters
 constexpr int OZ_THREADS = (OZ_DRAIN_WARPS + 2) * 32;    // + producer warp + MMA warp
 
 // Warp roles: warps 0..15 drain TMEM into 64-bit integer accumulators at every chunk
-// end; warp 16 (lane 0) streams digit blocks into the shared-memory stages with bulk
-// copies; warp 17 (lane 0) issues the tensor-core MMAs.  They synchronise only through
+// end; warp 16 (lane 0) streams digit blocks into the shared-memory stages (two TMA
+// tensor copies per K step, or 2 NS bulk copies for a job without tensor maps); warp 17
+// (lane 0) issues the tensor-core MMAs.  They synchronise only through
 // mbarriers: full (copy landed), empty (MMAs done reading a stage), chunk (MMAs of a
 // chunk done), drained (TMEM read, accumulators may be overwritten).
 template <class Src, int NS, bool TMAP>
