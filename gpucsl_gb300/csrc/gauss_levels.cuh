@@ -143,10 +143,12 @@ __device__ __forceinline__ HeavyEdge load_heavy(const HeavyEdge *e) {
     return H;
 }
 
-// Unit phase: the keys of chunked edges after their first step, one unit (32 keys) per
-// warp; the last unit of an edge to finish combines its units in key order: the smallest
-// removing key is the canonical remover, and z* folds every unit that starts at or before
-// it (up to the unit's own first remover) together with the first step.
+// Unit phase: the keys of chunked edges (all of them for an edge handed over whole, else
+// those after its first step), one unit (32 keys) per warp; an edge's only unit finishes
+// the edge itself; otherwise the last unit of an edge to finish combines its units in
+// key order: the smallest removing key is the canonical remover, and z* folds every unit
+// that starts at or before it (up to the unit's own first remover) together with the
+// first step.
 template <int L, bool MIXED>
 __device__ __forceinline__ void level_unit_phase(const LevelCtx &x, const BinomRows *sb, long long w0, long long nw) {
     DevState *st = x.st;
